@@ -1,0 +1,186 @@
+/* rgr.h — C ABI of the GB300 wavefront path tracer (librgr.so).
+ *
+ * This is the drop-in boundary for the RaccoonGPURender hot path.  Each entry
+ * point replaces one call of the reference host API; the reference interface
+ * it stands in for is cited beside it (paths are relative to the reference
+ * project).  All functions return RGR_OK (0) or a negative status; none throw.
+ * Plain pointers and sizes only.  Host pointers unless a name says "device".
+ *
+ * Threading: a scene is not thread safe while it is being built; a context
+ * may be driven by one host thread at a time (the reference drives each
+ * WavefrontLane from one std::thread, common/wavefront_path_tracing.hpp:1299-1303).
+ */
+#ifndef RGR_H
+#define RGR_H
+#include <stdint.h>
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---------------------------------------------------- */
+#define RGR_OK 0
+#define RGR_E_INVALID (-1)   /* bad argument (the reference printf-skips non-triangle meshes, scene_manager.hpp:343-347) */
+#define RGR_E_CUDA (-2)      /* CUDA runtime error; rgr_last_error() has the text */
+#define RGR_E_OOM (-3)       /* device or host allocation failed */
+#define RGR_E_STATE (-4)     /* call out of order (e.g. render before upload) */
+#define RGR_E_OVERFLOW (-5)  /* a device-side capacity check fired (stack, queue) */
+#define RGR_E_NODEVICE (-6)  /* no CUDA device / CUDA path unavailable */
+
+/* ---- materials (common/material_type.hpp:14-63, kernels/types.cl:73-102) */
+#define RGR_MAT_LAMBERTIAN 1
+#define RGR_MAT_SPECULAR 2
+#define RGR_MAT_DIELECTRIC 3
+#define RGR_MAT_WARD 4
+#define RGR_MAT_HOMOGENEOUS_VOLUME 5
+
+typedef struct rgr_material {
+    int32_t type;          /* RGR_MAT_* */
+    int32_t back_emission; /* Lambertian::BackEmission (stored, unused by the kernels, as in the reference) */
+    float le[3];           /* Lambertian::Le */
+    float r[3];            /* Lambertian::R, Ward::reflectance, HomogeneousVolume::R */
+    float edgetint[3];     /* Ward::edgetint */
+    float alpha;           /* Ward::alpha */
+    float falloff;         /* Ward::falloff */
+    float c;               /* HomogeneousVolume::C */
+} rgr_material;
+
+/* ---- scene (replaces rt::SceneManager, common/scene_manager.hpp:330-672) */
+typedef struct rgr_scene rgr_scene;
+
+typedef struct rgr_bvh_params {
+    int32_t max_leaf_size;   /* primitives per leaf, 1..8 (reference Embree build: maxLeafSize 5) */
+    int32_t sah_bins;        /* binned SAH bins per axis */
+    float traversal_cost;    /* SAH cost of one node visit */
+    float intersect_cost;    /* SAH cost of one primitive test */
+    int32_t max_depth;       /* <= 63: the reference traversal's 64-bit bit stack */
+    int32_t num_threads;     /* host threads for the build (0 = all) */
+} rgr_bvh_params;
+
+typedef struct rgr_scene_info {
+    uint64_t num_triangles, num_spheres, num_vertices;
+    uint64_t num_nodes_stackless;  /* nodes in the reference StacklessBVHNode layout */
+    uint64_t num_inner_nodes;      /* 64-byte inner nodes in the device layout */
+    uint64_t num_leaves;
+    int32_t depth;                 /* tree depth (root = 0) */
+    int32_t sphere_begin;          /* first sphere primitive id */
+    float bounds[6];               /* scene AABB: lower xyz, upper xyz */
+    double sah_cost;
+} rgr_scene_info;
+
+/* reference StacklessBVHNode (common/stackless_bvh.hpp:264-275), 96 bytes */
+typedef struct rgr_stackless_node {
+    float L_lower[4], L_upper[4], R_lower[4], R_upper[4];
+    uint32_t link_parent, link_L, link_R, link_sibling;
+    uint32_t primitive_indices_beg, primitive_indices_end;
+    uint32_t pad[2];
+} rgr_stackless_node;
+
+void rgr_bvh_params_default(rgr_bvh_params* p);
+int rgr_scene_create(rgr_scene** out);
+void rgr_scene_destroy(rgr_scene* s);
+/* SceneManager::addPolymesh (scene_manager.hpp:339-370) + add_materials (:197-277):
+   P is xyz per vertex (already transformed), idx 3 per triangle, one material per triangle. */
+int rgr_scene_add_mesh(rgr_scene* s, const float* P, uint64_t nverts, const uint32_t* idx, uint64_t ntris,
+                       const rgr_material* per_tri);
+/* SceneManager::addPointPrimitive (scene_manager.hpp:372-431): xyzr per sphere */
+int rgr_scene_add_spheres(rgr_scene* s, const float* xyzr, uint64_t n, const rgr_material* per_sphere);
+/* SceneManager::addPoint "ImageEnvmap" branch (scene_manager.hpp:432-497): RGBA float image,
+   clamp_rgb(0, clamp_max) then scale; builds the uniform and six axis alias tables
+   (common/share/envmap.hpp:160-242, alias_method.hpp:47-114).  Without an envmap the
+   renderer selects BSDF sampling only (the reference requires one). */
+int rgr_scene_set_envmap(rgr_scene* s, const float* rgba, int32_t w, int32_t h, float clamp_max, float scale);
+/* SceneManager::buildBVH (scene_manager.hpp:517-577): binned-SAH build, deterministic. */
+int rgr_scene_build_bvh(rgr_scene* s, const rgr_bvh_params* p);
+int rgr_scene_get_info(const rgr_scene* s, rgr_scene_info* info);
+/* create_stackless_bvh (stackless_bvh.hpp:283-341): the same tree in the reference layout */
+int rgr_bvh_export_stackless(const rgr_scene* s, rgr_stackless_node* nodes, uint64_t node_cap, uint32_t* prim_ids,
+                             uint64_t prim_cap);
+/* createEnvmapBuffer (scene_manager.hpp:604-650): tables as uploaded.  pdf/height/alias hold
+   7*w*h entries (uniform, then +x,-x,+y,-y,+z,-z); frag holds 4*w*h (beg_y,end_y,beg_phi,end_phi). */
+int rgr_scene_export_envmap(const rgr_scene* s, float* pdf, float* height, int32_t* alias, float* frag);
+
+/* ---- device context (replaces rt::WavefrontLane, wavefront_path_tracing.hpp:339-1153) */
+typedef struct rgr_context rgr_context;
+
+/* StandardCamera (kernels/camera.cl:4-22, host standardCamera wavefront_path_tracing.hpp:103-118) */
+typedef struct rgr_camera {
+    float eye[3], forward[3], up[3], right[3];
+    float imageplane_o[3], imageplane_r[3], imageplane_b[3];
+    uint32_t image_w, image_h;
+} rgr_camera;
+
+/* Constants the reference hard-codes, as fields whose defaults equal the reference. */
+typedef struct rgr_render_config {
+    float dof;              /* thin-lens radius, new_path.cl:61 (0.0045) */
+    int32_t rr_depth;       /* Russian roulette after this many segments, logic.cl:76 (25) */
+    float radiance_clamp;   /* discard finished samples >= this, logic.cl:125 (1000) */
+    float env_select_prob;  /* one-sample MIS env probability, mixture_density.cl:38 (0.5) */
+    int32_t max_depth;      /* bounces; 0 = unlimited (reference) */
+    uint32_t seed_offset;   /* random_initialize seed offset (lane_index * pool, :544-548) */
+    uint64_t spp;           /* 0 = progressive round robin forever (reference); else stop
+                               generating paths after W*H*spp samples */
+} rgr_render_config;
+
+typedef struct rgr_stats {
+    uint64_t steps;             /* bounces of the whole pool run since render_begin */
+    uint64_t paths_started;     /* next_pixel_index */
+    uint64_t samples_accumulated;
+    uint64_t rays_traced;       /* extension rays cast */
+    double avg_spp;             /* stat kernel (stat.cl), wavefront_path_tracing.hpp:919-934 */
+    uint32_t active_paths;
+    uint32_t error_flags;       /* device-side checks (RGR_E_OVERFLOW causes) */
+} rgr_stats;
+
+#define RGR_FMT_RGBA8 0        /* tonemap (accumlation.cl:68-79) */
+#define RGR_FMT_RGB16 1        /* RGB16IntermediateValueType: half mean + ushort count (accumlation.cl:6-25) */
+#define RGR_FMT_FP64_SUMS 2    /* double r,g,b sums and count per pixel */
+
+void rgr_render_config_default(rgr_render_config* c);
+int rgr_camera_look_at(rgr_camera* c, const float eye[3], const float target[3], const float up[3], float vfov_deg,
+                       uint32_t image_w, uint32_t image_h);
+
+/* OpenCLContext::lane_initialize + WavefrontLane ctor (raccoon_ocl.hpp:752-771, :341-349).
+   path_count = resident paths (reference kWavefrontPathCountGPU = 2^22). */
+int rgr_context_create(rgr_context** out, int32_t device, uint32_t path_count);
+void rgr_context_destroy(rgr_context* c);
+/* WavefrontLane::setup (wavefront_path_tracing.hpp:451-522): upload scene, materials, envmap */
+int rgr_device_upload(rgr_context* c, const rgr_scene* s);
+/* WavefrontLane::initialize / re_start (:532-570, :1013-1018) */
+int rgr_render_begin(rgr_context* c, const rgr_camera* cam, const rgr_render_config* cfg);
+/* WavefrontLane::step() x steps (:591-939); launch_fixed(steps) (:1443-1458).  Asynchronous. */
+int rgr_render_step(rgr_context* c, int32_t steps);
+/* step until every generated sample has finished (needs cfg.spp > 0) or max_steps ran */
+int rgr_render_until_done(rgr_context* c, int32_t max_steps, int32_t* steps_done);
+/* update_intermediate + finalize_color (:942-1007), stat_avg_sample (:1148-1151); synchronous */
+int rgr_render_readback(rgr_context* c, int32_t fmt, void* dst, uint64_t dst_bytes);
+int rgr_render_stats(rgr_context* c, rgr_stats* st);
+/* merge_from (:963-991): add src's accumulation into dst (replicas on several GPUs) */
+int rgr_accum_merge(rgr_context* dst, rgr_context* src);
+int rgr_synchronize(rgr_context* c);
+/* capture the bounce loop in a CUDA graph (1) or launch stage by stage (0; default 1) */
+int rgr_set_graph_mode(rgr_context* c, int32_t enabled);
+
+/* ---- closest hit as a service (extension_ray_cast_stackless.cl:202-246) */
+typedef struct rgr_ray_soa {
+    const float *ox, *oy, *oz, *dx, *dy, *dz, *tmax;
+} rgr_ray_soa;
+/* host arrays in, host arrays out (copies inside) */
+int rgr_trace_closest(rgr_context* c, const rgr_ray_soa* rays, uint64_t n, int32_t* prim, float* t);
+/* device arrays in and out, enqueued on `stream` (cudaStream_t, NULL = context stream) */
+int rgr_trace_closest_device(rgr_context* c, const rgr_ray_soa* rays, uint64_t n, int32_t* prim, float* t,
+                             float* ng_xyz, void* stream);
+
+/* ---- diagnostics --------------------------------------------------------- */
+const char* rgr_status_string(int status);
+const char* rgr_last_error(void);
+/* per-slot path state after the last step, 34 uint32 words per slot in this order:
+   T[3] L[3] ro[3] rd[3] logic_i pixel_index rng[4] hit_surface hit_volume tmin Ng[3]
+   queue vol_count vols[7]  (queue: 0 new path, 1..6 material type, -1 idle) */
+int rgr_debug_read_slots(rgr_context* c, uint32_t* out, uint64_t nslots);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,227 @@
+"""ctypes binding of the CPU oracle (test infrastructure only).
+
+Imported by tests/, __graft_entry__.smoke() and bench.py's CPU baseline, never
+by the product package.  ``OracleScene.from_scene`` builds the oracle's view
+of a scene from the inputs given to the product (points, indices, per
+primitive materials, envmap image) plus the tree the product built, exported
+in the reference StacklessBVHNode layout.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+from . import build_oracle
+
+HERE = Path(__file__).resolve().parent
+
+ORC_SLOT_DTYPE = np.dtype([("T", "<f4", 3), ("L", "<f4", 3), ("ro", "<f4", 3), ("rd", "<f4", 3),
+                           ("logic_i", "<u4"), ("pixel_index", "<u4"), ("rng", "<u4", 4), ("hit_surface", "<i4"),
+                           ("hit_volume", "<i4"), ("tmin", "<f4"), ("Ng", "<f4", 3), ("queue", "<i4"),
+                           ("vol_count", "<i4"), ("vols", "<i4", 7)])
+assert ORC_SLOT_DTYPE.itemsize == 33 * 4
+
+
+class orc_scene(C.Structure):
+    _fields_ = [("points", C.c_void_p), ("indices", C.c_void_p), ("ntris", C.c_uint32), ("spheres", C.c_void_p),
+                ("nspheres", C.c_uint32), ("sphere_begin", C.c_int32), ("nodes", C.c_void_p), ("nnodes", C.c_uint32),
+                ("prim_ids", C.c_void_p), ("nprim_ids", C.c_uint32), ("materials", C.c_void_p),
+                ("lambertians", C.c_void_p), ("wards", C.c_void_p), ("volumes", C.c_void_p),
+                ("env_rgba", C.c_void_p), ("env_w", C.c_int32), ("env_h", C.c_int32), ("env_pdf", C.c_void_p),
+                ("env_height", C.c_void_p), ("env_alias", C.c_void_p), ("env_frag", C.c_void_p)]
+
+
+class orc_camera(C.Structure):
+    _fields_ = [("eye", C.c_float * 4), ("forward", C.c_float * 4), ("up", C.c_float * 4), ("right", C.c_float * 4),
+                ("imageplane_o", C.c_float * 4), ("imageplane_r", C.c_float * 4), ("imageplane_b", C.c_float * 4),
+                ("image_w", C.c_uint32), ("image_h", C.c_uint32)]
+
+
+class orc_config(C.Structure):
+    _fields_ = [("dof", C.c_float), ("rr_depth", C.c_int32), ("radiance_clamp", C.c_float),
+                ("env_select_prob", C.c_float), ("max_depth", C.c_int32), ("seed_offset", C.c_uint32),
+                ("sample_limit", C.c_uint64), ("new_path_y_first", C.c_int32)]
+
+
+_lib = None
+_ref = None
+
+VP, U64, I32, U32, F32C = C.c_void_p, C.c_uint64, C.c_int32, C.c_uint32, C.c_float
+_ORC_SIGS = {
+    "orc_random_initialize": (None, [VP, U64, U64]),
+    "orc_random_uniform": (None, [VP, VP, I32]),
+    "orc_random_uniform_integer": (None, [VP, VP, I32]),
+    "orc_trace": (None, [VP, VP, U64, VP, VP, VP, VP, VP, I32]),
+    "orc_envmap_build": (I32, [VP, I32, I32, VP, VP, VP, VP]),
+    "orc_render": (U64, [VP, VP, VP, U32, I32, VP, VP, I32]),
+    "orc_intermediate": (None, [VP, U64, VP]),
+    "orc_tonemap": (None, [VP, U64, VP]),
+    "orc_float_to_half": (C.c_uint16, [F32C]),
+    "orc_half_to_float": (F32C, [C.c_uint16]),
+    "orc_cosine_hemisphere": (None, [F32C, F32C, VP]),
+    "orc_uniform_sphere": (None, [F32C, F32C, VP]),
+    "orc_sample_from_fragment": (None, [VP, VP, VP]),
+    "orc_orthonormal_basis": (None, [VP, VP, VP]),
+    "orc_sample_ward": (None, [VP, VP, F32C, F32C, F32C, VP]),
+    "orc_pdf_ward": (F32C, [VP, VP, VP, F32C]),
+    "orc_envmap_value": (None, [VP, VP, I32, VP]),
+    "orc_envmap_index": (I32, [VP, I32, I32]),
+    "orc_fm": (F32C, [I32, F32C, F32C]),
+}
+_REF_SIGS = {
+    "ref_random_initialize": (None, [VP, U64, U32]),
+    "ref_random_uniform": (None, [VP, VP, I32]),
+    "ref_random_uniform_integer": (None, [VP, VP, I32]),
+    "ref_trace": (None, [VP, VP, VP, VP, I32, VP, VP, U64, VP, VP, VP]),
+    "ref_render": (U64, [VP, VP, U32, U32, I32, VP, VP, VP]),
+    "ref_alias_method": (U32, [VP, VP, U32]),
+    "ref_sample_envmap_6axis": (None, [VP, VP, VP, VP, VP, VP, U32]),
+    "ref_envmap_index": (I32, [VP, I32, I32]),
+    "ref_envmap_pdf_six_axis": (F32C, [VP, VP, VP, I32, I32]),
+    "ref_pdf_ward": (F32C, [VP, VP, VP, F32C]),
+    "ref_accumlation_to_intermediate": (None, [VP, VP, U64]),
+    "ref_merge_intermediate": (None, [VP, VP, U64]),
+    "ref_tonemap": (None, [VP, VP, U64]),
+    "ref_stat": (None, [VP, VP, U64]),
+}
+
+
+def _bind(l: C.CDLL, sigs: dict) -> None:
+    for name, (res, args) in sigs.items():
+        fn = getattr(l, name)
+        fn.restype = res
+        fn.argtypes = args
+
+
+def lib() -> C.CDLL:
+    global _lib
+    if _lib is None:
+        _lib = C.CDLL(str(build_oracle.build_oracle()))
+        _bind(_lib, _ORC_SIGS)
+    return _lib
+
+
+def ref_lib() -> C.CDLL | None:
+    """The reference kernels compiled from source (None where the reference
+    sources are not available)."""
+    global _ref
+    if _ref is None:
+        p = build_oracle.build_ref()
+        if p is None or not Path(p).exists():
+            return None
+        _ref = C.CDLL(str(p))
+        _bind(_ref, _REF_SIGS)
+    return _ref
+
+
+def P(a: np.ndarray | None) -> int | None:
+    return None if a is None else a.ctypes.data
+
+
+def reference_materials(mats: list[dict]):
+    """MaterialStorage layout (scene_manager.hpp:106-172): per-primitive (type,
+    index) and the per-type arrays in the reference structs."""
+    n = len(mats)
+    ref = np.zeros((max(n, 1), 2), np.int32)
+    lam, ward, vol = [], [], []
+    cnt = {1: 0, 2: 0, 3: 0, 4: 0, 5: 0}
+    for i, m in enumerate(mats):
+        t = m["type"]
+        ref[i] = (t, cnt[t])
+        cnt[t] += 1
+        if t == 1:
+            rec = np.zeros(12, np.float32)
+            rec[0:3] = m.get("le", (0, 0, 0))
+            rec[4:7] = m.get("r", (1, 1, 1))
+            lam.append(rec)
+        elif t == 4:
+            rec = np.zeros(16, np.float32)
+            rec[0] = m.get("alpha", 0.1)
+            rec[4:7] = m.get("r", (1, 1, 1))
+            rec[8:11] = m.get("edgetint", (1, 1, 1))
+            rec[12] = m.get("falloff", 0.5)
+            ward.append(rec)
+        elif t == 5:
+            rec = np.zeros(8, np.float32)
+            rec[0] = m.get("c", 1.0)
+            rec[4:7] = m.get("r", (1, 1, 1))
+            vol.append(rec)
+
+    def stack(lst, width):
+        return np.stack(lst).astype(np.float32) if lst else np.zeros((1, width), np.float32)
+
+    return ref, stack(lam, 12), stack(ward, 16), stack(vol, 8)
+
+
+class OracleScene:
+    """Arrays kept alive for the orc_scene struct."""
+
+    def __init__(self):
+        self.s = orc_scene()
+
+    @classmethod
+    def from_scene(cls, sm, points, indices, spheres=None):
+        o = cls()
+        pts = np.zeros((points.shape[0], 4), np.float32)
+        pts[:, :3] = points
+        o.points = pts
+        o.indices = np.ascontiguousarray(indices, np.uint32).reshape(-1)
+        o.spheres = np.ascontiguousarray(spheres, np.float32) if spheres is not None else np.zeros((1, 4), np.float32)
+        ntri = o.indices.shape[0] // 3
+        nsph = 0 if spheres is None else spheres.shape[0]
+        o.nodes, o.prim_ids = sm.export_stackless()
+        o.mat, o.lam, o.ward, o.vol = reference_materials(sm.materials)
+        s = o.s
+        s.points, s.indices, s.ntris = P(o.points), P(o.indices), ntri
+        s.spheres, s.nspheres, s.sphere_begin = P(o.spheres), nsph, ntri
+        s.nodes, s.nnodes = P(o.nodes), o.nodes.shape[0]
+        s.prim_ids, s.nprim_ids = P(o.prim_ids), o.prim_ids.shape[0]
+        s.materials, s.lambertians, s.wards, s.volumes = P(o.mat), P(o.lam), P(o.ward), P(o.vol)
+        env = sm.export_envmap()
+        if env is not None:
+            o.env_rgba = np.ascontiguousarray(sm.envmap, np.float32)
+            o.env = env
+            s.env_rgba, s.env_w, s.env_h = P(o.env_rgba), env["w"], env["h"]
+            s.env_pdf, s.env_height, s.env_alias, s.env_frag = (P(env["pdf"]), P(env["height"]), P(env["alias"]),
+                                                                P(env["frag"]))
+        return o
+
+    def trace(self, rays8: np.ndarray, counters: bool = False, threads: int = 8):
+        n = rays8.shape[0]
+        prim = np.empty(n, np.int32)
+        t = np.empty(n, np.float32)
+        ng = np.empty((n, 3), np.float32)
+        nv = np.empty(n, np.uint32) if counters else None
+        nt = np.empty(n, np.uint32) if counters else None
+        lib().orc_trace(C.byref(self.s), P(rays8), n, P(prim), P(t), P(ng), P(nv), P(nt), threads)
+        return (prim, t, ng, nv, nt) if counters else (prim, t, ng)
+
+    def render(self, cam: orc_camera, cfg: orc_config, npaths: int, steps: int, threads: int = 8,
+               want_slots: bool = True):
+        npix = cam.image_w * cam.image_h
+        accum = np.zeros((npix, 4), np.float64)
+        slots = np.zeros(npaths, ORC_SLOT_DTYPE) if want_slots else None
+        nxt = lib().orc_render(C.byref(self.s), C.byref(cam), C.byref(cfg), npaths, steps, P(accum), P(slots),
+                               threads)
+        return accum, slots, int(nxt)
+
+
+def camera_from_rgr(cam) -> orc_camera:
+    o = orc_camera()
+    for name in ("eye", "forward", "up", "right", "imageplane_o", "imageplane_r", "imageplane_b"):
+        src = getattr(cam, name)
+        dst = getattr(o, name)
+        for k in range(3):
+            dst[k] = src[k]
+    o.image_w, o.image_h = cam.image_w, cam.image_h
+    return o
+
+
+def config_from_rgr(cfg, npix: int) -> orc_config:
+    o = orc_config()
+    o.dof, o.rr_depth, o.radiance_clamp = cfg.dof, cfg.rr_depth, cfg.radiance_clamp
+    o.env_select_prob, o.max_depth, o.seed_offset = cfg.env_select_prob, cfg.max_depth, cfg.seed_offset
+    o.sample_limit = cfg.spp * npix if cfg.spp else 0
+    return o

@@ -1,0 +1,429 @@
+"""raccoongpurender_gb300 — a GB300-native wavefront path tracer with the
+host API of RaccoonGPURender's hot path.
+
+Python mirror of the reference host classes over the C ABI of ``librgr.so``
+(``include/rgr.h``):
+
+* :class:`SceneManager`  — ``rt::SceneManager`` (common/scene_manager.hpp:330-672):
+  ``addPolymesh``, ``addSpheres``, ``setEnvmap``, ``buildBVH``.
+* :class:`WavefrontLane` — ``rt::WavefrontLane`` (common/wavefront_path_tracing.hpp:339-1153):
+  ``setup``, ``initialize``, ``step``, ``finalize_color``, ``stats``.
+* :class:`WavefrontPathTracing` — the fixed-work front end, ``launch_fixed(steps)``
+  and ``create_color_image()`` (wavefront_path_tracing.hpp:1443-1458, :1345-1408).
+
+The compute path is the CUDA library only: if ``librgr.so`` is missing or no
+GPU is present, the device calls raise :class:`RgrError`; there is no CPU
+fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from pathlib import Path
+
+import numpy as np
+
+from . import materials  # noqa: F401  (public)
+
+_PKG = Path(__file__).resolve().parent
+LIB_PATH = _PKG / "_lib" / "librgr.so"
+
+RGR_OK = 0
+RGR_FMT_RGBA8, RGR_FMT_RGB16, RGR_FMT_FP64_SUMS = 0, 1, 2
+STATUS = {0: "ok", -1: "invalid argument", -2: "CUDA error", -3: "out of memory", -4: "call out of order",
+          -5: "device capacity check fired", -6: "no CUDA device"}
+
+
+class RgrError(RuntimeError):
+    def __init__(self, status: int, where: str, detail: str = ""):
+        self.status = status
+        super().__init__(f"{where}: {STATUS.get(status, status)}{(' — ' + detail) if detail else ''}")
+
+
+class rgr_material(C.Structure):
+    _fields_ = [("type", C.c_int32), ("back_emission", C.c_int32), ("le", C.c_float * 3), ("r", C.c_float * 3),
+                ("edgetint", C.c_float * 3), ("alpha", C.c_float), ("falloff", C.c_float), ("c", C.c_float)]
+
+
+class rgr_bvh_params(C.Structure):
+    _fields_ = [("max_leaf_size", C.c_int32), ("sah_bins", C.c_int32), ("traversal_cost", C.c_float),
+                ("intersect_cost", C.c_float), ("max_depth", C.c_int32), ("num_threads", C.c_int32)]
+
+
+class rgr_scene_info(C.Structure):
+    _fields_ = [("num_triangles", C.c_uint64), ("num_spheres", C.c_uint64), ("num_vertices", C.c_uint64),
+                ("num_nodes_stackless", C.c_uint64), ("num_inner_nodes", C.c_uint64), ("num_leaves", C.c_uint64),
+                ("depth", C.c_int32), ("sphere_begin", C.c_int32), ("bounds", C.c_float * 6),
+                ("sah_cost", C.c_double)]
+
+
+class rgr_camera(C.Structure):
+    _fields_ = [("eye", C.c_float * 3), ("forward", C.c_float * 3), ("up", C.c_float * 3), ("right", C.c_float * 3),
+                ("imageplane_o", C.c_float * 3), ("imageplane_r", C.c_float * 3), ("imageplane_b", C.c_float * 3),
+                ("image_w", C.c_uint32), ("image_h", C.c_uint32)]
+
+
+class rgr_render_config(C.Structure):
+    _fields_ = [("dof", C.c_float), ("rr_depth", C.c_int32), ("radiance_clamp", C.c_float),
+                ("env_select_prob", C.c_float), ("max_depth", C.c_int32), ("seed_offset", C.c_uint32),
+                ("spp", C.c_uint64)]
+
+
+class rgr_stats(C.Structure):
+    _fields_ = [("steps", C.c_uint64), ("paths_started", C.c_uint64), ("samples_accumulated", C.c_uint64),
+                ("rays_traced", C.c_uint64), ("avg_spp", C.c_double), ("active_paths", C.c_uint32),
+                ("error_flags", C.c_uint32)]
+
+
+class rgr_ray_soa(C.Structure):
+    _fields_ = [(n, C.c_void_p) for n in ("ox", "oy", "oz", "dx", "dy", "dz", "tmax")]
+
+
+STACKLESS_NODE_DTYPE = np.dtype([("L_lower", "<f4", 4), ("L_upper", "<f4", 4), ("R_lower", "<f4", 4),
+                                 ("R_upper", "<f4", 4), ("link_parent", "<u4"), ("link_L", "<u4"),
+                                 ("link_R", "<u4"), ("link_sibling", "<u4"), ("primitive_indices_beg", "<u4"),
+                                 ("primitive_indices_end", "<u4"), ("pad", "<u4", 2)])
+assert STACKLESS_NODE_DTYPE.itemsize == 96
+
+# exported C symbols and their signatures (include/rgr.h)
+_SIGS = {
+    "rgr_status_string": (C.c_char_p, [C.c_int]),
+    "rgr_last_error": (C.c_char_p, []),
+    "rgr_bvh_params_default": (None, [C.c_void_p]),
+    "rgr_scene_create": (C.c_int, [C.c_void_p]),
+    "rgr_scene_destroy": (None, [C.c_void_p]),
+    "rgr_scene_add_mesh": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p, C.c_uint64, C.c_void_p]),
+    "rgr_scene_add_spheres": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p]),
+    "rgr_scene_set_envmap": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_float, C.c_float]),
+    "rgr_scene_build_bvh": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "rgr_scene_get_info": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "rgr_bvh_export_stackless": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p, C.c_uint64]),
+    "rgr_scene_export_envmap": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "rgr_render_config_default": (None, [C.c_void_p]),
+    "rgr_camera_look_at": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_float, C.c_uint32,
+                                     C.c_uint32]),
+    "rgr_context_create": (C.c_int, [C.c_void_p, C.c_int32, C.c_uint32]),
+    "rgr_context_destroy": (None, [C.c_void_p]),
+    "rgr_device_upload": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "rgr_render_begin": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "rgr_render_step": (C.c_int, [C.c_void_p, C.c_int32]),
+    "rgr_render_until_done": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p]),
+    "rgr_render_readback": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_uint64]),
+    "rgr_render_stats": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "rgr_accum_merge": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "rgr_synchronize": (C.c_int, [C.c_void_p]),
+    "rgr_set_graph_mode": (C.c_int, [C.c_void_p, C.c_int32]),
+    "rgr_trace_closest": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p, C.c_void_p]),
+    "rgr_trace_closest_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p, C.c_void_p,
+                                           C.c_void_p, C.c_void_p]),
+    "rgr_debug_read_slots": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64]),
+}
+
+_lib = None
+
+
+def load_library(build_if_missing: bool = True) -> C.CDLL:
+    """Load librgr.so (building it first if it is absent)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not LIB_PATH.exists() and build_if_missing and os.environ.get("RGR_NO_BUILD") != "1":
+        from . import _build
+        _build.build()
+    if not LIB_PATH.exists():
+        raise RgrError(-6, "load_library", f"{LIB_PATH} is missing; run raccoongpurender_gb300._build.build()")
+    lib = C.CDLL(str(LIB_PATH))
+    for name, (res, args) in _SIGS.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def _check(st: int, where: str) -> None:
+    if st != RGR_OK:
+        detail = load_library().rgr_last_error()
+        raise RgrError(st, where, detail.decode() if detail else "")
+
+
+def _ptr(a: np.ndarray) -> int:
+    return a.ctypes.data
+
+
+def _materials_to_c(mats) -> C.Array:
+    arr = (rgr_material * max(1, len(mats)))()
+    for i, m in enumerate(mats):
+        x = arr[i]
+        x.type = m["type"]
+        x.back_emission = int(m.get("back_emission", 0))
+        for k, v in enumerate(m.get("le", (0.0, 0.0, 0.0))):
+            x.le[k] = v
+        for k, v in enumerate(m.get("r", (1.0, 1.0, 1.0))):
+            x.r[k] = v
+        for k, v in enumerate(m.get("edgetint", (1.0, 1.0, 1.0))):
+            x.edgetint[k] = v
+        x.alpha = m.get("alpha", 0.1)
+        x.falloff = m.get("falloff", 0.5)
+        x.c = m.get("c", 1.0)
+    return arr
+
+
+class SceneManager:
+    """Scene upload side of the reference (rt::SceneManager)."""
+
+    def __init__(self):
+        self._lib = load_library()
+        self._h = C.c_void_p()
+        _check(self._lib.rgr_scene_create(C.byref(self._h)), "rgr_scene_create")
+        self.materials: list[dict] = []     # per primitive, triangles then spheres
+        self.num_triangles = 0
+        self.envmap = None
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h and h.value:
+            self._lib.rgr_scene_destroy(h)
+            self._h = C.c_void_p()
+
+    @property
+    def handle(self):
+        return self._h
+
+    def addPolymesh(self, points, indices, materials) -> None:
+        """SceneManager::addPolymesh (scene_manager.hpp:339-370)."""
+        P = np.ascontiguousarray(points, dtype=np.float32).reshape(-1, 3)
+        I = np.ascontiguousarray(indices, dtype=np.uint32).reshape(-1, 3)
+        if len(materials) != I.shape[0]:
+            raise ValueError("one material per triangle")
+        cm = _materials_to_c(materials)
+        _check(self._lib.rgr_scene_add_mesh(self._h, _ptr(P), P.shape[0], _ptr(I), I.shape[0], C.addressof(cm)),
+               "rgr_scene_add_mesh")
+        self.materials.extend(materials)
+        self.num_triangles += I.shape[0]
+
+    def addMesh(self, mesh) -> None:
+        self.addPolymesh(mesh.points, mesh.indices, mesh.materials)
+
+    def addSpheres(self, xyzr, materials) -> None:
+        """SceneManager::addPointPrimitive (scene_manager.hpp:372-431)."""
+        S = np.ascontiguousarray(xyzr, dtype=np.float32).reshape(-1, 4)
+        cm = _materials_to_c(materials)
+        _check(self._lib.rgr_scene_add_spheres(self._h, _ptr(S), S.shape[0], C.addressof(cm)),
+               "rgr_scene_add_spheres")
+        self.materials.extend(materials)
+
+    def setEnvmap(self, rgba, clamp_max: float = 3.4028234663852886e38, scale: float = 1.0) -> None:
+        """The ImageEnvmap point of SceneManager::addPoint (scene_manager.hpp:432-497)."""
+        if rgba is None:
+            _check(self._lib.rgr_scene_set_envmap(self._h, None, 0, 0, 0.0, 1.0), "rgr_scene_set_envmap")
+            self.envmap = None
+            return
+        img = np.ascontiguousarray(rgba, dtype=np.float32)
+        h, w = img.shape[:2]
+        _check(self._lib.rgr_scene_set_envmap(self._h, _ptr(img), w, h, clamp_max, scale), "rgr_scene_set_envmap")
+        proc = img.copy()
+        proc[..., :3] = np.minimum(np.maximum(proc[..., :3], np.float32(0)), np.float32(clamp_max))
+        if scale != 1.0:
+            proc[..., :3] *= np.float32(scale)
+        self.envmap = proc
+
+    def buildBVH(self, max_leaf_size: int = 4, sah_bins: int = 32, num_threads: int = 0) -> None:
+        """SceneManager::buildBVH (scene_manager.hpp:517-577)."""
+        p = rgr_bvh_params()
+        self._lib.rgr_bvh_params_default(C.byref(p))
+        p.max_leaf_size = max_leaf_size
+        p.sah_bins = sah_bins
+        p.num_threads = num_threads
+        _check(self._lib.rgr_scene_build_bvh(self._h, C.byref(p)), "rgr_scene_build_bvh")
+
+    def info(self) -> rgr_scene_info:
+        i = rgr_scene_info()
+        _check(self._lib.rgr_scene_get_info(self._h, C.byref(i)), "rgr_scene_get_info")
+        return i
+
+    def export_stackless(self):
+        """The tree in the reference StacklessBVHNode layout (stackless_bvh.hpp:264-341)."""
+        inf = self.info()
+        nodes = np.zeros(inf.num_nodes_stackless, dtype=STACKLESS_NODE_DTYPE)
+        ids = np.zeros(inf.num_triangles + inf.num_spheres, dtype=np.uint32)
+        _check(self._lib.rgr_bvh_export_stackless(self._h, _ptr(nodes), nodes.shape[0], _ptr(ids), ids.shape[0]),
+               "rgr_bvh_export_stackless")
+        return nodes, ids
+
+    def export_envmap(self):
+        if self.envmap is None:
+            return None
+        h, w = self.envmap.shape[:2]
+        n = w * h
+        pdf = np.zeros(7 * n, np.float32)
+        height = np.zeros(7 * n, np.float32)
+        alias = np.zeros(7 * n, np.int32)
+        frag = np.zeros(4 * n, np.float32)
+        _check(self._lib.rgr_scene_export_envmap(self._h, _ptr(pdf), _ptr(height), _ptr(alias), _ptr(frag)),
+               "rgr_scene_export_envmap")
+        return dict(pdf=pdf, height=height, alias=alias, frag=frag, w=w, h=h)
+
+
+def render_config(**kw) -> rgr_render_config:
+    """A render config with the reference defaults, overridden by keywords
+    (dof, rr_depth, radiance_clamp, env_select_prob, max_depth, seed_offset, spp)."""
+    c = rgr_render_config()
+    load_library().rgr_render_config_default(C.byref(c))
+    for k, v in kw.items():
+        setattr(c, k, v)
+    return c
+
+
+def camera_look_at(eye, target, up, vfov: float, w: int, h: int) -> rgr_camera:
+    cam = rgr_camera()
+    f3 = C.c_float * 3
+    _check(load_library().rgr_camera_look_at(C.byref(cam), f3(*eye), f3(*target), f3(*up), vfov, w, h),
+           "rgr_camera_look_at")
+    return cam
+
+
+SLOT_WORDS = 34
+SLOT_FIELDS = dict(T=(0, 3), L=(3, 6), ro=(6, 9), rd=(9, 12), logic_i=(12, 13), pixel_index=(13, 14),
+                   rng=(14, 18), hit_surface=(18, 19), hit_volume=(19, 20), tmin=(20, 21), Ng=(21, 24),
+                   queue=(24, 25), vol_count=(25, 26), vols=(26, 33))
+
+
+class WavefrontLane:
+    """One GPU's path pool (rt::WavefrontLane)."""
+
+    def __init__(self, device: int = 0, path_count: int = 1 << 22):
+        self._lib = load_library()
+        self._h = C.c_void_p()
+        _check(self._lib.rgr_context_create(C.byref(self._h), device, path_count), "rgr_context_create")
+        self.path_count = path_count
+        self.camera = None
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h and h.value:
+            self._lib.rgr_context_destroy(h)
+            self._h = C.c_void_p()
+
+    @property
+    def handle(self):
+        return self._h
+
+    def setup(self, scene: SceneManager) -> None:
+        """WavefrontLane::setup (wavefront_path_tracing.hpp:451-522)."""
+        _check(self._lib.rgr_device_upload(self._h, scene.handle), "rgr_device_upload")
+
+    def initialize(self, camera: rgr_camera, config: rgr_render_config | None = None) -> None:
+        """WavefrontLane::initialize (:532-570)."""
+        self.camera = camera
+        cfg = config if config is not None else render_config()
+        _check(self._lib.rgr_render_begin(self._h, C.byref(camera), C.byref(cfg)), "rgr_render_begin")
+
+    re_start = initialize
+
+    def step(self, steps: int = 1) -> None:
+        """WavefrontLane::step() (:591-939), `steps` times; asynchronous."""
+        _check(self._lib.rgr_render_step(self._h, steps), "rgr_render_step")
+
+    def render_until_done(self, max_steps: int = 100000) -> int:
+        n = C.c_int32()
+        _check(self._lib.rgr_render_until_done(self._h, max_steps, C.byref(n)), "rgr_render_until_done")
+        return n.value
+
+    def synchronize(self) -> None:
+        _check(self._lib.rgr_synchronize(self._h), "rgr_synchronize")
+
+    def set_graph_mode(self, enabled: bool) -> None:
+        _check(self._lib.rgr_set_graph_mode(self._h, int(enabled)), "rgr_set_graph_mode")
+
+    def _npix(self) -> int:
+        return int(self.camera.image_w) * int(self.camera.image_h)
+
+    def accumulation(self) -> np.ndarray:
+        """FP64 per-pixel (r, g, b, count) sums, shape (H, W, 4)."""
+        out = np.zeros((self._npix(), 4), np.float64)
+        _check(self._lib.rgr_render_readback(self._h, RGR_FMT_FP64_SUMS, _ptr(out), out.nbytes),
+               "rgr_render_readback")
+        return out.reshape(self.camera.image_h, self.camera.image_w, 4)
+
+    def intermediate(self) -> np.ndarray:
+        """RGB16IntermediateValueType per pixel (half mean, ushort count)."""
+        out = np.zeros((self._npix(), 4), np.uint16)
+        _check(self._lib.rgr_render_readback(self._h, RGR_FMT_RGB16, _ptr(out), out.nbytes), "rgr_render_readback")
+        return out.reshape(self.camera.image_h, self.camera.image_w, 4)
+
+    def finalize_color(self) -> np.ndarray:
+        """WavefrontLane::finalize_color (:993-1007): RGBA8, shape (H, W, 4)."""
+        out = np.zeros((self._npix(), 4), np.uint8)
+        _check(self._lib.rgr_render_readback(self._h, RGR_FMT_RGBA8, _ptr(out), out.nbytes), "rgr_render_readback")
+        return out.reshape(self.camera.image_h, self.camera.image_w, 4)
+
+    def stats(self) -> rgr_stats:
+        s = rgr_stats()
+        _check(self._lib.rgr_render_stats(self._h, C.byref(s)), "rgr_render_stats")
+        return s
+
+    def stat_avg_sample(self) -> float:
+        return self.stats().avg_spp
+
+    def debug_slots(self) -> dict:
+        """Per-slot path state as a dict of arrays (float fields as float32)."""
+        raw = np.zeros((self.path_count, SLOT_WORDS), np.uint32)
+        _check(self._lib.rgr_debug_read_slots(self._h, _ptr(raw), self.path_count), "rgr_debug_read_slots")
+        return slots_from_words(raw)
+
+    def merge_from(self, other: "WavefrontLane") -> None:
+        """WavefrontLane::merge_from (:963-991)."""
+        _check(self._lib.rgr_accum_merge(self._h, other.handle), "rgr_accum_merge")
+
+    # ---- closest hit as a service
+    def trace_closest(self, rays) -> tuple[np.ndarray, np.ndarray]:
+        """Closest hit of host rays: returns (prim int32, t float32)."""
+        soa = rays.soa() if hasattr(rays, "soa") else rays
+        soa = [np.ascontiguousarray(a, dtype=np.float32) for a in soa]
+        n = soa[0].shape[0]
+        prim = np.empty(n, np.int32)
+        t = np.empty(n, np.float32)
+        r = rgr_ray_soa(*[_ptr(a) for a in soa])
+        _check(self._lib.rgr_trace_closest(self._h, C.byref(r), n, _ptr(prim), _ptr(t)), "rgr_trace_closest")
+        return prim, t
+
+    def trace_closest_device(self, soa_ptrs, n: int, prim_ptr: int, t_ptr: int, ng_ptr: int = 0,
+                             stream: int = 0) -> None:
+        """Closest hit of device rays (7 device pointers), enqueued on `stream`."""
+        r = rgr_ray_soa(*soa_ptrs)
+        _check(self._lib.rgr_trace_closest_device(self._h, C.byref(r), n, prim_ptr, t_ptr, ng_ptr or None,
+                                                  stream or None), "rgr_trace_closest_device")
+
+
+def slots_from_words(raw: np.ndarray) -> dict:
+    out = {}
+    for k, (a, b) in SLOT_FIELDS.items():
+        v = raw[:, a:b]
+        if k in ("T", "L", "ro", "rd", "tmin", "Ng"):
+            v = v.view(np.float32)
+        elif k in ("hit_surface", "hit_volume", "queue", "vol_count", "vols"):
+            v = v.view(np.int32)
+        out[k] = v if b - a > 1 else v[:, 0]
+    return out
+
+
+class WavefrontPathTracing:
+    """Fixed-work front end on one GPU (rt::WavefrontPathTracing, RenderMode_SingleGPU)."""
+
+    def __init__(self, scene: SceneManager, camera: rgr_camera, config: rgr_render_config | None = None,
+                 path_count: int = 1 << 22, device: int = 0):
+        self.lane = WavefrontLane(device, path_count)
+        self.lane.setup(scene)
+        self.lane.initialize(camera, config)
+
+    def launch_fixed(self, steps: int) -> np.ndarray:
+        """Run `steps` bounces of the whole pool, then create_color_image()."""
+        self.lane.step(steps)
+        return self.create_color_image()
+
+    def create_color_image(self) -> np.ndarray:
+        return self.lane.finalize_color()
+
+    def re_start(self, camera: rgr_camera, config: rgr_render_config | None = None) -> None:
+        self.lane.initialize(camera, config)

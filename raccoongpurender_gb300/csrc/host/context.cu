@@ -1,0 +1,514 @@
+// context.cu — the device half of the C ABI: upload, render loop, readback,
+// ray-cast service.  Replaces rt::WavefrontLane
+// (common/wavefront_path_tracing.hpp:339-1153) on one GPU.  The per-bounce
+// launch sequence is captured once into a CUDA graph and replayed, instead of
+// the reference's ~24 enqueued NDRange launches per bounce.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../kernels/wavefront.cuh"
+#include "../rgr_internal.h"
+
+using namespace rgr;
+using namespace rgr::dev;
+
+namespace {
+
+bool cuda_ok(cudaError_t e, const char* what) {
+    if (e == cudaSuccess) return true;
+    set_error(std::string(what) + ": " + cudaGetErrorString(e));
+    return false;
+}
+#define RGR_CUDA(call)                                      \
+    do {                                                    \
+        if (!cuda_ok((call), #call)) return RGR_E_CUDA;     \
+    } while (0)
+
+struct DevBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+    DevBuf() = default;
+    DevBuf(const DevBuf&) = delete;
+    DevBuf& operator=(const DevBuf&) = delete;
+    ~DevBuf() { release(); }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+    }
+    int alloc(size_t n) {
+        if (n <= bytes && p) return RGR_OK;
+        release();
+        size_t b = std::max<size_t>(n, 256);
+        cudaError_t e = cudaMalloc(&p, b);
+        if (e != cudaSuccess) {
+            p = nullptr;
+            set_error(std::string("cudaMalloc: ") + cudaGetErrorString(e));
+            return e == cudaErrorMemoryAllocation ? RGR_E_OOM : RGR_E_CUDA;
+        }
+        bytes = b;
+        return RGR_OK;
+    }
+    int upload(const void* src, size_t n, cudaStream_t st) {
+        int r = alloc(n);
+        if (r != RGR_OK) return r;
+        if (n) RGR_CUDA(cudaMemcpyAsync(p, src, n, cudaMemcpyHostToDevice, st));
+        return RGR_OK;
+    }
+    template <class T>
+    T* as() const {
+        return reinterpret_cast<T*>(p);
+    }
+};
+
+}  // namespace
+
+struct rgr_context {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    int num_sms = 152;
+    uint32_t npaths = 0, ntiles = 0;
+    // scene
+    DevBuf nodes, prims, points, indices, spheres, materials, lambertians, wards, volumes;
+    DevBuf env_rgba, env_pdf, env_alias, env_frag;
+    SceneView sv{};
+    bool uploaded = false;
+    // paths
+    DevBuf ro, rd, T, L, ng, rng, vols, qid, queues[kNumQueues], counts, tile_new, scalars, accum, err;
+    PathsView pv{};
+    QueueView qv{};
+    RenderParams rp{};
+    bool begun = false;
+    uint64_t steps = 0;
+    uint32_t npix = 0;
+    int shade_grid = 0;
+    // CUDA graph of one bounce
+    bool graph_mode = true;
+    cudaGraphExec_t graph_exec = nullptr;
+    // ray-cast service buffers
+    DevBuf trays[7], tprim, tt, tread;
+
+    ~rgr_context() {
+        if (graph_exec) cudaGraphExecDestroy(graph_exec);
+        if (stream) cudaStreamDestroy(stream);
+    }
+    int step_launches(cudaStream_t st) {
+        launch_compact_new(pv, qv, st);
+        launch_shade(sv, pv, qv, rp, shade_grid, st);
+        RGR_CUDA(cudaMemsetAsync(qv.counts + 1, 0, sizeof(uint32_t) * (kNumQueues - 1), st));
+        RGR_CUDA(cudaMemsetAsync(qv.tile_new, 0, sizeof(uint32_t) * ntiles, st));
+        launch_trace_logic(sv, pv, qv, rp, 128, st);
+        RGR_CUDA(cudaGetLastError());
+        return RGR_OK;
+    }
+    void drop_graph() {
+        if (graph_exec) cudaGraphExecDestroy(graph_exec);
+        graph_exec = nullptr;
+    }
+};
+
+extern "C" {
+
+int rgr_context_create(rgr_context** out, int32_t device, uint32_t path_count) {
+    if (!out || path_count == 0 || path_count > (1u << 28)) return RGR_E_INVALID;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        set_error("no CUDA device");
+        return RGR_E_NODEVICE;
+    }
+    if (device < 0 || device >= ndev) return RGR_E_INVALID;
+    rgr_context* c = new (std::nothrow) rgr_context();
+    if (!c) return RGR_E_OOM;
+    c->device = device;
+    if (!cuda_ok(cudaSetDevice(device), "cudaSetDevice") ||
+        !cuda_ok(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking), "cudaStreamCreate")) {
+        delete c;
+        return RGR_E_CUDA;
+    }
+    cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device);
+    c->npaths = path_count;
+    c->ntiles = (path_count + kTile - 1) / kTile;
+    *out = c;
+    return RGR_OK;
+}
+
+void rgr_context_destroy(rgr_context* c) {
+    if (!c) return;
+    cudaSetDevice(c->device);
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    delete c;
+}
+
+int rgr_set_graph_mode(rgr_context* c, int32_t enabled) {
+    if (!c) return RGR_E_INVALID;
+    c->graph_mode = enabled != 0;
+    c->drop_graph();
+    return RGR_OK;
+}
+
+int rgr_device_upload(rgr_context* c, const rgr_scene* s) {
+    if (!c || !s) return RGR_E_INVALID;
+    if (!s->bvh.built) {
+        set_error("rgr_device_upload: build the BVH first");
+        return RGR_E_STATE;
+    }
+    RGR_CUDA(cudaSetDevice(c->device));
+    cudaStream_t st = c->stream;
+    const Bvh& b = s->bvh;
+    int r;
+#define UP(buf, ptr, bytes)                                  \
+    if ((r = c->buf.upload((ptr), (bytes), st)) != RGR_OK) return r;
+    UP(nodes, b.nodes.data(), b.nodes.size() * sizeof(NodeD));
+    UP(prims, b.prims.data(), b.prims.size() * sizeof(PrimD));
+    const size_t nv = s->points.size() / 3, ntri = s->indices.size() / 3, nsph = s->spheres.size() / 4;
+    std::vector<float> p4(4 * nv);
+    for (size_t i = 0; i < nv; ++i) {
+        p4[4 * i] = s->points[3 * i];
+        p4[4 * i + 1] = s->points[3 * i + 1];
+        p4[4 * i + 2] = s->points[3 * i + 2];
+        p4[4 * i + 3] = 0.0f;
+    }
+    UP(points, p4.data(), p4.size() * 4);
+    UP(indices, s->indices.data(), s->indices.size() * 4);
+    UP(spheres, s->spheres.data(), s->spheres.size() * 4);
+    std::vector<MaterialRef> mats(s->tri_materials);
+    mats.insert(mats.end(), s->sphere_materials.begin(), s->sphere_materials.end());
+    UP(materials, mats.data(), mats.size() * sizeof(MaterialRef));
+    UP(lambertians, s->lambertians.data(), s->lambertians.size() * sizeof(LambertianD));
+    UP(wards, s->wards.data(), s->wards.size() * sizeof(WardD));
+    UP(volumes, s->volumes.data(), s->volumes.size() * sizeof(VolumeD));
+    const EnvTables& e = s->env;
+    std::vector<int32_t> alias2;
+    if (e.present) {
+        size_t n7 = e.alias.size();
+        alias2.resize(2 * n7);
+        for (size_t i = 0; i < n7; ++i) {
+            memcpy(&alias2[2 * i], &e.height[i], 4);
+            alias2[2 * i + 1] = e.alias[i];
+        }
+        UP(env_rgba, e.rgba.data(), e.rgba.size() * 4);
+        UP(env_pdf, e.pdf.data(), e.pdf.size() * 4);
+        UP(env_alias, alias2.data(), alias2.size() * 4);
+        UP(env_frag, e.frag.data(), e.frag.size() * 4);
+    } else {
+        UP(env_rgba, nullptr, 0);
+        UP(env_pdf, nullptr, 0);
+        UP(env_alias, nullptr, 0);
+        UP(env_frag, nullptr, 0);
+    }
+#undef UP
+    RGR_CUDA(cudaStreamSynchronize(st));  // host staging vectors go out of scope
+    SceneView& v = c->sv;
+    v.nodes = c->nodes.as<float4>();
+    v.prims = c->prims.as<float4>();
+    v.root_link = b.root_link;
+    v.num_prims = (uint32_t)b.prims.size();
+    v.points = c->points.as<float4>();
+    v.indices = c->indices.as<uint32_t>();
+    v.spheres = c->spheres.as<float4>();
+    v.sphere_begin = (int32_t)ntri;
+    (void)nsph;
+    v.materials = c->materials.as<int2>();
+    v.lambertians = c->lambertians.as<float4>();
+    v.wards = c->wards.as<float4>();
+    v.volumes = c->volumes.as<float4>();
+    v.env_rgba = c->env_rgba.as<float4>();
+    v.env_pdf = c->env_pdf.as<float>();
+    v.env_alias = c->env_alias.as<int2>();
+    v.env_frag = c->env_frag.as<float4>();
+    v.env_w = e.present ? e.w : 0;
+    v.env_h = e.present ? e.h : 0;
+    v.has_env = e.present ? 1 : 0;
+    c->uploaded = true;
+    c->drop_graph();
+    return RGR_OK;
+}
+
+int rgr_render_begin(rgr_context* c, const rgr_camera* cam, const rgr_render_config* cfg) {
+    if (!c || !cam) return RGR_E_INVALID;
+    if (!c->uploaded) {
+        set_error("rgr_render_begin: upload a scene first");
+        return RGR_E_STATE;
+    }
+    if (cam->image_w == 0 || cam->image_h == 0 || (uint64_t)cam->image_w * cam->image_h > (1ull << 31))
+        return RGR_E_INVALID;
+    rgr_render_config d;
+    rgr_render_config_default(&d);
+    const rgr_render_config& k = cfg ? *cfg : d;
+    RGR_CUDA(cudaSetDevice(c->device));
+    cudaStream_t st = c->stream;
+    const size_t n = (size_t)c->ntiles * kTile;  // padded to whole tiles
+    int r;
+#define AL(buf, bytes)                                    \
+    if ((r = c->buf.alloc(bytes)) != RGR_OK) return r;
+    AL(ro, 16 * n);
+    AL(rd, 16 * n);
+    AL(T, 16 * n);
+    AL(L, 16 * n);
+    AL(ng, 16 * n);
+    AL(rng, 16 * n);
+    AL(vols, 32 * n);
+    AL(qid, n);
+    for (int q = 0; q < kNumQueues; ++q) AL(queues[q], 4 * n);
+    AL(counts, 4 * 8);
+    AL(tile_new, 4 * (size_t)c->ntiles);
+    AL(scalars, 8 * 8);
+    AL(err, 16);
+    c->npix = cam->image_w * cam->image_h;
+    AL(accum, 32 * (size_t)c->npix);
+#undef AL
+    PathsView& p = c->pv;
+    p.ro = c->ro.as<float4>();
+    p.rd = c->rd.as<float4>();
+    p.T = c->T.as<float4>();
+    p.L = c->L.as<float4>();
+    p.ng = c->ng.as<float4>();
+    p.rng = c->rng.as<uint4>();
+    p.vols = c->vols.as<int4>();
+    p.qid = c->qid.as<uint8_t>();
+    p.n = c->npaths;
+    QueueView& q = c->qv;
+    for (int i = 0; i < kNumQueues; ++i) q.items[i] = c->queues[i].as<uint32_t>();
+    q.counts = c->counts.as<uint32_t>();
+    q.tile_new = c->tile_new.as<uint32_t>();
+    q.ntiles = c->ntiles;
+    unsigned long long* sc = c->scalars.as<unsigned long long>();
+    q.next_pixel = sc + 0;
+    q.step_base = sc + 1;
+    RenderParams& rp = c->rp;
+    CameraD& cd = rp.cam;
+    for (int i = 0; i < 3; ++i) {
+        cd.eye[i] = cam->eye[i];
+        cd.up[i] = cam->up[i];
+        cd.right[i] = cam->right[i];
+        cd.o[i] = cam->imageplane_o[i];
+        cd.r[i] = cam->imageplane_r[i];
+        cd.b[i] = cam->imageplane_b[i];
+    }
+    cd.w = cam->image_w;
+    cd.h = cam->image_h;
+    rp.dof = k.dof;
+    rp.rr_depth = k.rr_depth;
+    rp.radiance_clamp = k.radiance_clamp;
+    rp.env_p = k.env_select_prob;
+    rp.max_depth = k.max_depth;
+    rp.sample_limit = k.spp ? (unsigned long long)k.spp * c->npix : 0ull;
+    rp.accum = c->accum.as<double>();
+    rp.err = c->err.as<uint32_t>();
+    rp.rays = sc + 2;
+    RGR_CUDA(cudaMemsetAsync(c->accum.p, 0, 32 * (size_t)c->npix, st));
+    RGR_CUDA(cudaMemsetAsync(c->counts.p, 0, 32, st));
+    RGR_CUDA(cudaMemsetAsync(c->scalars.p, 0, 64, st));
+    RGR_CUDA(cudaMemsetAsync(c->err.p, 0, 16, st));
+    launch_init(p, q, k.seed_offset, st);
+    RGR_CUDA(cudaGetLastError());
+    c->shade_grid = c->num_sms * 8;
+    c->steps = 0;
+    c->begun = true;
+    c->drop_graph();
+    return RGR_OK;
+}
+
+int rgr_render_step(rgr_context* c, int32_t steps) {
+    if (!c || steps < 0) return RGR_E_INVALID;
+    if (!c->begun) return RGR_E_STATE;
+    RGR_CUDA(cudaSetDevice(c->device));
+    cudaStream_t st = c->stream;
+    for (int32_t i = 0; i < steps; ++i) {
+        if (c->graph_mode) {
+            if (!c->graph_exec) {
+                cudaGraph_t g = nullptr;
+                RGR_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+                int r = c->step_launches(st);
+                cudaError_t e = cudaStreamEndCapture(st, &g);
+                if (r != RGR_OK) return r;
+                RGR_CUDA(e);
+                e = cudaGraphInstantiate(&c->graph_exec, g, 0);
+                cudaGraphDestroy(g);
+                RGR_CUDA(e);
+            }
+            RGR_CUDA(cudaGraphLaunch(c->graph_exec, st));
+        } else {
+            int r = c->step_launches(st);
+            if (r != RGR_OK) return r;
+        }
+        c->steps++;
+    }
+    return RGR_OK;
+}
+
+int rgr_synchronize(rgr_context* c) {
+    if (!c) return RGR_E_INVALID;
+    RGR_CUDA(cudaSetDevice(c->device));
+    RGR_CUDA(cudaStreamSynchronize(c->stream));
+    uint32_t err = 0;
+    if (c->begun) {
+        RGR_CUDA(cudaMemcpy(&err, c->err.p, 4, cudaMemcpyDeviceToHost));
+        if (err) {
+            set_error("device capacity check fired (flags " + std::to_string(err) + ")");
+            return RGR_E_OVERFLOW;
+        }
+    }
+    return RGR_OK;
+}
+
+int rgr_render_until_done(rgr_context* c, int32_t max_steps, int32_t* steps_done) {
+    if (!c || max_steps < 0) return RGR_E_INVALID;
+    if (!c->begun || c->rp.sample_limit == 0) return RGR_E_STATE;
+    int32_t done = 0;
+    while (done < max_steps) {
+        int batch = std::min<int32_t>(8, max_steps - done);
+        int r = rgr_render_step(c, batch);
+        if (r != RGR_OK) return r;
+        done += batch;
+        uint32_t counts[8];
+        unsigned long long np = 0;
+        RGR_CUDA(cudaMemcpyAsync(counts, c->counts.p, 32, cudaMemcpyDeviceToHost, c->stream));
+        RGR_CUDA(cudaMemcpyAsync(&np, c->scalars.p, 8, cudaMemcpyDeviceToHost, c->stream));
+        RGR_CUDA(cudaStreamSynchronize(c->stream));
+        uint64_t live = 0;
+        for (int k = 1; k < kNumQueues; ++k) live += counts[k];
+        if (np >= c->rp.sample_limit && live == 0) break;
+    }
+    if (steps_done) *steps_done = done;
+    return rgr_synchronize(c);
+}
+
+int rgr_render_readback(rgr_context* c, int32_t fmt, void* dst, uint64_t dst_bytes) {
+    if (!c || !dst) return RGR_E_INVALID;
+    if (!c->begun) return RGR_E_STATE;
+    RGR_CUDA(cudaSetDevice(c->device));
+    cudaStream_t st = c->stream;
+    const size_t npix = c->npix;
+    if (fmt == RGR_FMT_FP64_SUMS) {
+        if (dst_bytes < 32 * npix) return RGR_E_INVALID;
+        RGR_CUDA(cudaMemcpyAsync(dst, c->accum.p, 32 * npix, cudaMemcpyDeviceToHost, st));
+    } else if (fmt == RGR_FMT_RGBA8 || fmt == RGR_FMT_RGB16) {
+        size_t bytes = (fmt == RGR_FMT_RGBA8 ? 4 : 8) * npix;
+        if (dst_bytes < bytes) return RGR_E_INVALID;
+        int r = c->tread.alloc(bytes);
+        if (r != RGR_OK) return r;
+        launch_readback(fmt, c->accum.as<double>(), (uint32_t)npix, c->tread.p, st);
+        RGR_CUDA(cudaGetLastError());
+        RGR_CUDA(cudaMemcpyAsync(dst, c->tread.p, bytes, cudaMemcpyDeviceToHost, st));
+    } else {
+        return RGR_E_INVALID;
+    }
+    return rgr_synchronize(c);
+}
+
+int rgr_render_stats(rgr_context* c, rgr_stats* s) {
+    if (!c || !s) return RGR_E_INVALID;
+    memset(s, 0, sizeof(*s));
+    if (!c->begun) return RGR_E_STATE;
+    RGR_CUDA(cudaSetDevice(c->device));
+    cudaStream_t st = c->stream;
+    int r = c->tread.alloc(std::max<size_t>(c->tread.bytes, 64));
+    if (r != RGR_OK) return r;
+    RGR_CUDA(cudaMemsetAsync(c->tread.p, 0, 8, st));
+    launch_sum_counts(c->accum.as<double>(), c->npix, c->tread.as<unsigned long long>(), st);
+    RGR_CUDA(cudaGetLastError());
+    unsigned long long vals[3] = {0, 0, 0}, total = 0;
+    uint32_t counts[8], err = 0;
+    RGR_CUDA(cudaMemcpyAsync(vals, c->scalars.p, 24, cudaMemcpyDeviceToHost, st));
+    RGR_CUDA(cudaMemcpyAsync(&total, c->tread.p, 8, cudaMemcpyDeviceToHost, st));
+    RGR_CUDA(cudaMemcpyAsync(counts, c->counts.p, 32, cudaMemcpyDeviceToHost, st));
+    RGR_CUDA(cudaMemcpyAsync(&err, c->err.p, 4, cudaMemcpyDeviceToHost, st));
+    RGR_CUDA(cudaStreamSynchronize(st));
+    s->steps = c->steps;
+    s->paths_started = vals[0];
+    s->rays_traced = vals[2];
+    s->samples_accumulated = total;
+    s->avg_spp = (double)total / (double)c->npix;
+    uint64_t live = 0;
+    for (int k = 0; k < kNumQueues; ++k) live += counts[k];
+    s->active_paths = (uint32_t)std::min<uint64_t>(live, c->npaths);
+    s->error_flags = err;
+    return RGR_OK;
+}
+
+int rgr_accum_merge(rgr_context* dst, rgr_context* src) {
+    if (!dst || !src || !dst->begun || !src->begun || dst->npix != src->npix) return RGR_E_INVALID;
+    RGR_CUDA(cudaSetDevice(src->device));
+    RGR_CUDA(cudaStreamSynchronize(src->stream));
+    RGR_CUDA(cudaSetDevice(dst->device));
+    int r = dst->tread.alloc(32 * (size_t)dst->npix);
+    if (r != RGR_OK) return r;
+    RGR_CUDA(cudaMemcpyPeerAsync(dst->tread.p, dst->device, src->accum.p, src->device, 32 * (size_t)src->npix,
+                                 dst->stream));
+    launch_accum_add(dst->accum.as<double>(), dst->tread.as<double>(), dst->npix, dst->stream);
+    RGR_CUDA(cudaGetLastError());
+    return rgr_synchronize(dst);
+}
+
+int rgr_trace_closest_device(rgr_context* c, const rgr_ray_soa* rays, uint64_t n, int32_t* prim, float* t,
+                             float* ng_xyz, void* stream) {
+    if (!c || !rays || !prim || !t) return RGR_E_INVALID;
+    if (!c->uploaded) return RGR_E_STATE;
+    if (n == 0) return RGR_OK;
+    if (!rays->ox || !rays->oy || !rays->oz || !rays->dx || !rays->dy || !rays->dz || !rays->tmax)
+        return RGR_E_INVALID;
+    RGR_CUDA(cudaSetDevice(c->device));
+    cudaStream_t st = stream ? (cudaStream_t)stream : c->stream;
+    int r = c->err.alloc(16);
+    if (r != RGR_OK) return r;
+    launch_trace_rays(c->sv, rays->ox, rays->oy, rays->oz, rays->dx, rays->dy, rays->dz, rays->tmax, n, prim, t, ng_xyz,
+                      c->err.as<uint32_t>(), 128, st);
+    RGR_CUDA(cudaGetLastError());
+    return RGR_OK;
+}
+
+int rgr_trace_closest(rgr_context* c, const rgr_ray_soa* rays, uint64_t n, int32_t* prim, float* t) {
+    if (!c || !rays || !prim || !t) return RGR_E_INVALID;
+    if (!c->uploaded) return RGR_E_STATE;
+    if (n == 0) return RGR_OK;
+    RGR_CUDA(cudaSetDevice(c->device));
+    cudaStream_t st = c->stream;
+    const float* src[7] = {rays->ox, rays->oy, rays->oz, rays->dx, rays->dy, rays->dz, rays->tmax};
+    int r;
+    for (int k = 0; k < 7; ++k) {
+        if (!src[k]) return RGR_E_INVALID;
+        if ((r = c->trays[k].upload(src[k], 4 * n, st)) != RGR_OK) return r;
+    }
+    if ((r = c->tprim.alloc(4 * n)) != RGR_OK) return r;
+    if ((r = c->tt.alloc(4 * n)) != RGR_OK) return r;
+    rgr_ray_soa d{c->trays[0].as<float>(), c->trays[1].as<float>(), c->trays[2].as<float>(), c->trays[3].as<float>(),
+                  c->trays[4].as<float>(), c->trays[5].as<float>(), c->trays[6].as<float>()};
+    if ((r = c->err.alloc(16)) != RGR_OK) return r;
+    RGR_CUDA(cudaMemsetAsync(c->err.p, 0, 4, st));
+    r = rgr_trace_closest_device(c, &d, n, c->tprim.as<int32_t>(), c->tt.as<float>(), nullptr, st);
+    if (r != RGR_OK) return r;
+    uint32_t err = 0;
+    RGR_CUDA(cudaMemcpyAsync(prim, c->tprim.p, 4 * n, cudaMemcpyDeviceToHost, st));
+    RGR_CUDA(cudaMemcpyAsync(t, c->tt.p, 4 * n, cudaMemcpyDeviceToHost, st));
+    RGR_CUDA(cudaMemcpyAsync(&err, c->err.p, 4, cudaMemcpyDeviceToHost, st));
+    RGR_CUDA(cudaStreamSynchronize(st));
+    if (err) {
+        set_error("traversal stack overflow");
+        return RGR_E_OVERFLOW;
+    }
+    return RGR_OK;
+}
+
+int rgr_debug_read_slots(rgr_context* c, uint32_t* out, uint64_t nslots) {
+    if (!c || !out) return RGR_E_INVALID;
+    if (!c->begun) return RGR_E_STATE;
+    if (nslots < c->npaths) return RGR_E_INVALID;
+    RGR_CUDA(cudaSetDevice(c->device));
+    cudaStream_t st = c->stream;
+    size_t bytes = 34 * 4 * (size_t)c->npaths;
+    int r = c->tread.alloc(bytes);
+    if (r != RGR_OK) return r;
+    launch_debug_slots(c->pv, c->tread.as<uint32_t>(), st);
+    RGR_CUDA(cudaGetLastError());
+    RGR_CUDA(cudaMemcpyAsync(out, c->tread.p, bytes, cudaMemcpyDeviceToHost, st));
+    return rgr_synchronize(c);
+}
+
+}  // extern "C"

@@ -1,0 +1,304 @@
+// scene.cpp — the scene half of the C ABI (rgr_scene_*), replacing
+// rt::SceneManager (common/scene_manager.hpp:330-672).
+#include "../rgr_internal.h"
+
+#include <cmath>
+#include <cstring>
+#include <mutex>
+
+namespace rgr {
+namespace {
+thread_local std::string g_last_error;
+
+// MaterialStorage::add (scene_manager.hpp:148-160): one record per primitive,
+// index = running count of that material type.
+int add_material(rgr_scene* s, const rgr_material& m, MaterialRef* out) {
+    switch (m.type) {
+        case RGR_MAT_LAMBERTIAN: {
+            LambertianD d;
+            for (int k = 0; k < 3; ++k) {
+                d.le[k] = m.le[k];
+                d.r[k] = m.r[k];
+            }
+            d.le[3] = d.r[3] = 0.0f;
+            *out = MaterialRef{RGR_MAT_LAMBERTIAN, (int32_t)s->lambertians.size()};
+            s->lambertians.push_back(d);
+            return RGR_OK;
+        }
+        case RGR_MAT_SPECULAR:
+            *out = MaterialRef{RGR_MAT_SPECULAR, s->num_speculars++};
+            return RGR_OK;
+        case RGR_MAT_DIELECTRIC:
+            *out = MaterialRef{RGR_MAT_DIELECTRIC, s->num_dielectrics++};
+            return RGR_OK;
+        case RGR_MAT_WARD: {
+            WardD d;
+            d.alpha = m.alpha;
+            d.falloff = m.falloff;
+            d.pad0 = d.pad1 = 0.0f;
+            for (int k = 0; k < 3; ++k) {
+                d.reflectance[k] = m.r[k];
+                d.edgetint[k] = m.edgetint[k];
+            }
+            d.reflectance[3] = d.edgetint[3] = 0.0f;
+            *out = MaterialRef{RGR_MAT_WARD, (int32_t)s->wards.size()};
+            s->wards.push_back(d);
+            return RGR_OK;
+        }
+        case RGR_MAT_HOMOGENEOUS_VOLUME: {
+            VolumeD d;
+            for (int k = 0; k < 3; ++k) d.r[k] = m.r[k];
+            d.c = m.c;
+            *out = MaterialRef{RGR_MAT_HOMOGENEOUS_VOLUME, (int32_t)s->volumes.size()};
+            s->volumes.push_back(d);
+            return RGR_OK;
+        }
+        default:
+            set_error("unknown material type " + std::to_string(m.type));
+            return RGR_E_INVALID;
+    }
+}
+}  // namespace
+
+void set_error(const std::string& msg) { g_last_error = msg; }
+const char* last_error() { return g_last_error.c_str(); }
+
+}  // namespace rgr
+
+using namespace rgr;
+
+extern "C" {
+
+const char* rgr_last_error(void) { return rgr::last_error(); }
+
+const char* rgr_status_string(int st) {
+    switch (st) {
+        case RGR_OK: return "ok";
+        case RGR_E_INVALID: return "invalid argument";
+        case RGR_E_CUDA: return "CUDA error";
+        case RGR_E_OOM: return "out of memory";
+        case RGR_E_STATE: return "call out of order";
+        case RGR_E_OVERFLOW: return "device capacity check fired";
+        case RGR_E_NODEVICE: return "no CUDA device";
+        default: return "unknown status";
+    }
+}
+
+void rgr_bvh_params_default(rgr_bvh_params* p) {
+    if (!p) return;
+    p->max_leaf_size = 4;
+    p->sah_bins = 32;
+    p->traversal_cost = 1.0f;
+    p->intersect_cost = 1.0f;
+    p->max_depth = 63;
+    p->num_threads = 0;
+}
+
+int rgr_scene_create(rgr_scene** out) {
+    if (!out) return RGR_E_INVALID;
+    try {
+        *out = new rgr_scene();
+    } catch (...) {
+        return RGR_E_OOM;
+    }
+    return RGR_OK;
+}
+
+void rgr_scene_destroy(rgr_scene* s) { delete s; }
+
+int rgr_scene_add_mesh(rgr_scene* s, const float* P, uint64_t nverts, const uint32_t* idx, uint64_t ntris,
+                       const rgr_material* per_tri) {
+    if (!s || (nverts && !P) || (ntris && (!idx || !per_tri))) {
+        set_error("rgr_scene_add_mesh: null pointer");
+        return RGR_E_INVALID;
+    }
+    if (!s->spheres.empty()) {
+        // primitive ids: triangles first, then spheres (sphereBegin, scene_manager.hpp:551)
+        set_error("rgr_scene_add_mesh: add meshes before spheres");
+        return RGR_E_STATE;
+    }
+    for (uint64_t i = 0; i < 3 * ntris; ++i) {
+        if (idx[i] >= nverts) {
+            set_error("rgr_scene_add_mesh: index out of range");
+            return RGR_E_INVALID;
+        }
+    }
+    for (uint64_t i = 0; i < 3 * nverts; ++i) {
+        if (!std::isfinite(P[i])) {
+            set_error("rgr_scene_add_mesh: non-finite vertex");
+            return RGR_E_INVALID;
+        }
+    }
+    try {
+        uint32_t base = (uint32_t)(s->points.size() / 3);
+        std::vector<MaterialRef> refs(ntris);
+        for (uint64_t t = 0; t < ntris; ++t) {
+            int st = add_material(s, per_tri[t], &refs[t]);
+            if (st != RGR_OK) return st;
+        }
+        s->points.insert(s->points.end(), P, P + 3 * nverts);
+        s->indices.reserve(s->indices.size() + 3 * ntris);
+        for (uint64_t i = 0; i < 3 * ntris; ++i) s->indices.push_back(base + idx[i]);
+        s->tri_materials.insert(s->tri_materials.end(), refs.begin(), refs.end());
+        s->bvh.built = false;
+    } catch (...) {
+        return RGR_E_OOM;
+    }
+    return RGR_OK;
+}
+
+int rgr_scene_add_spheres(rgr_scene* s, const float* xyzr, uint64_t n, const rgr_material* per_sphere) {
+    if (!s || (n && (!xyzr || !per_sphere))) return RGR_E_INVALID;
+    for (uint64_t i = 0; i < 4 * n; ++i) {
+        if (!std::isfinite(xyzr[i])) {
+            set_error("rgr_scene_add_spheres: non-finite value");
+            return RGR_E_INVALID;
+        }
+    }
+    try {
+        for (uint64_t i = 0; i < n; ++i) {
+            MaterialRef r;
+            int st = add_material(s, per_sphere[i], &r);
+            if (st != RGR_OK) return st;
+            s->sphere_materials.push_back(r);
+        }
+        s->spheres.insert(s->spheres.end(), xyzr, xyzr + 4 * n);
+        s->bvh.built = false;
+    } catch (...) {
+        return RGR_E_OOM;
+    }
+    return RGR_OK;
+}
+
+int rgr_scene_set_envmap(rgr_scene* s, const float* rgba, int32_t w, int32_t h, float clamp_max, float scale) {
+    if (!s) return RGR_E_INVALID;
+    if (!rgba) {
+        s->env = EnvTables();
+        return RGR_OK;
+    }
+    if (w <= 0 || h <= 0 || (int64_t)w * h > (1ll << 26)) {
+        set_error("rgr_scene_set_envmap: bad size");
+        return RGR_E_INVALID;
+    }
+    EnvTables env;
+    env.present = true;
+    env.w = w;
+    env.h = h;
+    env.rgba.assign(rgba, rgba + 4 * (size_t)w * h);
+    // Image2D::clamp_rgb then scale (image2d.hpp:36-49, scene_manager.hpp:467-471)
+    for (size_t i = 0; i < (size_t)w * h; ++i) {
+        for (int k = 0; k < 3; ++k) {
+            float v = env.rgba[4 * i + k];
+            v = v < 0.0f ? 0.0f : v;
+            v = clamp_max < v ? clamp_max : v;
+            if (scale != 1.0f) v *= scale;
+            env.rgba[4 * i + k] = v;
+        }
+    }
+    int st = build_envmap_tables(env);
+    if (st != RGR_OK) return st;
+    s->env = std::move(env);
+    return RGR_OK;
+}
+
+int rgr_scene_build_bvh(rgr_scene* s, const rgr_bvh_params* p) {
+    if (!s) return RGR_E_INVALID;
+    rgr_bvh_params d;
+    rgr_bvh_params_default(&d);
+    try {
+        return build_bvh(s, p ? *p : d);
+    } catch (const std::bad_alloc&) {
+        return RGR_E_OOM;
+    }
+}
+
+int rgr_scene_get_info(const rgr_scene* s, rgr_scene_info* info) {
+    if (!s || !info) return RGR_E_INVALID;
+    memset(info, 0, sizeof(*info));
+    info->num_triangles = s->indices.size() / 3;
+    info->num_spheres = s->spheres.size() / 4;
+    info->num_vertices = s->points.size() / 3;
+    info->num_nodes_stackless = s->bvh.ref_nodes.size();
+    info->num_inner_nodes = s->bvh.nodes.size();
+    info->num_leaves = s->bvh.num_leaves;
+    info->depth = s->bvh.depth;
+    info->sphere_begin = (int32_t)info->num_triangles;
+    memcpy(info->bounds, s->bvh.bounds, sizeof(info->bounds));
+    info->sah_cost = s->bvh.sah_cost;
+    return RGR_OK;
+}
+
+int rgr_bvh_export_stackless(const rgr_scene* s, rgr_stackless_node* nodes, uint64_t node_cap, uint32_t* prim_ids,
+                             uint64_t prim_cap) {
+    if (!s || !s->bvh.built) return RGR_E_STATE;
+    if (node_cap < s->bvh.ref_nodes.size() || prim_cap < s->bvh.ref_prim_ids.size()) return RGR_E_INVALID;
+    if (!s->bvh.ref_nodes.empty())
+        memcpy(nodes, s->bvh.ref_nodes.data(), sizeof(rgr_stackless_node) * s->bvh.ref_nodes.size());
+    if (!s->bvh.ref_prim_ids.empty())
+        memcpy(prim_ids, s->bvh.ref_prim_ids.data(), 4 * s->bvh.ref_prim_ids.size());
+    return RGR_OK;
+}
+
+int rgr_scene_export_envmap(const rgr_scene* s, float* pdf, float* height, int32_t* alias, float* frag) {
+    if (!s || !s->env.present) return RGR_E_STATE;
+    size_t n = (size_t)s->env.w * s->env.h;
+    if (pdf) memcpy(pdf, s->env.pdf.data(), 4 * 7 * n);
+    if (height) memcpy(height, s->env.height.data(), 4 * 7 * n);
+    if (alias) memcpy(alias, s->env.alias.data(), 4 * 7 * n);
+    if (frag) memcpy(frag, s->env.frag.data(), 4 * 4 * n);
+    return RGR_OK;
+}
+
+void rgr_render_config_default(rgr_render_config* c) {
+    if (!c) return;
+    c->dof = 0.0045f;
+    c->rr_depth = 25;
+    c->radiance_clamp = 1000.0f;
+    c->env_select_prob = 0.5f;
+    c->max_depth = 0;
+    c->seed_offset = 0;
+    c->spp = 0;
+}
+
+// A pinhole camera in the reference StandardCamera form (wavefront_path_tracing.hpp:103-118):
+// image plane at focus distance 1 with height 2*tan(vfov/2).
+int rgr_camera_look_at(rgr_camera* c, const float eye[3], const float target[3], const float up[3], float vfov_deg,
+                       uint32_t image_w, uint32_t image_h) {
+    if (!c || !eye || !target || !up || image_w == 0 || image_h == 0) return RGR_E_INVALID;
+    double f[3], r[3], u[3];
+    double len = 0;
+    for (int k = 0; k < 3; ++k) {
+        f[k] = (double)target[k] - eye[k];
+        len += f[k] * f[k];
+    }
+    len = std::sqrt(len);
+    if (!(len > 0)) return RGR_E_INVALID;
+    for (int k = 0; k < 3; ++k) f[k] /= len;
+    // right = forward x up, true up = right x forward
+    r[0] = f[1] * up[2] - f[2] * up[1];
+    r[1] = f[2] * up[0] - f[0] * up[2];
+    r[2] = f[0] * up[1] - f[1] * up[0];
+    len = std::sqrt(r[0] * r[0] + r[1] * r[1] + r[2] * r[2]);
+    if (!(len > 0)) return RGR_E_INVALID;
+    for (int k = 0; k < 3; ++k) r[k] /= len;
+    u[0] = r[1] * f[2] - r[2] * f[1];
+    u[1] = r[2] * f[0] - r[0] * f[2];
+    u[2] = r[0] * f[1] - r[1] * f[0];
+    double ph = 2.0 * std::tan(vfov_deg * 3.14159265358979323846 / 360.0);
+    double pw = ph * (double)image_w / (double)image_h;
+    for (int k = 0; k < 3; ++k) {
+        c->eye[k] = eye[k];
+        c->forward[k] = (float)f[k];
+        c->up[k] = (float)u[k];
+        c->right[k] = (float)r[k];
+        // imageplane_o = eye + forward*focus + left*w/2 + up*h/2; left = -right
+        c->imageplane_o[k] = (float)(eye[k] + f[k] - r[k] * pw * 0.5 + u[k] * ph * 0.5);
+        c->imageplane_r[k] = (float)(r[k] * pw / image_w);
+        c->imageplane_b[k] = (float)(-u[k] * ph / image_h);
+    }
+    c->image_w = image_w;
+    c->image_h = image_h;
+    return RGR_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,835 @@
+// wavefront.cu — the per-bounce kernels of the wavefront path tracer (sm_103a).
+//
+// One reference step() (common/wavefront_path_tracing.hpp:591-939) is about
+// twenty launches of 2^22 work items.  Here it is three kernels and a memset:
+//   1. compact_new  — ordered compaction of the slots logic marked "new path"
+//      (slot order, so pixels are assigned exactly as a sequential run of
+//      new_path.cl:41-43 over that queue would);
+//   2. shade        — persistent kernel draining the new-path queue and the six
+//      material queues back to back; per item it runs, in the reference stage
+//      order, new_path / strategy_selection / envmap sample / BSDF sample or
+//      pdf / envmap pdf / material stage / homogeneous_volume_through, keeping
+//      IncidentSample and ShadingResult in registers;
+//   3. trace_logic  — closest-hit traversal fused with logic.cl: throughput
+//      update, envmap on miss, Russian roulette, FP64 per-pixel accumulation,
+//      and warp-aggregated enqueue into next step's material queues.
+// Every slot's arithmetic is the reference kernels' arithmetic (see the
+// file:line notes); the translation unit is built with --fmad=false.
+#include <cuda_fp16.h>
+
+#include "wavefront.cuh"
+#include "traverse.cuh"
+
+namespace rgr {
+namespace dev {
+namespace {
+
+using namespace rgr::fm;
+
+constexpr float kPiF = 3.14159274f;                 // (float)(M_PI)
+constexpr float kPdfUniformSphere = 0.0795774683f;  // (float)(1.0 / (M_PI * 4.0))
+constexpr float kFourPiF = 12.566371f;              // (float)(4.0 * M_PI)
+constexpr double kPiD = 3.14159265358979323846;     // M_PI
+constexpr float kFltMax = 3.40282347e+38f;
+
+enum { kBxdf = 0, kEnv = 1, kNone = 2 };
+enum { kMatLambertian = 1, kMatSpecular = 2, kMatDielectric = 3, kMatWard = 4, kMatVolume = 5, kMatVolumeInside = 6 };
+
+RGR_DEV f3 mix3(f3 a, f3 b, float t) { return mk(mix_(a.x, b.x, t), mix_(a.y, b.y, t), mix_(a.z, b.z, t)); }
+RGR_DEV float sqr(float x) { return x * x; }
+RGR_DEV int to_int(float x) {
+    if (isnan(x)) return 0;
+    if (x >= 2147483648.0f) return 2147483647;
+    if (x <= -2147483648.0f) return (-2147483647 - 1);
+    return (int)x;
+}
+
+// ------------------------------------------------------------ envmap
+// cartesian_to_polar (envmap_sampling.cl:25-34)
+RGR_DEV void cartesian_to_polar(f3 rd, float& theta, float& phi) {
+    float z = rd.y, x = rd.z, y = rd.x;
+    theta = atan2_(sqrtf(x * x + y * y), z);
+    phi = atan2_(y, x);
+    if (!is_finite(phi)) phi = 0.0f;
+}
+// envmap_index (envmap_sampling.cl:75-95)
+RGR_DEV int envmap_index(f3 wi, int width, int height) {
+    float theta, phi;
+    cartesian_to_polar(wi, theta, phi);
+    float u = 1.0f - phi / (2.0f * kPiF);
+    float v = theta / kPiF;
+    int ix = to_int(floorf(u * (float)width));
+    int iy = to_int(floorf(v * (float)height));
+    int r = ix % width;
+    ix = r < 0 ? r + width : r;
+    iy = min(max(iy, 0), height - 1);
+    return iy * width + ix;
+}
+RGR_DEV f3 texel(const SceneView& sc, int i, int j) { return xyz(__ldg(sc.env_rgba + (size_t)j * sc.env_w + i)); }
+// get_envmap_value (envmap_sampling.cl:36-52): read_imagef with normalized
+// coordinates, CLK_ADDRESS_REPEAT, nearest or bilinear (OpenCL 1.2 sampler
+// formulas, FP32 weights)
+RGR_DEV f3 envmap_value(const SceneView& sc, f3 rd, bool linear) {
+    float theta, phi;
+    cartesian_to_polar(rd, theta, phi);
+    float su = 1.0f - phi / (2.0f * kPiF);
+    float sv = theta / kPiF;
+    const int w = sc.env_w, h = sc.env_h;
+    float u = (su - floorf(su)) * (float)w;
+    float v = (sv - floorf(sv)) * (float)h;
+    if (!linear) {
+        int i = to_int(floorf(u)), j = to_int(floorf(v));
+        if (i > w - 1) i = i - w;
+        if (j > h - 1) j = j - h;
+        i = min(max(i, 0), w - 1);
+        j = min(max(j, 0), h - 1);
+        return texel(sc, i, j);
+    }
+    float uu = u - 0.5f, vv = v - 0.5f;
+    int i0 = to_int(floorf(uu)), j0 = to_int(floorf(vv));
+    int i1 = i0 + 1, j1 = j0 + 1;
+    if (i0 < 0) i0 = w + i0;
+    if (i1 > w - 1) i1 = i1 - w;
+    if (j0 < 0) j0 = h + j0;
+    if (j1 > h - 1) j1 = j1 - h;
+    i0 = min(max(i0, 0), w - 1);
+    i1 = min(max(i1, 0), w - 1);
+    j0 = min(max(j0, 0), h - 1);
+    j1 = min(max(j1, 0), h - 1);
+    float a = uu - floorf(uu), b = vv - floorf(vv);
+    float w00 = (1.0f - a) * (1.0f - b), w10 = a * (1.0f - b);
+    float w01 = (1.0f - a) * b, w11 = a * b;
+    return ((texel(sc, i0, j0) * w00 + texel(sc, i1, j0) * w10) + texel(sc, i0, j1) * w01) + texel(sc, i1, j1) * w11;
+}
+// alias_method (envmap_sampling.cl:54-66); table t of 7
+RGR_DEV uint32_t alias_method(const SceneView& sc, size_t base, Rng& st, uint32_t count) {
+    uint32_t idx = (uint32_t)(st.uniform_integer() % (uint64_t)count);
+    int2 b = __ldg(sc.env_alias + base + idx);
+    if (b.y < 0) return idx;
+    float u = st.uniform();
+    if (u < __int_as_float(b.x)) return idx;
+    return (uint32_t)b.y;
+}
+// sample_from_fragment (envmap_sampling.cl:68-73, 158-167)
+RGR_DEV f3 sample_from_fragment(const SceneView& sc, uint32_t idx, Rng& st) {
+    float4 fr = __ldg(sc.env_frag + idx);
+    float y = mix_(fr.x, fr.y, st.uniform());
+    float phi = mix_(fr.z, fr.w, st.uniform());
+    float sp, cp;
+    sincos_(phi, &sp, &cp);
+    f3 p = mk(sp, y, cp);
+    float r_xz = sqrtf(fmax_(1.0f - p.y * p.y, 0.0f));
+    p.x *= r_xz;
+    p.z *= r_xz;
+    return p;
+}
+RGR_DEV void six_axis_bases(size_t count, f3 n, size_t& xb, size_t& yb, size_t& zb) {
+    xb = count * (0.0f < n.x ? 1 : 2);
+    yb = count * (0.0f < n.y ? 3 : 4);
+    zb = count * (0.0f < n.z ? 5 : 6);
+}
+
+// ------------------------------------------------------------ BSDFs
+// cosine_weighted_hemisphere_z_up (lambertian.cl:9-20)
+RGR_DEV f3 cosine_hemisphere(float a, float b) {
+    float r = sqrtf(a);
+    float theta = (float)((double)b * kPiD * 2.0);
+    float s, c;
+    sincos_(theta, &s, &c);
+    return mk(r * c, r * s, sqrtf(fmax_(1.0f - a, 0.0f)));
+}
+// get_orthonormal_basis (lambertian.cl:26-32)
+RGR_DEV void orthonormal_basis(f3 z, f3& xa, f3& ya) {
+    const float sign = copysign_(1.0f, z.z);
+    const float a = -1.0f / (sign + z.z);
+    const float b = z.x * z.y * a;
+    xa = mk(1.0f + sign * z.x * z.x * a, sign * b, -sign * z.x);
+    ya = mk(b, sign + z.y * z.y * a, -z.y);
+}
+RGR_DEV f3 reflect(f3 d, f3 n) { return d - (2.0f * dot(d, n)) * n; }
+// sample_ward (ward.cl:40-53)
+RGR_DEV f3 sample_ward(f3 wo, f3 zaxis, float alpha, float u0, float u1) {
+    float phiH = u0 * 2.0f * kPiF;
+    float thetaH = atan_(alpha * sqrtf(-log_(u1)));
+    float st, ct, sp, cp;
+    sincos_(thetaH, &st, &ct);
+    sincos_(phiH, &sp, &cp);
+    f3 hl = mk(st * cp, st * sp, ct);
+    f3 xa, ya;
+    orthonormal_basis(zaxis, xa, ya);
+    f3 h = xa * hl.x + ya * hl.y + zaxis * hl.z;
+    return reflect(-wo, h);
+}
+// pdf_ward (ward.cl:55-74)
+RGR_DEV float pdf_ward(f3 wo, f3 wi, f3 zaxis, float alpha) {
+    if (dot(wo, zaxis) * dot(wi, zaxis) < 0.0f) return 0.0f;
+    const float alpha2 = sqr(alpha);
+    f3 h = normalize(wi + wo);
+    float c = dot(h, zaxis);
+    float c2 = sqr(c);
+    float tan2 = (1.0f - c2) / c2;
+    float k0 = 1.0f / (4.0f * kPiF * alpha2 * dot(h, wi) * (c * c * c));
+    float k1 = exp_(-tan2 / alpha2);
+    return k0 * k1;
+}
+// fresnel_dielectrics, refract (delta_materials.cl:11-32)
+RGR_DEV float fresnel_dielectrics(float c, float eta_t, float eta_i) {
+    float g = sqrtf(eta_t * eta_t / sqr(eta_i) - 1.0f + sqr(c));
+    float a = 0.5f * sqr(g - c) / sqr(g + c);
+    float b = 1.0f + sqr(c * (g + c) - 1.0f) / sqr(c * (g - c) + 1.0f);
+    return a * b;
+}
+RGR_DEV bool refract(f3& out, f3 d, f3 n, float eta_i, float eta_t) {
+    float eta = eta_i / eta_t;
+    float NoD = dot(n, d);
+    float k = 1.0f - eta * eta * (1.0f - NoD * NoD);
+    if (k <= 0.0f) return false;
+    out = eta * d - (eta * NoD + sqrtf(k)) * n;
+    return true;
+}
+// uniform_on_unit_sphere (homogeneous_volume.cl:7-14)
+RGR_DEV f3 uniform_sphere(float u0, float u1) {
+    float phi = (float)((double)u0 * kPiD * 2.0);
+    float z = mix_(-1.0f, 1.0f, u1);
+    float r_xy = sqrtf(fmax_(1.0f - z * z, 0.0f));
+    float s, c;
+    sincos_(phi, &s, &c);
+    return mk(r_xy * c, r_xy * s, z);
+}
+RGR_DEV uint32_t volume_hash(float4 v) {  // types.cl:104-106 (C, R.x, R.y, R.z)
+    return __float_as_uint(v.w) ^ __float_as_uint(v.x) ^ __float_as_uint(v.y) ^ __float_as_uint(v.z);
+}
+
+struct Incident {
+    f3 wi;
+    float sel0, sel1, pdf0, pdf1;
+    int strategy;
+};
+RGR_DEV float incident_pdf(const Incident& is) {  // types.cl:65-71
+    float pdf = 0.0f;
+    pdf = pdf + is.sel0 * is.pdf0;
+    pdf = pdf + is.sel1 * is.pdf1;
+    return pdf;
+}
+
+// One slot's share of a step, from new_path to homogeneous_volume_through.
+// k: the queue the slot came from (0 = new path, else its material type).
+RGR_DEV void shade_slot(const SceneView& sc, const PathsView& P, const RenderParams& rp, int k, uint32_t slot,
+                        unsigned long long gpix) {
+    float4 ro4 = P.ro[slot], rd4 = P.rd[slot], T4 = P.T[slot], L4 = P.L[slot], ng4 = P.ng[slot];
+    int4 va = P.vols[2 * (size_t)slot], vb = P.vols[2 * (size_t)slot + 1];
+    Rng rng = rng_load(P.rng, slot);
+    f3 ro = xyz(ro4), rd = xyz(rd4), T = xyz(T4), L = xyz(L4), Ng = xyz(ng4);
+    float tmin = ro4.w;
+    int32_t hv = __float_as_int(rd4.w);
+    int32_t hs = __float_as_int(ng4.w);
+    uint32_t pixel = __float_as_uint(T4.w);
+    uint32_t logic_i = __float_as_uint(L4.w);
+    int vcount = vb.w;
+
+    if (k == 0) {  // new_path (new_path.cl:17-83)
+        const CameraD& cam = rp.cam;
+        T = mk(1, 1, 1);
+        L = mk(0, 0, 0);
+        logic_i = 0;
+        uint32_t npix = cam.w * cam.h;
+        pixel = (uint32_t)(gpix % (unsigned long long)npix);
+        uint32_t x = pixel % cam.w, y = pixel / cam.w;
+        float ux = rng.uniform();
+        float uy = rng.uniform();
+        f3 sop = mk(cam.o[0], cam.o[1], cam.o[2]) + mk(cam.r[0], cam.r[1], cam.r[2]) * ((float)x + ux) +
+                 mk(cam.b[0], cam.b[1], cam.b[2]) * ((float)y + uy);
+        float u0 = rng.uniform();
+        float u1 = rng.uniform();
+        float r = sqrtf(u0);
+        float theta = (float)((double)u1 * kPiD * 2.0);
+        float s, c;
+        sincos_(theta, &s, &c);
+        float lensx = rp.dof * r * c;
+        float lensy = rp.dof * r * s;
+        f3 lens = mk(cam.eye[0], cam.eye[1], cam.eye[2]) + mk(cam.up[0], cam.up[1], cam.up[2]) * lensx +
+                  mk(cam.right[0], cam.right[1], cam.right[2]) * lensy;
+        ro = lens;
+        rd = normalize(sop - lens);
+        vcount = 0;
+        hs = -1;
+        tmin = kFltMax;
+        Ng = mk(0, 0, 0);
+    }
+    f3 shLe = mk(0, 0, 0), shT = mk(1, 1, 1);
+
+    // strategy_selection (mixture_density.cl:7-133)
+    Incident is;
+    is.wi = mk(0, 0, 0);
+    is.sel0 = is.sel1 = is.pdf0 = is.pdf1 = 0.0f;
+    is.strategy = kNone;
+    const bool surface_hit = 0 <= hs, volume_hit = 0 <= hv;
+    int envq = -1;
+    if (surface_hit || volume_hit) {
+        const float env_p = sc.has_env ? rp.env_p : 0.0f;
+        if (surface_hit) {
+            int mt = __ldg(sc.materials + hs).x;
+            if (mt == kMatLambertian || mt == kMatWard) {
+                const float bxdf_p = 1.0f - env_p;
+                is.sel0 = bxdf_p;
+                is.sel1 = 1.0f - bxdf_p;
+            } else {
+                is.sel0 = 1.0f;
+                is.sel1 = 0.0f;
+            }
+        } else {
+            const float bxdf_p = 1.0f - env_p;
+            is.sel0 = bxdf_p;
+            is.sel1 = 1.0f - bxdf_p;
+        }
+        float u = rng.uniform();
+        is.strategy = (u <= is.sel0) ? kBxdf : kEnv;
+        if (is.sel1 != 0.0f) {
+            const int sq = volume_hit ? 0 : 2, eq = volume_hit ? 1 : 3;
+            envq = is.strategy == kEnv ? sq : eq;
+        }
+    }
+    const size_t count = (size_t)sc.env_w * sc.env_h;
+    // sample_envmap_6axis_stage / sample_envmap_stage (envmap_sampling.cl:169-248)
+    if (envq == 2) {
+        f3 n = Ng;
+        if (dot(n, -rd) < 0.0f) n = -n;
+        size_t xb, yb, zb;
+        six_axis_bases(count, n, xb, yb, zb);
+        float u = rng.uniform();
+        f3 ap = n * n;
+        size_t sel = (u < ap.x) ? xb : ((u < ap.x + ap.y) ? yb : zb);
+        uint32_t idx = alias_method(sc, sel, rng, (uint32_t)count);
+        float pdf = 0.0f;
+        pdf = pdf + ap.x * __ldg(sc.env_pdf + xb + idx);
+        pdf = pdf + ap.y * __ldg(sc.env_pdf + yb + idx);
+        pdf = pdf + ap.z * __ldg(sc.env_pdf + zb + idx);
+        is.wi = sample_from_fragment(sc, idx, rng);
+        is.pdf1 = pdf;
+    } else if (envq == 0) {
+        uint32_t idx = alias_method(sc, 0, rng, (uint32_t)count);
+        float pdf = __ldg(sc.env_pdf + idx);
+        is.wi = sample_from_fragment(sc, idx, rng);
+        is.pdf1 = pdf;
+    }
+    // BSDF sample or pdf
+    int2 mref = make_int2(0, 0);
+    if (k >= 1 && k <= 5) mref = __ldg(sc.materials + hs);
+    if (k == kMatLambertian) {  // sample_or_eval_lambertian_stage (lambertian.cl:34-71)
+        float cosTheta;
+        if (is.strategy == kBxdf) {
+            float u0 = rng.uniform();
+            float u1 = rng.uniform();
+            f3 wl = cosine_hemisphere(u0, u1);
+            f3 xa, ya;
+            orthonormal_basis(Ng, xa, ya);
+            is.wi = xa * wl.x + ya * wl.y + Ng * wl.z;
+            cosTheta = wl.z;
+        } else {
+            cosTheta = dot(Ng, is.wi);
+        }
+        is.pdf0 = fmax_(cosTheta, 0.0f) / kPiF;
+    } else if (k == kMatWard) {  // sample_or_eval_ward_stage (ward.cl:76-117)
+        float4 w0 = __ldg(sc.wards + 3 * (size_t)mref.y);
+        f3 wo = -rd;
+        f3 n = Ng;
+        if (dot(n, wo) < 0.0f) n = -n;
+        f3 wi;
+        if (is.strategy == kBxdf) {
+            float u0 = rng.uniform();
+            float u1 = rng.uniform();
+            wi = sample_ward(wo, n, w0.x, u0, u1);
+        } else {
+            wi = is.wi;
+        }
+        is.wi = wi;
+        is.pdf0 = pdf_ward(wo, wi, n, w0.x);
+    } else if (k == kMatVolumeInside) {  // homogeneous_volume.cl:66-88
+        if (is.strategy == kBxdf) {
+            float u0 = rng.uniform();
+            float u1 = rng.uniform();
+            is.wi = uniform_sphere(u0, u1);
+        }
+        is.pdf0 = kPdfUniformSphere;
+    }
+    // evaluate_envmap_6axis_pdf_stage / evaluate_envmap_pdf_stage (envmap_sampling.cl:250-281)
+    if (envq == 3) {
+        size_t xb, yb, zb;
+        six_axis_bases(count, Ng, xb, yb, zb);  // the raw Ng, as the reference does
+        f3 ap = Ng * Ng;
+        int index = envmap_index(is.wi, sc.env_w, sc.env_h);
+        float pdf = 0.0f;
+        pdf = pdf + ap.x * __ldg(sc.env_pdf + xb + index);
+        pdf = pdf + ap.y * __ldg(sc.env_pdf + yb + index);
+        pdf = pdf + ap.z * __ldg(sc.env_pdf + zb + index);
+        is.pdf1 = pdf;
+    } else if (envq == 1) {
+        is.pdf1 = __ldg(sc.env_pdf + envmap_index(is.wi, sc.env_w, sc.env_h));
+    }
+    // material stages
+    if (k == kMatLambertian) {  // lambertian_stage (lambertian.cl:73-123)
+        float4 le = __ldg(sc.lambertians + 2 * (size_t)mref.y), R = __ldg(sc.lambertians + 2 * (size_t)mref.y + 1);
+        f3 n = Ng;
+        if (dot(n, -rd) < 0.0f) n = -n;
+        f3 wi = is.wi;
+        float pdf = incident_pdf(is);
+        float cosTheta = dot(wi, n);
+        f3 Ts = mk(0, 0, 0);
+        if (0.0f < cosTheta) Ts = xyz(R) / kPiF * cosTheta / pdf;
+        shLe = xyz(le);
+        shT = Ts;
+        ro = ro + rd * tmin + wi * 1.0e-5f + n * 1.0e-5f;
+        rd = wi;
+    } else if (k == kMatWard) {  // ward_stage (ward.cl:119-186)
+        float4 w0 = __ldg(sc.wards + 3 * (size_t)mref.y);
+        float4 refl = __ldg(sc.wards + 3 * (size_t)mref.y + 1), edge = __ldg(sc.wards + 3 * (size_t)mref.y + 2);
+        f3 n = Ng;
+        f3 wo = -rd;
+        if (dot(n, wo) < 0.0f) n = -n;
+        f3 wi = is.wi;
+        float pdf = incident_pdf(is);
+        float cosTheta = dot(wi, n);
+        f3 Ts = mk(0, 0, 0);
+        if (0.0f < cosTheta) {
+            f3 lv = wi + wo;
+            f3 h = normalize(lv);
+            float alpha2 = sqr(w0.x);
+            float cth = dot(h, n);
+            float cth2 = sqr(cth);
+            float tan2 = (1.0f - cth2) / cth2;
+            float mu = dot(h, wi);
+            f3 rho = mix3(xyz(refl), xyz(edge), pow_(1.0f - mu, 1.0f / w0.y));
+            f3 k0 = rho / (kPiF * alpha2);
+            float k1 = exp_(-tan2 / alpha2);
+            float dn = dot(lv, n);
+            float k2 = dot(lv, lv) / sqr(sqr(dn));
+            Ts = k0 * k1 * k2 * cosTheta / pdf;
+        }
+        shT = Ts;
+        ro = ro + rd * tmin + wi * 1.0e-5f + n * 1.0e-5f;
+        rd = wi;
+    } else if (k == kMatVolume) {  // homogeneous_volume_stage (homogeneous_volume.cl:19-64)
+        bool backside = dot(Ng, -rd) < 0.0f;
+        int vols[8] = {va.x, va.y, va.z, va.w, vb.x, vb.y, vb.z, 0};
+        if (backside) {  // inVolumeList_Remove (types.cl:115-132)
+            uint32_t hsh = volume_hash(__ldg(sc.volumes + mref.y));
+            bool move = false;
+            for (int i = 0; i < vcount && i < 7; ++i) {
+                if (move) {
+                    vols[i - 1] = vols[i];
+                } else {
+                    int2 mi = __ldg(sc.materials + vols[i]);
+                    if (volume_hash(__ldg(sc.volumes + mi.y)) == hsh) move = true;
+                }
+            }
+            if (move) vcount--;
+        } else if (vcount < 7) {  // inVolumeList_Add (types.cl:108-114)
+            vols[vcount] = hs;
+            vcount++;
+        }
+        va = make_int4(vols[0], vols[1], vols[2], vols[3]);
+        vb = make_int4(vols[4], vols[5], vols[6], vcount);
+        ro = ro + rd * (tmin + 1.0e-5f);
+    } else if (k == kMatVolumeInside) {  // homogeneous_volume_inside_stage (homogeneous_volume.cl:90-129)
+        int2 mi = __ldg(sc.materials + hv);
+        float4 vol = __ldg(sc.volumes + mi.y);
+        float pdf = incident_pdf(is);
+        shT = xyz(vol) / kFourPiF / pdf;
+        ro = ro + rd * tmin;
+        rd = is.wi;
+    } else if (k == kMatSpecular) {  // delta_materials.cl:34-64
+        f3 n = Ng;
+        if (dot(n, -rd) < 0.0f) n = -n;
+        f3 wi = reflect(rd, n);
+        ro = ro + rd * tmin + wi * 1.0e-5f;
+        rd = wi;
+    } else if (k == kMatDielectric) {  // delta_materials.cl:66-121
+        f3 n = Ng;
+        f3 wo = -rd;
+        bool backside = dot(n, wo) < 0.0f;
+        float eta_i = 1.0f, eta_t = 1.5f;
+        if (backside) {
+            float e = eta_i;
+            eta_i = eta_t;
+            eta_t = e;
+            n = -n;
+        }
+        float f = fresnel_dielectrics(fabs_(dot(n, wo)), eta_t, eta_i);
+        float u = rng.uniform();
+        float rc = 1.0f;
+        f3 wi;
+        if (u < f) {
+            wi = reflect(rd, n);
+        } else if (!refract(wi, rd, n, eta_i, eta_t)) {
+            wi = reflect(rd, n);
+        } else {
+            rc = sqr(eta_t / eta_i);
+        }
+        shT = mk(rc, rc, rc);
+        ro = ro + rd * tmin + wi * 1.0e-5f;
+        rd = wi;
+    }
+    // logic.cl:31-33, applied here: the stage that made the shading result consumes it
+    L = L + T * shLe;
+    T = T * shT;
+
+    // homogeneous_volume_through (homogeneous_volume_through.cl:7-44)
+    hs = -1;
+    hv = -1;
+    if (0 < vcount) {
+        uint64_t u = rng.uniform_integer();
+        int sel = (int)(u % (uint64_t)vcount);
+        int vols[7] = {va.x, va.y, va.z, va.w, vb.x, vb.y, vb.z};
+        hv = vols[sel < 7 ? sel : 6];
+    }
+    tmin = kFltMax;
+    if (0 <= hv) {
+        int2 mi = __ldg(sc.materials + hv);
+        float4 vol = __ldg(sc.volumes + mi.y);
+        float u = rng.uniform();
+        tmin = -1.0f / vol.w * log_(u);
+    }
+    P.ro[slot] = f4(ro, tmin);
+    P.rd[slot] = f4(rd, __int_as_float(hv));
+    P.T[slot] = f4(T, __uint_as_float(pixel));
+    P.L[slot] = f4(L, __uint_as_float(logic_i));
+    P.ng[slot] = f4(Ng, __int_as_float(hs));
+    if (k == 0 || k == kMatVolume) {
+        P.vols[2 * (size_t)slot] = va;
+        P.vols[2 * (size_t)slot + 1] = vb;
+    }
+    rng_store(P.rng, slot, rng);
+}
+
+// ------------------------------------------------------------ kernels
+__global__ void k_init(PathsView P, QueueView Q, uint32_t seed_offset) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < Q.ntiles) {
+        uint32_t beg = i * kTile;
+        Q.tile_new[i] = min(kTile, P.n - beg);
+    }
+    if (i >= Q.ntiles * kTile) return;
+    if (i >= P.n) {
+        P.qid[i] = kQueueIdle;  // padding up to a whole tile
+        return;
+    }
+    // random_initialize (peseudo_random.cl:48-64)
+    unsigned long long x = (unsigned long long)seed_offset + i;
+    unsigned long long r[2];
+    for (int k = 0; k < 2; ++k) {
+        unsigned long long z = (x += 0x9e3779b97f4a7c15ull);
+        z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+        z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+        r[k] = z ^ (z >> 31);
+    }
+    uint4 s = make_uint4((uint32_t)r[0], (uint32_t)(r[0] >> 32), (uint32_t)r[1], (uint32_t)(r[1] >> 32));
+    if ((s.x | s.y | s.z | s.w) == 0u) s.x = 1u;
+    P.rng[i] = s;
+    P.ro[i] = make_float4(0, 0, 0, kFltMax);
+    P.rd[i] = make_float4(0, 0, 0, __int_as_float(-1));
+    P.T[i] = make_float4(0, 0, 0, 0);
+    P.L[i] = make_float4(0, 0, 0, 0);
+    P.ng[i] = make_float4(0, 0, 0, __int_as_float(-1));
+    P.vols[2 * (size_t)i] = make_int4(0, 0, 0, 0);
+    P.vols[2 * (size_t)i + 1] = make_int4(0, 0, 0, 0);
+    P.qid[i] = 0;  // initialize_all_as_new_path (new_path.cl:9-15)
+}
+
+// Ordered compaction of new-path slots: block t owns slots [t*4096, (t+1)*4096).
+__global__ void __launch_bounds__(256) k_compact_new(PathsView P, QueueView Q) {
+    __shared__ uint32_t s_warp[8];
+    __shared__ uint32_t s_prefix;
+    const uint32_t t = blockIdx.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    // prefix of the tile counts before this tile
+    uint32_t sum = 0;
+    for (uint32_t j = tid; j < t; j += 256) sum += Q.tile_new[j];
+    for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+    if (lane == 0) s_warp[warp] = sum;
+    __syncthreads();
+    if (tid == 0) {
+        uint32_t p = 0;
+        for (int w = 0; w < 8; ++w) p += s_warp[w];
+        s_prefix = p;
+    }
+    __syncthreads();
+    const uint32_t prefix = s_prefix;
+    // 16 consecutive slots per thread
+    const uint32_t base = t * kTile + tid * 16;
+    uint4 q = *reinterpret_cast<const uint4*>(P.qid + base);
+    uint32_t words[4] = {q.x, q.y, q.z, q.w};
+    uint32_t mask = 0;
+    for (int k = 0; k < 16; ++k) {
+        uint32_t b = (words[k >> 2] >> (8 * (k & 3))) & 0xffu;
+        if (b == 0u) mask |= 1u << k;
+    }
+    uint32_t c = __popc(mask);
+    // block exclusive scan of c
+    uint32_t inc = c;
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t v = __shfl_up_sync(0xffffffffu, inc, o);
+        if (lane >= (uint32_t)o) inc += v;
+    }
+    __syncthreads();
+    if (lane == 31) s_warp[warp] = inc;
+    __syncthreads();
+    uint32_t woff = 0, total = 0;
+    for (int w = 0; w < 8; ++w) {
+        uint32_t v = s_warp[w];
+        if (w < (int)warp) woff += v;
+        total += v;
+    }
+    uint32_t pos = prefix + woff + inc - c;
+    uint32_t* out = Q.items[0];
+    while (mask) {
+        int k = __ffs(mask) - 1;
+        mask &= mask - 1;
+        out[pos++] = base + k;
+    }
+    if (t == Q.ntiles - 1 && tid == 0) {
+        uint32_t all = prefix + total;
+        Q.counts[0] = all;
+        unsigned long long np = *Q.next_pixel;
+        *Q.step_base = np;
+        *Q.next_pixel = np + all;  // finalize_new_path (new_path.cl:85-88)
+    }
+}
+
+__global__ void __launch_bounds__(256) k_shade(SceneView sc, PathsView P, QueueView Q, RenderParams rp) {
+    uint32_t off[kNumQueues + 1];
+    off[0] = 0;
+#pragma unroll
+    for (int k = 0; k < kNumQueues; ++k) off[k + 1] = off[k] + Q.counts[k];
+    const uint32_t total = off[kNumQueues];
+    const unsigned long long base_pixel = *Q.step_base;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += stride) {
+        int k = 0;
+#pragma unroll
+        for (int j = 1; j < kNumQueues; ++j) k += (i >= off[j]) ? 1 : 0;
+        const uint32_t slot = Q.items[k][i - off[k]];
+        unsigned long long gpix = 0;
+        if (k == 0) {
+            gpix = base_pixel + (i - off[0]);
+            if (rp.sample_limit != 0ull && gpix >= rp.sample_limit) {
+                P.qid[slot] = kQueueIdle;  // sample budget reached: the slot retires
+                continue;
+            }
+        }
+        shade_slot(sc, P, rp, k, slot, gpix);
+    }
+}
+
+// warp-aggregated append of `slot` to queue q (one atomic per distinct queue per warp)
+RGR_DEV void enqueue(const QueueView& Q, int q, uint32_t slot, unsigned active) {
+    unsigned peers = __match_any_sync(active, q);
+    int leader = __ffs(peers) - 1;
+    int lane = threadIdx.x & 31;
+    uint32_t base = 0;
+    if (lane == leader) base = atomicAdd(Q.counts + q, (uint32_t)__popc(peers));
+    base = __shfl_sync(peers, base, leader);
+    uint32_t rank = __popc(peers & ((1u << lane) - 1u));
+    Q.items[q][base + rank] = slot;
+}
+
+__global__ void __launch_bounds__(128) k_trace_logic(SceneView sc, PathsView P, QueueView Q, RenderParams rp) {
+    const uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool live = slot < P.n && P.qid[slot] != kQueueIdle;
+    const unsigned active = __ballot_sync(0xffffffffu, live);
+    if (!live) return;
+    float4 ro4 = P.ro[slot], rd4 = P.rd[slot];
+    f3 ro = xyz(ro4), rd = xyz(rd4);
+    float tmin = ro4.w;
+    int32_t hv = __float_as_int(rd4.w);
+    uint32_t err = 0;
+    // extension_ray_cast (extension_ray_cast_stackless.cl:202-246)
+    int32_t hs = trace_closest<false>(sc, ro, rd, tmin, nullptr, err);
+    if (hs >= 0) {
+        f3 ng = hit_normal(sc, hs, ro, rd, tmin);
+        P.ng[slot] = f4(ng, __int_as_float(hs));
+        P.ro[slot] = f4(ro, tmin);
+        hv = -1;
+        P.rd[slot] = f4(rd, __int_as_float(-1));
+    }
+    // logic (logic.cl:27-190)
+    float4 T4 = P.T[slot], L4 = P.L[slot];
+    f3 T = xyz(T4), L = xyz(L4);
+    uint32_t logic_i = __float_as_uint(L4.w);
+    Rng rng = rng_load(P.rng, slot);
+    bool evalEnv = false, newPath = false;
+    if (hs < 0 && hv < 0) {
+        newPath = true;
+        evalEnv = true;
+    }
+    float lum = 0.2126f * T.x + 0.7152f * T.y + 0.0722f * T.z;
+    float cp = 1.0f;
+    if ((long long)rp.rr_depth < (long long)logic_i) cp = fmin_(lum, 1.0f);
+    float u = rng.uniform();
+    if (u < cp) {
+        T = T / cp;
+    } else {
+        newPath = true;
+    }
+    if (lum < 1.0e-5f) newPath = true;
+    if (evalEnv && sc.has_env) L = L + T * envmap_value(sc, rd, logic_i == 0);
+    // depth limit: end after segment max_depth, adding the emission that the
+    // next material stage would add (lambertian.cl:395)
+    if (rp.max_depth > 0 && !newPath && (long long)logic_i >= (long long)rp.max_depth) {
+        if (0 <= hs) {
+            int2 m = __ldg(sc.materials + hs);
+            f3 Le = mk(0, 0, 0);
+            if (m.x == kMatLambertian) Le = xyz(__ldg(sc.lambertians + 2 * (size_t)m.y));
+            L = L + T * Le;
+        }
+        newPath = true;
+    }
+    if (newPath) {
+        const float cl = rp.radiance_clamp;
+        if (is_finite(L.x) && is_finite(L.y) && is_finite(L.z) && L.x < cl && L.y < cl && L.z < cl) {
+            double* a = rp.accum + 4 * (size_t)__float_as_uint(T4.w);
+            atomicAdd(a + 0, (double)L.x);
+            atomicAdd(a + 1, (double)L.y);
+            atomicAdd(a + 2, (double)L.z);
+            atomicAdd(a + 3, 1.0);
+        }
+    }
+    P.T[slot] = f4(T, T4.w);
+    P.L[slot] = f4(L, __uint_as_float(logic_i + 1));
+    rng_store(P.rng, slot, rng);
+    int q;
+    if (newPath) {
+        q = 0;
+    } else if (0 <= hs) {
+        q = __ldg(sc.materials + hs).x;
+    } else {
+        q = kMatVolumeInside;
+    }
+    P.qid[slot] = (uint8_t)q;
+    {
+        // new paths: count per tile for the ordered compaction; others: material queue
+        const unsigned newmask = __ballot_sync(active, q == 0);
+        if (q == 0) {
+            unsigned tp = __match_any_sync(newmask, (int)(slot / kTile));
+            int leader = __ffs(tp) - 1;
+            if ((int)(threadIdx.x & 31) == leader) atomicAdd(Q.tile_new + slot / kTile, (uint32_t)__popc(tp));
+        } else {
+            enqueue(Q, q, slot, active & ~newmask);
+        }
+    }
+    {
+        int lane = threadIdx.x & 31;
+        int leader = __ffs(active) - 1;
+        if (lane == leader) atomicAdd(rp.rays, (unsigned long long)__popc(active));
+        if (err) atomicOr(rp.err, err);
+    }
+}
+
+// RGB16 intermediate (accumlation.cl:6-25) from FP64 sums: mean in double,
+// rounded to float, then to half; count to 16 bits.
+__global__ void k_readback(int fmt, const double* accum, uint32_t npix, void* out) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= npix) return;
+    const double* a = accum + 4 * (size_t)i;
+    double cnt = a[3];
+    unsigned short h[3];
+    for (int k = 0; k < 3; ++k) {
+        float m = cnt > 0.0 ? (float)(a[k] / cnt) : 0.0f;
+        h[k] = __half_as_ushort(__float2half_rn(m));
+    }
+    if (fmt == 1) {
+        ushort4 v = make_ushort4(h[0], h[1], h[2], (unsigned short)((unsigned long long)cnt & 0xffffull));
+        reinterpret_cast<ushort4*>(out)[i] = v;
+        return;
+    }
+    // tonemap (accumlation.cl:68-79)
+    uchar4 px;
+    unsigned char c[3];
+    for (int k = 0; k < 3; ++k) {
+        float v = __half2float(__ushort_as_half(h[k]));
+        int iv = to_int(pow_(v * 1.0f, 1.0f / 2.2f) * 256.0f);
+        iv = min(max(iv, 0), 255);
+        c[k] = (unsigned char)iv;
+    }
+    px.x = c[0];
+    px.y = c[1];
+    px.z = c[2];
+    px.w = 255;
+    reinterpret_cast<uchar4*>(out)[i] = px;
+}
+
+// stat (stat.cl:6-39): total accumulated samples
+__global__ void k_sum_counts(const double* accum, uint32_t npix, unsigned long long* out) {
+    unsigned long long s = 0;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < npix; i += gridDim.x * blockDim.x)
+        s += (unsigned long long)accum[4 * (size_t)i + 3];
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if ((threadIdx.x & 31) == 0) atomicAdd(out, s);
+}
+
+__global__ void k_accum_add(double* dst, const double* src, uint32_t n4) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n4) dst[i] += src[i];
+}
+
+__global__ void k_debug_slots(PathsView P, uint32_t* out) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P.n) return;
+    uint32_t* o = out + 34 * (size_t)i;
+    float4 T = P.T[i], L = P.L[i], ro = P.ro[i], rd = P.rd[i], ng = P.ng[i];
+    uint4 r = P.rng[i];
+    int4 va = P.vols[2 * (size_t)i], vb = P.vols[2 * (size_t)i + 1];
+    const float f[12] = {T.x, T.y, T.z, L.x, L.y, L.z, ro.x, ro.y, ro.z, rd.x, rd.y, rd.z};
+    for (int k = 0; k < 12; ++k) o[k] = __float_as_uint(f[k]);
+    o[12] = __float_as_uint(L.w);
+    o[13] = __float_as_uint(T.w);
+    o[14] = r.x;
+    o[15] = r.y;
+    o[16] = r.z;
+    o[17] = r.w;
+    o[18] = __float_as_uint(ng.w);
+    o[19] = __float_as_uint(rd.w);
+    o[20] = __float_as_uint(ro.w);
+    o[21] = __float_as_uint(ng.x);
+    o[22] = __float_as_uint(ng.y);
+    o[23] = __float_as_uint(ng.z);
+    uint8_t q = P.qid[i];
+    o[24] = q == kQueueIdle ? 0xffffffffu : (uint32_t)q;
+    o[25] = (uint32_t)vb.w;
+    const int v[7] = {va.x, va.y, va.z, va.w, vb.x, vb.y, vb.z};
+    for (int k = 0; k < 7; ++k) o[26 + k] = (uint32_t)v[k];
+    o[33] = 0;
+}
+
+}  // namespace
+
+void launch_init(const PathsView& p, const QueueView& q, uint32_t seed_offset, cudaStream_t st) {
+    uint32_t n = q.ntiles * kTile;
+    k_init<<<(n + 255) / 256, 256, 0, st>>>(p, q, seed_offset);
+}
+void launch_compact_new(const PathsView& p, const QueueView& q, cudaStream_t st) {
+    k_compact_new<<<q.ntiles, 256, 0, st>>>(p, q);
+}
+void launch_shade(const SceneView& sc, const PathsView& p, const QueueView& q, const RenderParams& rp, int grid,
+                  cudaStream_t st) {
+    k_shade<<<grid, 256, 0, st>>>(sc, p, q, rp);
+}
+void launch_trace_logic(const SceneView& sc, const PathsView& p, const QueueView& q, const RenderParams& rp,
+                        int block, cudaStream_t st) {
+    (void)block;
+    k_trace_logic<<<(p.n + 127) / 128, 128, 0, st>>>(sc, p, q, rp);
+}
+void launch_readback(int fmt, const double* accum, uint32_t npix, void* out, cudaStream_t st) {
+    k_readback<<<(npix + 255) / 256, 256, 0, st>>>(fmt, accum, npix, out);
+}
+void launch_sum_counts(const double* accum, uint32_t npix, unsigned long long* out, cudaStream_t st) {
+    k_sum_counts<<<152 * 4, 256, 0, st>>>(accum, npix, out);
+}
+void launch_debug_slots(const PathsView& p, uint32_t* out, cudaStream_t st) {
+    k_debug_slots<<<(p.n + 255) / 256, 256, 0, st>>>(p, out);
+}
+void launch_accum_add(double* dst, const double* src, uint32_t npix, cudaStream_t st) {
+    uint32_t n4 = npix * 4;
+    k_accum_add<<<(n4 + 255) / 256, 256, 0, st>>>(dst, src, n4);
+}
+
+}  // namespace dev
+}  // namespace rgr

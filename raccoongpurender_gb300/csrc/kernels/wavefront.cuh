@@ -1,0 +1,80 @@
+// wavefront.cuh — device data of the wavefront renderer and the launchers
+// that the host orchestration (context.cu) calls.
+#pragma once
+#include "rgr_device.cuh"
+
+namespace rgr {
+namespace dev {
+
+constexpr uint32_t kTile = 4096;         // slots per compaction tile
+constexpr uint8_t kQueueIdle = 0xff;     // slot finished its sample budget
+constexpr int kNumQueues = 7;            // 0 new path, 1..6 material types (logic.cl:317-331)
+
+// Path state, structure of arrays, one entry per resident path slot.
+// Reference fields (kernels/types.cl:18-63) are packed into 16-byte vectors:
+//   ro   = (WavefrontPath.ro, ExtensionResult.tmin)
+//   rd   = (WavefrontPath.rd, ExtensionResult.hit_volume_material as int bits)
+//   T    = (WavefrontPath.T, WavefrontPath.pixel_index bits)
+//   L    = (WavefrontPath.L, WavefrontPath.logic_i bits)
+//   ng   = (ExtensionResult.Ng, ExtensionResult.hit_surface_material bits)
+//   vols = InVolumeList as two int4: volumes[0..3], (volumes[4..6], count)
+// ShadingResult and IncidentSample never leave registers: the stage that
+// produces them also consumes them.
+struct PathsView {
+    float4* ro;
+    float4* rd;
+    float4* T;
+    float4* L;
+    float4* ng;
+    uint4* rng;
+    int4* vols;
+    uint8_t* qid;    // queue of the next step, kQueueIdle when done
+    uint32_t n;
+};
+
+struct QueueView {
+    uint32_t* items[kNumQueues];
+    uint32_t* counts;               // [kNumQueues]
+    uint32_t* tile_new;             // new paths per tile, for the ordered compaction
+    uint32_t ntiles;
+    unsigned long long* next_pixel; // new_path.cl next_pixel_index
+    unsigned long long* step_base;  // next_pixel_index at the start of this step
+};
+
+struct CameraD {
+    float eye[3], up[3], right[3];
+    float o[3], r[3], b[3];
+    uint32_t w, h;
+};
+
+struct RenderParams {
+    CameraD cam;
+    float dof;
+    int32_t rr_depth;
+    float radiance_clamp;
+    float env_p;
+    int32_t max_depth;
+    unsigned long long sample_limit;  // 0 = none
+    double* accum;                    // 4 doubles per pixel: r, g, b, count
+    uint32_t* err;
+    unsigned long long* rays;         // extension rays cast
+};
+
+// launchers (wavefront.cu)
+void launch_init(const PathsView& p, const QueueView& q, uint32_t seed_offset, cudaStream_t st);
+void launch_compact_new(const PathsView& p, const QueueView& q, cudaStream_t st);
+void launch_shade(const SceneView& sc, const PathsView& p, const QueueView& q, const RenderParams& rp, int grid,
+                  cudaStream_t st);
+void launch_trace_logic(const SceneView& sc, const PathsView& p, const QueueView& q, const RenderParams& rp,
+                        int block, cudaStream_t st);
+void launch_readback(int fmt, const double* accum, uint32_t npix, void* dev_out, cudaStream_t st);
+void launch_sum_counts(const double* accum, uint32_t npix, unsigned long long* out, cudaStream_t st);
+void launch_debug_slots(const PathsView& p, uint32_t* out, cudaStream_t st);
+void launch_accum_add(double* dst, const double* src, uint32_t npix, cudaStream_t st);
+// trace.cu
+void launch_trace_rays(const SceneView& sc, const float* ox, const float* oy, const float* oz, const float* dx,
+                       const float* dy, const float* dz, const float* tmax, uint64_t n, int32_t* prim, float* t,
+                       float* ng, uint32_t* err, int block, cudaStream_t st);
+
+}  // namespace dev
+}  // namespace rgr
