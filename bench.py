@@ -1,0 +1,322 @@
+#!/usr/bin/env python3
+"""Headline benchmark: closest-hit ray casting on one GB300.
+
+Workload (the reference path's ray-cast microbenchmark): a seeded icosphere
+subdivided to 1,310,720 triangles with radial 3-octave value-noise
+displacement, SAH BVH with leaves of at most 4 triangles; 4,194,304 coherent
+pinhole primary rays (2048x2048) plus 4,194,304 incoherent rays (origins
+uniform in the bounding box, directions uniform on the sphere), FP32.  One
+step casts all 8,388,608 rays (two launches of the traversal kernel) and
+produces the closest primitive id and t for each, bit-identical to the
+reference traversal.
+
+Metric: Mrays/s.  ``value`` times the step with the rays already in HBM
+(CUDA events on the launching stream); ``e2e`` runs the same step through the
+C ABI with pinned host buffers, host-to-device copy of the rays and
+device-to-host copy of the hits inside the timed region.  The rays (224 MB)
+are larger than the 129 MB L2, so consecutive steps do not reuse them.
+
+``--impl reference`` times the reference traversal on the host cores (the
+oracle's restatement of kernels/extension_ray_cast_stackless.cl, all
+threads, on a bounded sample of the same rays).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+WORKLOAD = "closest-hit: 1.31M-tri displaced icosphere, 4M coherent + 4M incoherent rays"
+METRIC = "closest-hit Mrays/s (1 GB300)"
+
+
+def measured_peaks() -> dict:
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return dict(hbm_gbs=float(d["hbm_gbs"]), source="measured")
+    return dict(hbm_gbs=6800.0, source="fallback")
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self) -> dict:
+        rows = []
+        if self.path and os.path.exists(self.path):
+            for line in open(self.path):
+                parts = [x.strip() for x in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+            os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+
+        def num(x):
+            try:
+                return float(x)
+            except ValueError:
+                return None
+
+        sm = [num(r[1]) for r in rows if num(r[1]) is not None]
+        smax = max((num(r[2]) or 0.0) for r in rows)
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k].lower().startswith("active")})
+        sm.sort()
+        return {"sm_mhz": sm[len(sm) // 2] if sm else None, "sm_max_mhz": smax, "reasons": reasons,
+                "samples": len(rows)}
+
+
+def build_workload(level: int = 8, res: int = 2048):
+    import raccoongpurender_gb300 as rg
+    from raccoongpurender_gb300 import scenes
+    mesh = scenes.displaced_icosphere(level, seed=7)
+    mesh.materials = [rg.materials.lambertian()] * mesh.ntris
+    sm = rg.SceneManager()
+    sm.addMesh(mesh)
+    t0 = time.time()
+    sm.buildBVH(max_leaf_size=4)
+    build_s = time.time() - t0
+    coherent, incoherent = scenes.closest_hit_rays(mesh, res=res, n_random=res * res, seed=11)
+    return mesh, sm, coherent, incoherent, build_s
+
+
+def cpu_baseline(mesh, sm, coherent, incoherent, sample: int = 1048576) -> dict:
+    """The oracle traversal (kernels/extension_ray_cast_stackless.cl restated)
+    on all host threads over a bounded sample: the first `sample` rays of each
+    set, with the same 1:1 coherent/incoherent mix."""
+    import numpy as np
+    from oracle import pyoracle as po
+    osc = po.OracleScene.from_scene(sm, mesh.points, mesh.indices)
+    threads = os.cpu_count() or 1
+    idx = np.arange(sample)
+    rays = np.concatenate([coherent.subset(idx).packed8(), incoherent.subset(idx).packed8()])
+    osc.trace(rays[:1024], threads=threads)  # warm
+    t0 = time.perf_counter()
+    osc.trace(rays, threads=threads)
+    dt = time.perf_counter() - t0
+    return {"value": round(rays.shape[0] / dt / 1e6, 3), "unit": "Mrays/s", "cores": threads, "kind": "port",
+            "sample": f"{sample} coherent + {sample} incoherent rays of the same workload, {dt:.2f} s"}
+
+
+def run_reference(args) -> None:
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    mesh, sm, coherent, incoherent, _ = build_workload()
+    # the reference has no GPU implementation available here: its traversal
+    # restated on the host cores is the comparison arm
+    vals = []
+    for _ in range(args.warmup):
+        cpu_baseline(mesh, sm, coherent, incoherent, sample=8192)
+    for _ in range(args.steps):
+        vals.append(cpu_baseline(mesh, sm, coherent, incoherent, sample=32768))
+    v = sorted(x["value"] for x in vals)[len(vals) // 2]
+    base = vals[0]
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "Mrays/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "triangles": int(mesh.ntris), "rays_per_step": 2 * 32768},
+            "cpu_baseline": {"value": v, "unit": "Mrays/s", "cores": base["cores"], "kind": "port",
+                             "sample": base["sample"]},
+            "e2e": {"value": v, "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--e2e-steps", type=int, default=3)
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+        return
+
+    import numpy as np
+    import torch
+
+    import raccoongpurender_gb300 as rg
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    mesh, sm, coherent, incoherent, build_s = build_workload()
+    n_each = len(coherent)
+    lane = rg.WavefrontLane(local, 1024)
+    lane.setup(sm)
+    dev = torch.device("cuda", local)
+    sets = []
+    for rays in (coherent, incoherent):
+        soa = [torch.from_numpy(a).to(dev) for a in rays.soa()]
+        prim = torch.empty(len(rays), dtype=torch.int32, device=dev)
+        t = torch.empty(len(rays), dtype=torch.float32, device=dev)
+        sets.append((soa, prim, t, len(rays)))
+    # an explicit stream: handle 0 would mean "the context's own stream" to the C ABI
+    stream = torch.cuda.Stream(dev)
+    torch.cuda.set_stream(stream)
+    sptr = stream.cuda_stream
+    assert sptr != 0
+
+    def step():
+        for soa, prim, t, n in sets:
+            lane.trace_closest_device([a.data_ptr() for a in soa], n, prim.data_ptr(), t.data_ptr(), 0, sptr)
+
+    # algorithmic traffic: exact node visits and primitive tests per ray
+    counts = []
+    for soa, prim, t, n in sets:
+        nodes = torch.empty(n, dtype=torch.int32, device=dev)
+        prims = torch.empty(n, dtype=torch.int32, device=dev)
+        lane.trace_closest_counts_device([a.data_ptr() for a in soa], n, prim.data_ptr(), t.data_ptr(),
+                                         nodes.data_ptr(), prims.data_ptr(), sptr)
+        stream.synchronize()
+        counts.append((float(nodes.double().mean()), float(prims.double().mean()), float((prim >= 0).double().mean())))
+    bytes_per_ray = [28 + 8 + 64 * c[0] + 48 * c[1] for c in counts]
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize(dev)
+    if world > 1:
+        torch.distributed.barrier()
+
+    # per-launch timing of the two ray sets (events on the launching stream)
+    ev = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(args.steps)]
+    with ClockSampler(local) as clk:
+        t_start = torch.cuda.Event(enable_timing=True)
+        t_end = torch.cuda.Event(enable_timing=True)
+        t_start.record(stream)
+        for k in range(args.steps):
+            ev[k][0].record(stream)
+            soa, prim, t, n = sets[0]
+            lane.trace_closest_device([a.data_ptr() for a in soa], n, prim.data_ptr(), t.data_ptr(), 0, sptr)
+            ev[k][1].record(stream)
+            soa, prim, t, n = sets[1]
+            lane.trace_closest_device([a.data_ptr() for a in soa], n, prim.data_ptr(), t.data_ptr(), 0, sptr)
+            ev[k][2].record(stream)
+        t_end.record(stream)
+        torch.cuda.synchronize(dev)
+    clocks = clk.summary()
+    total_ms = t_start.elapsed_time(t_end)
+    coh_ms = sum(e[0].elapsed_time(e[1]) for e in ev) / args.steps
+    inc_ms = sum(e[1].elapsed_time(e[2]) for e in ev) / args.steps
+    if world > 1:
+        x = torch.tensor([total_ms], device=dev)
+        torch.distributed.all_reduce(x, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(x.item())
+    ms_per_step = total_ms / args.steps
+    rays_per_step = 2 * n_each
+    value = rays_per_step * world / (ms_per_step * 1e-3) / 1e6
+
+    # end to end through the C ABI with pinned host buffers
+    host = []
+    for rays in (coherent, incoherent):
+        soa = [torch.from_numpy(a).pin_memory() for a in rays.soa()]
+        host.append((soa, len(rays)))
+    out_prim = [torch.empty(n_each, dtype=torch.int32).pin_memory() for _ in range(2)]
+    out_t = [torch.empty(n_each, dtype=torch.float32).pin_memory() for _ in range(2)]
+
+    def e2e_step():
+        for k, (soa, n) in enumerate(host):
+            r = rg.rgr_ray_soa(*[a.data_ptr() for a in soa])
+            st = lane._lib.rgr_trace_closest(lane.handle, rg.C.byref(r), n, out_prim[k].data_ptr(),
+                                             out_t[k].data_ptr())
+            rg._check(st, "rgr_trace_closest")
+
+    e2e_step()
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    for _ in range(args.e2e_steps):
+        e2e_step()
+    torch.cuda.synchronize(dev)
+    e2e_s = (time.perf_counter() - t0) / args.e2e_steps
+    e2e_value = rays_per_step / e2e_s / 1e6
+    # the e2e hits must equal the device-resident hits
+    assert (out_prim[0].numpy() == sets[0][1].cpu().numpy()).all()
+
+    peaks = measured_peaks()
+    coh_bytes = bytes_per_ray[0] * n_each
+    inc_bytes = bytes_per_ray[1] * n_each
+    achieved = (coh_bytes + inc_bytes) / ((coh_ms + inc_ms) * 1e-3) / 1e9
+    roof = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peaks["hbm_gbs"], "unit": "GB/s",
+            "frac": round(achieved / peaks["hbm_gbs"], 4), "traffic": None,
+            "peak_source": peaks["source"] + " hbm_gbs",
+            "per_set": {"coherent": {"ms": round(coh_ms, 3), "mrays_s": round(n_each / coh_ms / 1e3, 1),
+                                     "nodes_per_ray": round(counts[0][0], 2), "prims_per_ray": round(counts[0][1], 2),
+                                     "bytes_per_ray": round(bytes_per_ray[0], 1), "hit_rate": round(counts[0][2], 4)},
+                        "incoherent": {"ms": round(inc_ms, 3), "mrays_s": round(n_each / inc_ms / 1e3, 1),
+                                       "nodes_per_ray": round(counts[1][0], 2),
+                                       "prims_per_ray": round(counts[1][1], 2),
+                                       "bytes_per_ray": round(bytes_per_ray[1], 1),
+                                       "hit_rate": round(counts[1][2], 4)}}}
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(mesh, sm, coherent, incoherent)
+    info = sm.info()
+    if rank == 0:
+        line = {"metric": METRIC, "value": round(value, 1), "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": round(ms_per_step, 4), "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+                "config": {"workload": WORKLOAD, "triangles": int(mesh.ntris), "rays_per_step": rays_per_step,
+                           "bvh": {"max_leaf": 4, "inner_nodes": int(info.num_inner_nodes),
+                                   "depth": int(info.depth), "build_s": round(build_s, 2)},
+                           "l2": "inputs larger than L2 (224 MB of rays per step)",
+                           "parallelism": f"replicas{world}"},
+                "e2e": {"value": round(e2e_value, 1), "unit": "Mrays/s", "h2d_bytes_per_step": rays_per_step * 28,
+                        "d2h_bytes_per_step": rays_per_step * 8},
+                "gpu_launches": 2 * args.steps, "roofline": roof, "cpu_baseline": cpu, "clocks": clocks}
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -172,6 +172,12 @@ int rgr_trace_closest(rgr_context* c, const rgr_ray_soa* rays, uint64_t n, int32
 int rgr_trace_closest_device(rgr_context* c, const rgr_ray_soa* rays, uint64_t n, int32_t* prim, float* t,
                              float* ng_xyz, void* stream);
 
+/* Instrumented closest hit (same results) that also returns, per ray, the
+   inner nodes visited and primitives tested: the algorithmic traffic of the
+   traversal (bytes = 64 per node + 48 per primitive record). */
+int rgr_trace_closest_counts_device(rgr_context* c, const rgr_ray_soa* rays, uint64_t n, int32_t* prim, float* t,
+                                    uint32_t* node_visits, uint32_t* prim_tests, void* stream);
+
 /* ---- diagnostics --------------------------------------------------------- */
 const char* rgr_status_string(int status);
 const char* rgr_last_error(void);

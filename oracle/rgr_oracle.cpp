@@ -457,7 +457,7 @@ enum {
     kMatVolume = 5, kMatVolumeInside = 6
 };
 struct Slot {
-    f3 T, L, ro, rd;
+    f3 T{0, 0, 0}, L{0, 0, 0}, ro{0, 0, 0}, rd{0, 0, 0};
     uint32_t logic_i = 0, pixel_index = 0;
     Rng rng;
     int32_t hit_surface = -1, hit_volume = -1;  // hit_volume initialised to -1 (reference leaves it unset)

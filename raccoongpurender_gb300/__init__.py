@@ -117,6 +117,8 @@ _SIGS = {
     "rgr_trace_closest_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p, C.c_void_p,
                                            C.c_void_p, C.c_void_p]),
     "rgr_debug_read_slots": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64]),
+    "rgr_trace_closest_counts_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p, C.c_void_p,
+                                                  C.c_void_p, C.c_void_p, C.c_void_p]),
 }
 
 _lib = None
@@ -387,6 +389,12 @@ class WavefrontLane:
         r = rgr_ray_soa(*[_ptr(a) for a in soa])
         _check(self._lib.rgr_trace_closest(self._h, C.byref(r), n, _ptr(prim), _ptr(t)), "rgr_trace_closest")
         return prim, t
+
+    def trace_closest_counts_device(self, soa_ptrs, n: int, prim_ptr: int, t_ptr: int, nodes_ptr: int,
+                                    prims_ptr: int, stream: int = 0) -> None:
+        r = rgr_ray_soa(*soa_ptrs)
+        _check(self._lib.rgr_trace_closest_counts_device(self._h, C.byref(r), n, prim_ptr, t_ptr, nodes_ptr, prims_ptr,
+                                                         stream or None), "rgr_trace_closest_counts_device")
 
     def trace_closest_device(self, soa_ptrs, n: int, prim_ptr: int, t_ptr: int, ng_ptr: int = 0,
                              stream: int = 0) -> None:

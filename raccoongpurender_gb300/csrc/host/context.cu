@@ -464,6 +464,21 @@ int rgr_trace_closest_device(rgr_context* c, const rgr_ray_soa* rays, uint64_t n
     return RGR_OK;
 }
 
+int rgr_trace_closest_counts_device(rgr_context* c, const rgr_ray_soa* rays, uint64_t n, int32_t* prim, float* t,
+                                    uint32_t* node_visits, uint32_t* prim_tests, void* stream) {
+    if (!c || !rays || !prim || !t || !node_visits || !prim_tests) return RGR_E_INVALID;
+    if (!c->uploaded) return RGR_E_STATE;
+    if (n == 0) return RGR_OK;
+    RGR_CUDA(cudaSetDevice(c->device));
+    cudaStream_t st = stream ? (cudaStream_t)stream : c->stream;
+    int r = c->err.alloc(16);
+    if (r != RGR_OK) return r;
+    launch_trace_rays_counts(c->sv, rays->ox, rays->oy, rays->oz, rays->dx, rays->dy, rays->dz, rays->tmax, n, prim, t,
+                             node_visits, prim_tests, c->err.as<uint32_t>(), st);
+    RGR_CUDA(cudaGetLastError());
+    return RGR_OK;
+}
+
 int rgr_trace_closest(rgr_context* c, const rgr_ray_soa* rays, uint64_t n, int32_t* prim, float* t) {
     if (!c || !rays || !prim || !t) return RGR_E_INVALID;
     if (!c->uploaded) return RGR_E_STATE;

@@ -495,6 +495,7 @@ RGR_DEV void shade_slot(const SceneView& sc, const PathsView& P, const RenderPar
     P.L[slot] = f4(L, __uint_as_float(logic_i));
     P.ng[slot] = f4(Ng, __int_as_float(hs));
     if (k == 0 || k == kMatVolume) {
+        vb.w = vcount;
         P.vols[2 * (size_t)slot] = va;
         P.vols[2 * (size_t)slot + 1] = vb;
     }

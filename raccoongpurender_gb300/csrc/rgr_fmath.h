@@ -106,6 +106,11 @@ RGR_HD void sincos_(float x, float* s_out, float* c_out) {
         *c_out = n;
         return;
     }
+    if (x == 0.0f) {  // keeps the sign of zero: sin(-0) = -0
+        *s_out = x;
+        *c_out = 1.0f;
+        return;
+    }
     const float kTwoOverPi = 0.636619747f;
     const float C1 = 1.57080078125f;            // 12 significant bits
     const float C2 = -4.45358455181121826e-06f; // 12 significant bits

@@ -207,7 +207,7 @@ def displaced_icosphere(level: int = 8, seed: int = 7, amplitude: float = 0.1) -
     n = value_noise3(v, seed)
     P = (v * (1.0 + amplitude * n)[:, None]).astype(F32)
     I = orient(P, f.astype(np.uint32), np.zeros(3, dtype=F32), outward=True)
-    return Mesh(P, I, [])
+    return Mesh(P, I, [M.lambertian(r=(0.8, 0.8, 0.8))] * int(I.shape[0]))
 
 
 # ------------------------------------------------------------------ rays

@@ -1,0 +1,91 @@
+"""Wavefront render on the GPU against the oracle.  Per-slot path state
+(throughput, radiance, ray, RNG state, hit record, volume list, next queue)
+must be bit-identical after every number of bounces tested; per-pixel FP64
+sums may differ only by summation order (relative 1e-12) and sample counts
+must be equal."""
+import numpy as np
+import pytest
+
+from raccoongpurender_gb300 import scenes
+from tests.helpers import build, camera, compare_slots
+
+pytestmark = pytest.mark.gpu
+
+
+def _render_pair(rg, po, sm, osc, cam, cfg, npaths, steps):
+    lane = rg.WavefrontLane(0, npaths)
+    lane.setup(sm)
+    lane.initialize(cam, cfg)
+    lane.step(steps)
+    lane.synchronize()
+    gslots = lane.debug_slots()
+    gacc = lane.accumulation().reshape(-1, 4)
+    oacc, oslots, onext = osc.render(po.camera_from_rgr(cam), po.config_from_rgr(cfg, cam.image_w * cam.image_h),
+                                     npaths, steps, threads=16)
+    st = lane.stats()
+    return lane, gslots, gacc, oslots, oacc, onext, st
+
+
+@pytest.mark.parametrize("steps", [1, 2, 7, 40])
+def test_cornell_slots(rg, po, steps):
+    mesh = scenes.cornell_box()
+    sm, osc = build(mesh)
+    cam = camera(scenes.cornell_camera(), 64, 64)
+    cfg = rg.render_config(dof=0.0, max_depth=0)
+    lane, gs, ga, os_, oa, onext, st = _render_pair(rg, po, sm, osc, cam, cfg, 1 << 14, steps)
+    assert compare_slots(gs, os_) == {}
+    assert st.paths_started == onext
+    assert (ga[:, 3] == oa[:, 3]).all()
+    np.testing.assert_allclose(ga[:, :3], oa[:, :3], rtol=1e-12, atol=1e-300)
+
+
+def test_mixed_scene_with_env_and_volume(rg, po):
+    mesh, env, camd = scenes.mixed_scene(level=4, seed=3)
+    sm, osc = build(mesh, env=env)
+    cam = camera(camd, 160, 90)
+    cfg = rg.render_config()  # reference defaults: thin lens 0.0045, RR after 25, clamp 1000
+    lane, gs, ga, os_, oa, onext, st = _render_pair(rg, po, sm, osc, cam, cfg, 1 << 15, 30)
+    assert compare_slots(gs, os_) == {}
+    assert (ga[:, 3] == oa[:, 3]).all()
+    np.testing.assert_allclose(ga[:, :3], oa[:, :3], rtol=1e-12, atol=1e-300)
+    # every queue was exercised
+    q = np.bincount(os_["queue"] + 1, minlength=8)
+    assert (q[[1, 2, 4, 5, 6, 7]] > 0).all(), q
+
+
+def test_fixed_spp_depth_limited(rg, po):
+    """Configuration-1 style render: fixed spp, max depth, no envmap."""
+    mesh = scenes.cornell_box()
+    sm, osc = build(mesh)
+    cam = camera(scenes.cornell_camera(), 32, 32)
+    cfg = rg.render_config(dof=0.0, max_depth=5, spp=4)
+    lane = rg.WavefrontLane(0, 1 << 12)
+    lane.setup(sm)
+    lane.initialize(cam, cfg)
+    steps = lane.render_until_done(1000)
+    ga = lane.accumulation().reshape(-1, 4)
+    oacc, oslots, _ = osc.render(po.camera_from_rgr(cam), po.config_from_rgr(cfg, 32 * 32), 1 << 12, steps,
+                                 threads=16)
+    assert (ga[:, 3] == oacc[:, 3]).all()
+    assert ga[:, 3].sum() <= 4 * 32 * 32
+    np.testing.assert_allclose(ga[:, :3], oacc[:, :3], rtol=1e-12, atol=1e-300)
+    assert (oslots["queue"] == -1).all()  # every slot retired
+    img = lane.finalize_color()
+    assert img.shape == (32, 32, 4) and (img[..., 3] == 255).all()
+
+
+def test_graph_and_eager_agree(rg, po):
+    mesh = scenes.cornell_box()
+    sm, _ = build(mesh)
+    cam = camera(scenes.cornell_camera(), 48, 48)
+    out = []
+    for graph in (True, False):
+        lane = rg.WavefrontLane(0, 1 << 12)
+        lane.set_graph_mode(graph)
+        lane.setup(sm)
+        lane.initialize(cam, rg.render_config(dof=0.0))
+        lane.step(12)
+        lane.synchronize()
+        out.append(lane.debug_slots())
+    for k in out[0]:
+        assert (np.asarray(out[0][k]).view(np.uint32) == np.asarray(out[1][k]).view(np.uint32)).all(), k
