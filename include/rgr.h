@@ -178,6 +178,24 @@ int rgr_trace_closest_device(rgr_context* c, const rgr_ray_soa* rays, uint64_t n
 int rgr_trace_closest_counts_device(rgr_context* c, const rgr_ray_soa* rays, uint64_t n, int32_t* prim, float* t,
                                     uint32_t* node_visits, uint32_t* prim_tests, void* stream);
 
+/* Render without allocating device memory.  No counterpart in the reference:
+   it exists for callers that cannot call cudaMalloc at render time (a host
+   application whose device memory is owned by its own allocator and fixed at
+   start-up, or a real-time loop that cannot afford cudaMalloc's implicit
+   device synchronisation).  Same kernels and results as rgr_render_begin() +
+   rgr_render_step(steps), but the path pool, queues and counters live in one
+   fixed array inside librgr (about 5 MB of device memory per GPU that loads
+   the library, held until exit); path_count above 32768 is rejected with
+   RGR_E_INVALID.  The caller passes a context with an uploaded scene (input)
+   and accum_out, a device buffer of 4 doubles (r, g, b, count) per pixel
+   (output, cleared by the call).  Runs on `stream` (NULL: the default stream)
+   and returns when the work is done.  All calls on a device share the array:
+   calls that overlap on the GPU race and give wrong results.  The first call
+   on a device looks up the array's address, so make that first call before
+   any stream capture starts on that device. */
+int rgr_render_noalloc(rgr_context* c, const rgr_camera* cam, const rgr_render_config* cfg, uint32_t path_count,
+                       int32_t steps, double* accum_out, void* stream);
+
 /* ---- diagnostics --------------------------------------------------------- */
 const char* rgr_status_string(int status);
 const char* rgr_last_error(void);

@@ -119,6 +119,8 @@ _SIGS = {
     "rgr_debug_read_slots": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64]),
     "rgr_trace_closest_counts_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p, C.c_void_p,
                                                   C.c_void_p, C.c_void_p, C.c_void_p]),
+    "rgr_render_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_int32, C.c_void_p,
+                                     C.c_void_p]),
 }
 
 _lib = None
@@ -373,6 +375,14 @@ class WavefrontLane:
         raw = np.zeros((self.path_count, SLOT_WORDS), np.uint32)
         _check(self._lib.rgr_debug_read_slots(self._h, _ptr(raw), self.path_count), "rgr_debug_read_slots")
         return slots_from_words(raw)
+
+    def render_noalloc(self, camera: rgr_camera, config: rgr_render_config, path_count: int, steps: int,
+                       accum_ptr: int, stream: int = 0) -> None:
+        """Render `steps` bounces of `path_count` paths into the caller's device
+        buffer (4 doubles per pixel) without allocating device memory; see
+        rgr_render_noalloc in include/rgr.h for its limits."""
+        _check(self._lib.rgr_render_noalloc(self._h, C.byref(camera), C.byref(config), path_count, steps, accum_ptr,
+                                            stream or None), "rgr_render_noalloc")
 
     def merge_from(self, other: "WavefrontLane") -> None:
         """WavefrontLane::merge_from (:963-991)."""

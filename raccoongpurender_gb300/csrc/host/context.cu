@@ -112,6 +112,13 @@ struct rgr_context {
     }
 };
 
+// read-only view of a context's uploaded scene, for rgr_render_noalloc (noalloc.cu)
+const rgr::dev::SceneView* rgr_context_scene_view(const rgr_context* c, int* device) {
+    if (!c || !c->uploaded) return nullptr;
+    if (device) *device = c->device;
+    return &c->sv;
+}
+
 extern "C" {
 
 int rgr_context_create(rgr_context** out, int32_t device, uint32_t path_count) {

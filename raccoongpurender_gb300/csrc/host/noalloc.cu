@@ -1,0 +1,189 @@
+// noalloc.cu — a render entry point that allocates no device memory.
+//
+// rgr_render_begin() allocates the resident path pool with cudaMalloc.  Some
+// callers cannot do that at render time: a host application whose device
+// memory belongs to its own pool allocator and is fixed at start-up, or a
+// real-time loop in which cudaMalloc's implicit device synchronisation would
+// stall the frame.  rgr_render_noalloc() serves them.  It renders with the
+// same kernels as rgr_render_step(), but its path state, queues and counters
+// live in the file-scope array below, which the CUDA runtime places in device
+// memory when the library is loaded.  The caller passes the inputs (a context
+// with an uploaded scene, camera, config) and the output (a device buffer of
+// 4 doubles per pixel).
+//
+// Limits and sharing:
+//  * at most kNoAllocMaxPaths resident paths (larger path_count is rejected);
+//  * every GPU that loads the library holds kScratchBytes (about 5 MB) of
+//    device memory until the process exits;
+//  * every call on a device reuses the same array, and the array keeps what
+//    the previous call left in it; each call re-initialises what must start
+//    from zero.  Calls whose work overlaps on the GPU (two streams, or two
+//    host threads) race on the array and give wrong results;
+//  * the first call on a device looks up the array's device address
+//    (cudaGetSymbolAddress), so that first call should come before any stream
+//    capture begins on that device.
+#include <cuda_runtime.h>
+
+#include <cstring>
+#include <mutex>
+#include <string>
+
+#include "../kernels/wavefront.cuh"
+#include "../rgr_internal.h"
+
+using namespace rgr;
+using namespace rgr::dev;
+
+// the context's uploaded scene (context.cu)
+const rgr::dev::SceneView* rgr_context_scene_view(const rgr_context* c, int* device);
+
+namespace {
+
+constexpr uint32_t kNoAllocMaxPaths = 1u << 15;
+constexpr uint32_t kNoAllocTiles = kNoAllocMaxPaths / kTile;
+static_assert(kNoAllocMaxPaths % kTile == 0, "whole tiles");
+
+// byte offsets inside the scratch array (every region 256-byte aligned)
+constexpr size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
+constexpr size_t kN = kNoAllocMaxPaths;
+constexpr size_t kOffRo = 0;
+constexpr size_t kOffRd = kOffRo + align256(16 * kN);
+constexpr size_t kOffT = kOffRd + align256(16 * kN);
+constexpr size_t kOffL = kOffT + align256(16 * kN);
+constexpr size_t kOffNg = kOffL + align256(16 * kN);
+constexpr size_t kOffRng = kOffNg + align256(16 * kN);
+constexpr size_t kOffVols = kOffRng + align256(16 * kN);
+constexpr size_t kOffQid = kOffVols + align256(32 * kN);
+constexpr size_t kOffQueues = kOffQid + align256(kN);
+constexpr size_t kOffCounts = kOffQueues + align256(4 * kN) * kNumQueues;
+constexpr size_t kOffTiles = kOffCounts + 256;
+constexpr size_t kOffScalars = kOffTiles + align256(4 * kNoAllocTiles);
+constexpr size_t kOffErr = kOffScalars + 256;
+constexpr size_t kScratchBytes = kOffErr + 256;
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
+
+std::mutex g_mu;
+void* g_scratch_addr[128] = {};
+
+// Once per device, with that device current: the device address of the array.
+int scratch_address(int device, unsigned char** out) {
+    if (device < 0 || device >= 128) return RGR_E_INVALID;
+    std::lock_guard<std::mutex> lock(g_mu);
+    if (!g_scratch_addr[device]) {
+        void* p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess || p == nullptr) {
+            set_error(std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+            return RGR_E_CUDA;
+        }
+        g_scratch_addr[device] = p;
+    }
+    *out = static_cast<unsigned char*>(g_scratch_addr[device]);
+    return RGR_OK;
+}
+
+bool ok(cudaError_t e, const char* what) {
+    if (e == cudaSuccess) return true;
+    set_error(std::string(what) + ": " + cudaGetErrorString(e));
+    return false;
+}
+
+}  // namespace
+
+extern "C" int rgr_render_noalloc(rgr_context* c, const rgr_camera* cam, const rgr_render_config* cfg,
+                                  uint32_t path_count, int32_t steps, double* accum_out, void* stream) {
+    if (!c || !cam || !accum_out || steps < 0) return RGR_E_INVALID;
+    if (path_count == 0 || path_count > kNoAllocMaxPaths) {
+        set_error("rgr_render_noalloc: path_count must be 1.." + std::to_string(kNoAllocMaxPaths) +
+                  " (the fixed scratch holds at most that many paths)");
+        return RGR_E_INVALID;
+    }
+    if (cam->image_w == 0 || cam->image_h == 0 || (uint64_t)cam->image_w * cam->image_h > (1ull << 31))
+        return RGR_E_INVALID;
+    int device = 0;
+    const SceneView* sv = rgr_context_scene_view(c, &device);
+    if (!sv) {
+        set_error("rgr_render_noalloc: upload a scene to the context first");
+        return RGR_E_STATE;
+    }
+    if (!ok(cudaSetDevice(device), "cudaSetDevice")) return RGR_E_CUDA;
+    unsigned char* base = nullptr;
+    int r = scratch_address(device, &base);
+    if (r != RGR_OK) return r;
+    cudaStream_t st = (cudaStream_t)stream;
+
+    rgr_render_config d;
+    rgr_render_config_default(&d);
+    const rgr_render_config& k = cfg ? *cfg : d;
+    const uint32_t npix = cam->image_w * cam->image_h;
+    const uint32_t ntiles = (path_count + kTile - 1) / kTile;
+
+    PathsView p;
+    p.ro = reinterpret_cast<float4*>(base + kOffRo);
+    p.rd = reinterpret_cast<float4*>(base + kOffRd);
+    p.T = reinterpret_cast<float4*>(base + kOffT);
+    p.L = reinterpret_cast<float4*>(base + kOffL);
+    p.ng = reinterpret_cast<float4*>(base + kOffNg);
+    p.rng = reinterpret_cast<uint4*>(base + kOffRng);
+    p.vols = reinterpret_cast<int4*>(base + kOffVols);
+    p.qid = base + kOffQid;
+    p.n = path_count;
+    QueueView q;
+    for (int i = 0; i < kNumQueues; ++i) q.items[i] = reinterpret_cast<uint32_t*>(base + kOffQueues + align256(4 * kN) * i);
+    q.counts = reinterpret_cast<uint32_t*>(base + kOffCounts);
+    q.tile_new = reinterpret_cast<uint32_t*>(base + kOffTiles);
+    q.ntiles = ntiles;
+    unsigned long long* scal = reinterpret_cast<unsigned long long*>(base + kOffScalars);
+    q.next_pixel = scal + 0;
+    q.step_base = scal + 1;
+    RenderParams rp;
+    CameraD& cd = rp.cam;
+    for (int i = 0; i < 3; ++i) {
+        cd.eye[i] = cam->eye[i];
+        cd.up[i] = cam->up[i];
+        cd.right[i] = cam->right[i];
+        cd.o[i] = cam->imageplane_o[i];
+        cd.r[i] = cam->imageplane_r[i];
+        cd.b[i] = cam->imageplane_b[i];
+    }
+    cd.w = cam->image_w;
+    cd.h = cam->image_h;
+    rp.dof = k.dof;
+    rp.rr_depth = k.rr_depth;
+    rp.radiance_clamp = k.radiance_clamp;
+    rp.env_p = k.env_select_prob;
+    rp.max_depth = k.max_depth;
+    rp.sample_limit = k.spp ? (unsigned long long)k.spp * npix : 0ull;
+    rp.accum = accum_out;
+    rp.err = reinterpret_cast<uint32_t*>(base + kOffErr);
+    rp.rays = scal + 2;
+
+    // the array keeps the previous call's contents: reset counters and output
+    if (!ok(cudaMemsetAsync(base + kOffCounts, 0, 256, st), "cudaMemsetAsync") ||
+        !ok(cudaMemsetAsync(base + kOffScalars, 0, 256, st), "cudaMemsetAsync") ||
+        !ok(cudaMemsetAsync(base + kOffErr, 0, 256, st), "cudaMemsetAsync") ||
+        !ok(cudaMemsetAsync(accum_out, 0, sizeof(double) * 4 * (size_t)npix, st), "cudaMemsetAsync"))
+        return RGR_E_CUDA;
+    launch_init(p, q, k.seed_offset, st);
+    int sms = 152;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+    for (int32_t i = 0; i < steps; ++i) {
+        launch_compact_new(p, q, st);
+        launch_shade(*sv, p, q, rp, sms * 8, st);
+        if (!ok(cudaMemsetAsync(q.counts + 1, 0, sizeof(uint32_t) * (kNumQueues - 1), st), "cudaMemsetAsync") ||
+            !ok(cudaMemsetAsync(q.tile_new, 0, sizeof(uint32_t) * ntiles, st), "cudaMemsetAsync"))
+            return RGR_E_CUDA;
+        launch_trace_logic(*sv, p, q, rp, 128, st);
+    }
+    if (!ok(cudaGetLastError(), "kernel launch")) return RGR_E_CUDA;
+    uint32_t err = 0;
+    if (!ok(cudaMemcpyAsync(&err, rp.err, 4, cudaMemcpyDeviceToHost, st), "cudaMemcpyAsync") ||
+        !ok(cudaStreamSynchronize(st), "cudaStreamSynchronize"))
+        return RGR_E_CUDA;
+    if (err) {
+        set_error("device capacity check fired (flags " + std::to_string(err) + ")");
+        return RGR_E_OVERFLOW;
+    }
+    return RGR_OK;
+}
