@@ -196,6 +196,11 @@ int rgr_trace_closest_counts_device(rgr_context* c, const rgr_ray_soa* rays, uin
 int rgr_render_noalloc(rgr_context* c, const rgr_camera* cam, const rgr_render_config* cfg, uint32_t path_count,
                        int32_t steps, double* accum_out, void* stream);
 
+/* Launch shape of the closest-hit kernel: refill a warp with new rays when at
+   least `refill` of its 32 lanes are idle (1..32); `blocks_per_sm` resident
+   256-thread blocks per SM (0 = as many as fit).  Chosen by the autotuner. */
+int rgr_set_trace_tuning(rgr_context* c, int32_t refill, int32_t blocks_per_sm);
+
 /* ---- diagnostics --------------------------------------------------------- */
 const char* rgr_status_string(int status);
 const char* rgr_last_error(void);

@@ -26,7 +26,8 @@ import numpy as np
 from . import materials  # noqa: F401  (public)
 
 _PKG = Path(__file__).resolve().parent
-LIB_PATH = _PKG / "_lib" / "librgr.so"
+# RGR_LIBRARY selects a variant build of the same library (launch-shape experiments)
+LIB_PATH = Path(os.environ.get("RGR_LIBRARY", _PKG / "_lib" / "librgr.so"))
 
 RGR_OK = 0
 RGR_FMT_RGBA8, RGR_FMT_RGB16, RGR_FMT_FP64_SUMS = 0, 1, 2
@@ -119,6 +120,7 @@ _SIGS = {
     "rgr_debug_read_slots": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64]),
     "rgr_trace_closest_counts_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p, C.c_void_p,
                                                   C.c_void_p, C.c_void_p, C.c_void_p]),
+    "rgr_set_trace_tuning": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32]),
     "rgr_render_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_int32, C.c_void_p,
                                      C.c_void_p]),
 }
@@ -232,13 +234,16 @@ class SceneManager:
             proc[..., :3] *= np.float32(scale)
         self.envmap = proc
 
-    def buildBVH(self, max_leaf_size: int = 4, sah_bins: int = 32, num_threads: int = 0) -> None:
+    def buildBVH(self, max_leaf_size: int = 4, sah_bins: int = 32, num_threads: int = 0,
+                 traversal_cost: float = 1.0, intersect_cost: float = 1.0) -> None:
         """SceneManager::buildBVH (scene_manager.hpp:517-577)."""
         p = rgr_bvh_params()
         self._lib.rgr_bvh_params_default(C.byref(p))
         p.max_leaf_size = max_leaf_size
         p.sah_bins = sah_bins
         p.num_threads = num_threads
+        p.traversal_cost = traversal_cost
+        p.intersect_cost = intersect_cost
         _check(self._lib.rgr_scene_build_bvh(self._h, C.byref(p)), "rgr_scene_build_bvh")
 
     def info(self) -> rgr_scene_info:
@@ -399,6 +404,9 @@ class WavefrontLane:
         r = rgr_ray_soa(*[_ptr(a) for a in soa])
         _check(self._lib.rgr_trace_closest(self._h, C.byref(r), n, _ptr(prim), _ptr(t)), "rgr_trace_closest")
         return prim, t
+
+    def set_trace_tuning(self, refill: int = 16, blocks_per_sm: int = 0) -> None:
+        _check(self._lib.rgr_set_trace_tuning(self._h, refill, blocks_per_sm), "rgr_set_trace_tuning")
 
     def trace_closest_counts_device(self, soa_ptrs, n: int, prim_ptr: int, t_ptr: int, nodes_ptr: int,
                                     prims_ptr: int, stream: int = 0) -> None:

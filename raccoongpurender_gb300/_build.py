@@ -64,23 +64,28 @@ def _all_inputs() -> list[Path]:
     return files
 
 
-def build(verbose: bool = False, force: bool = False) -> Path:
-    """Compile every translation unit and link librgr.so; returns its path."""
-    BUILD.mkdir(parents=True, exist_ok=True)
-    LIB_DIR.mkdir(parents=True, exist_ok=True)
+def build(verbose: bool = False, force: bool = False, defines: tuple = (), out: Path | None = None) -> Path:
+    """Compile every translation unit and link librgr.so; returns its path.
+    `defines` (e.g. ("RGR_TRACE_MIN_BLOCKS=6",)) and `out` build a variant of
+    the library elsewhere, for launch-shape experiments."""
+    lib = Path(out) if out else LIB
+    bdir = BUILD if not defines else BUILD.parent / ("rgr_" + hashlib.sha1(" ".join(defines).encode()).hexdigest()[:8])
+    bdir.mkdir(parents=True, exist_ok=True)
+    lib.parent.mkdir(parents=True, exist_ok=True)
     nvcc = _nvcc()
-    stamp = BUILD / "stamp"
-    key = _digest(_all_inputs(), " ".join(_cuda_flags() + _cxx_flags()) + os.uname().machine)
-    if not force and LIB.exists() and stamp.exists() and stamp.read_text() == key:
-        return LIB
+    dflags = [f"-D{d}" for d in defines]
+    stamp = bdir / "stamp"
+    key = _digest(_all_inputs(), " ".join(_cuda_flags() + _cxx_flags() + dflags) + os.uname().machine + str(lib))
+    if not force and lib.exists() and stamp.exists() and stamp.read_text() == key:
+        return lib
 
     jobs = []
     for src in CUDA_SOURCES:
-        obj = BUILD / (src.replace("/", "_") + ".o")
-        jobs.append([nvcc, *_cuda_flags(), "-c", str(CSRC / src), "-o", str(obj)])
+        obj = bdir / (src.replace("/", "_") + ".o")
+        jobs.append([nvcc, *_cuda_flags(), *dflags, "-c", str(CSRC / src), "-o", str(obj)])
     for src in CXX_SOURCES:
-        obj = BUILD / (src.replace("/", "_") + ".o")
-        jobs.append(["g++", *_cxx_flags(), "-c", str(CSRC / src), "-o", str(obj)])
+        obj = bdir / (src.replace("/", "_") + ".o")
+        jobs.append(["g++", *_cxx_flags(), *dflags, "-c", str(CSRC / src), "-o", str(obj)])
 
     def run(cmd: list[str]) -> None:
         if verbose:
@@ -93,12 +98,12 @@ def build(verbose: bool = False, force: bool = False) -> Path:
 
     with cf.ThreadPoolExecutor(max_workers=min(len(jobs), os.cpu_count() or 4)) as ex:
         list(ex.map(run, jobs))
-    objs = [str(BUILD / (s.replace("/", "_") + ".o")) for s in CUDA_SOURCES + CXX_SOURCES]
-    tmp = LIB.with_suffix(".so.tmp")
+    objs = [str(bdir / (s.replace("/", "_") + ".o")) for s in CUDA_SOURCES + CXX_SOURCES]
+    tmp = lib.with_suffix(".so.tmp")
     run([nvcc, *ARCH, "-shared", "-o", str(tmp), *objs, "-lpthread"])
-    os.replace(tmp, LIB)
+    os.replace(tmp, lib)
     stamp.write_text(key)
-    return LIB
+    return lib
 
 
 if __name__ == "__main__":

@@ -91,7 +91,9 @@ struct rgr_context {
     bool graph_mode = true;
     cudaGraphExec_t graph_exec = nullptr;
     // ray-cast service buffers
-    DevBuf trays[7], tprim, tt, tread;
+    DevBuf trays[7], tprim, tt, tread, tcounter;
+    int trace_grid = 0;      // persistent traversal grid (SMs x resident blocks)
+    int trace_refill = 24;   // refill a warp when this many lanes are idle (measured best of 1..32)
 
     ~rgr_context() {
         if (graph_exec) cudaGraphExecDestroy(graph_exec);
@@ -139,6 +141,7 @@ int rgr_context_create(rgr_context** out, int32_t device, uint32_t path_count) {
         return RGR_E_CUDA;
     }
     cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device);
+    c->trace_grid = c->num_sms * std::max(1, trace_rays_max_blocks_per_sm());
     c->npaths = path_count;
     c->ntiles = (path_count + kTile - 1) / kTile;
     *out = c;
@@ -232,6 +235,9 @@ int rgr_device_upload(rgr_context* c, const rgr_scene* s) {
     v.env_w = e.present ? e.w : 0;
     v.env_h = e.present ? e.h : 0;
     v.has_env = e.present ? 1 : 0;
+    bool small = true;
+    for (int k = 0; k < 6; ++k) small = small && std::fabs(b.bounds[k]) <= 1.0e30f;
+    v.small_coords = small ? 1 : 0;
     c->uploaded = true;
     c->drop_graph();
     return RGR_OK;
@@ -465,9 +471,19 @@ int rgr_trace_closest_device(rgr_context* c, const rgr_ray_soa* rays, uint64_t n
     cudaStream_t st = stream ? (cudaStream_t)stream : c->stream;
     int r = c->err.alloc(16);
     if (r != RGR_OK) return r;
+    if ((r = c->tcounter.alloc(8)) != RGR_OK) return r;
     launch_trace_rays(c->sv, rays->ox, rays->oy, rays->oz, rays->dx, rays->dy, rays->dz, rays->tmax, n, prim, t, ng_xyz,
-                      c->err.as<uint32_t>(), 128, st);
+                      c->err.as<uint32_t>(), c->tcounter.as<unsigned long long>(), c->trace_refill, c->trace_grid, st);
     RGR_CUDA(cudaGetLastError());
+    return RGR_OK;
+}
+
+int rgr_set_trace_tuning(rgr_context* c, int32_t refill, int32_t blocks_per_sm) {
+    if (!c || refill < 1 || refill > 32 || blocks_per_sm < 0) return RGR_E_INVALID;
+    int maxb = std::max(1, trace_rays_max_blocks_per_sm());
+    if (blocks_per_sm > maxb) return RGR_E_INVALID;
+    c->trace_refill = refill;
+    c->trace_grid = c->num_sms * (blocks_per_sm ? blocks_per_sm : maxb);
     return RGR_OK;
 }
 
@@ -480,8 +496,10 @@ int rgr_trace_closest_counts_device(rgr_context* c, const rgr_ray_soa* rays, uin
     cudaStream_t st = stream ? (cudaStream_t)stream : c->stream;
     int r = c->err.alloc(16);
     if (r != RGR_OK) return r;
+    if ((r = c->tcounter.alloc(8)) != RGR_OK) return r;
     launch_trace_rays_counts(c->sv, rays->ox, rays->oy, rays->oz, rays->dx, rays->dy, rays->dz, rays->tmax, n, prim, t,
-                             node_visits, prim_tests, c->err.as<uint32_t>(), st);
+                             node_visits, prim_tests, c->err.as<uint32_t>(), c->tcounter.as<unsigned long long>(),
+                             c->trace_grid, st);
     RGR_CUDA(cudaGetLastError());
     return RGR_OK;
 }

@@ -33,6 +33,10 @@ RGR_DEV f3 normalize(f3 v) {
     return mk(v.x / l, v.y / l, v.z / l);
 }
 RGR_DEV f3 xyz(float4 v) { return mk(v.x, v.y, v.z); }
+RGR_DEV bool is_finite_nonzero(float x) {
+    const uint32_t e = __float_as_uint(x) & 0x7fffffffu;
+    return e != 0u && e < 0x7f800000u;
+}
 RGR_DEV float4 f4(f3 v, float w) { return make_float4(v.x, v.y, v.z, w); }
 
 // ------------------------------------------------------------ RNG
@@ -85,6 +89,7 @@ struct SceneView {
     const float4* env_frag;     // w*h
     int32_t env_w, env_h;
     int32_t has_env;
+    int32_t small_coords;       // every scene coordinate within +-1e30 (no NaN in slab products)
 };
 
 constexpr uint32_t kLeafFlag = 0x80000000u;

@@ -2,78 +2,119 @@
 // service), the kernel of the ray-cast microbenchmark.
 //
 // Rays arrive as structure-of-arrays FP32 (ox, oy, oz, dx, dy, dz, tmax:
-// 28 bytes per ray, coalesced 128-byte warp loads per component); results
-// are the primitive id (-1 on a miss) and t (tmax on a miss), and optionally
-// the geometric normal.
+// 28 bytes per ray); results are the primitive id (-1 on a miss), t (tmax on
+// a miss) and optionally the geometric normal.
+//
+// Persistent warps: each warp keeps 32 rays in flight and, between traversal
+// rounds, hands finished lanes new rays from a global counter (one atomic per
+// refill per warp).  Rays are read and results written with streaming
+// (evict-first) cache hints; the tree is read with an L2 evict-last policy.
+// Each ray's traversal is unchanged, so results do not depend on the
+// schedule.
 #include "wavefront.cuh"
 #include "traverse.cuh"
+
+#ifndef RGR_TRACE_MIN_BLOCKS
+#define RGR_TRACE_MIN_BLOCKS 5  // resident 256-thread blocks per SM the register budget must allow
+#endif
 
 namespace rgr {
 namespace dev {
 namespace {
 
-__global__ void __launch_bounds__(128) k_trace_rays(SceneView sc, const float* __restrict__ ox,
-                                                    const float* __restrict__ oy, const float* __restrict__ oz,
-                                                    const float* __restrict__ dx, const float* __restrict__ dy,
-                                                    const float* __restrict__ dz, const float* __restrict__ tmax,
-                                                    uint64_t n, int32_t* __restrict__ prim, float* __restrict__ tout,
-                                                    float* __restrict__ ng, uint32_t* err_out) {
-    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    f3 ro = mk(__ldg(ox + i), __ldg(oy + i), __ldg(oz + i));
-    f3 rd = mk(__ldg(dx + i), __ldg(dy + i), __ldg(dz + i));
-    float t = __ldg(tmax + i);
-    uint32_t err = 0;
-    int32_t p = trace_closest<false>(sc, ro, rd, t, nullptr, err);
-    prim[i] = p;
-    tout[i] = t;
-    if (ng) {
-        f3 n = p >= 0 ? hit_normal(sc, p, ro, rd, t) : mk(0.0f, 0.0f, 0.0f);
-        ng[3 * i + 0] = n.x;
-        ng[3 * i + 1] = n.y;
-        ng[3 * i + 2] = n.z;
-    }
-    if (err) atomicOr(err_out, err);
-}
+struct RayBatch {
+    const float *ox, *oy, *oz, *dx, *dy, *dz, *tmax;
+    uint64_t n;
+    int32_t* prim;
+    float* t;
+    float* ng;                   // optional, 3 floats per ray
+    uint32_t* nodes;             // optional counters (instrumented kernel)
+    uint32_t* prims;
+    uint32_t* err;
+    unsigned long long* next;    // work counter, zero at launch
+    int refill;                  // refill when at least this many lanes are idle
+};
 
-__global__ void __launch_bounds__(128) k_trace_rays_counts(SceneView sc, const float* __restrict__ ox,
-                                                           const float* __restrict__ oy, const float* __restrict__ oz,
-                                                           const float* __restrict__ dx, const float* __restrict__ dy,
-                                                           const float* __restrict__ dz,
-                                                           const float* __restrict__ tmax, uint64_t n,
-                                                           int32_t* __restrict__ prim, float* __restrict__ tout,
-                                                           uint32_t* nodes, uint32_t* prims, uint32_t* err_out) {
-    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    f3 ro = mk(ox[i], oy[i], oz[i]);
-    f3 rd = mk(dx[i], dy[i], dz[i]);
-    float t = tmax[i];
+template <bool kCount>
+__global__ void __launch_bounds__(256, RGR_TRACE_MIN_BLOCKS) k_trace_rays(SceneView sc, RayBatch b) {
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const unsigned lt = (1u << lane) - 1u;
+    const uint64_t pol = l2_evict_last_policy();
+    TraceState s;
+    TraceCounters cnt;
+    uint64_t ray = ~0ull;  // ~0: idle
+    bool exhausted = false;
     uint32_t err = 0;
-    TraceCounters c;
-    int32_t p = trace_closest<true>(sc, ro, rd, t, &c, err);
-    prim[i] = p;
-    tout[i] = t;
-    nodes[i] = c.nodes;
-    prims[i] = c.prims;
-    if (err) atomicOr(err_out, err);
+    for (;;) {
+        const unsigned idle = __ballot_sync(full, ray == ~0ull);
+        if (!exhausted && (int)__popc(idle) >= b.refill) {
+            const uint32_t need = __popc(idle);
+            unsigned long long base = 0;
+            if (lane == 0) base = atomicAdd(b.next, (unsigned long long)need);
+            base = __shfl_sync(full, base, 0);
+            if (base + need >= b.n) exhausted = true;
+            if (ray == ~0ull) {
+                const uint64_t r = base + __popc(idle & lt);
+                if (r < b.n) {
+                    ray = r;
+                    trace_begin(sc, s, mk(__ldcs(b.ox + r), __ldcs(b.oy + r), __ldcs(b.oz + r)),
+                                mk(__ldcs(b.dx + r), __ldcs(b.dy + r), __ldcs(b.dz + r)), __ldcs(b.tmax + r));
+                    if (kCount) cnt = TraceCounters();
+                }
+            }
+        }
+        if (__ballot_sync(full, ray != ~0ull) == 0u) {
+            if (exhausted) break;
+            continue;
+        }
+        if (ray != ~0ull) {
+            if (s.link != kDone) trace_round<kCount>(sc, s, &cnt, err, pol);
+            if (s.link == kDone) {
+                __stcs(b.prim + ray, s.prim);
+                __stcs(b.t + ray, s.tmin);
+                if (b.ng) {
+                    f3 n = s.prim >= 0 ? hit_normal(sc, s.prim, s.ro, s.rd, s.tmin) : mk(0.0f, 0.0f, 0.0f);
+                    b.ng[3 * ray + 0] = n.x;
+                    b.ng[3 * ray + 1] = n.y;
+                    b.ng[3 * ray + 2] = n.z;
+                }
+                if (kCount) {
+                    b.nodes[ray] = cnt.nodes;
+                    b.prims[ray] = cnt.prims;
+                }
+                ray = ~0ull;
+            }
+        }
+    }
+    if (err) atomicOr(b.err, err);
 }
 
 }  // namespace
 
-void launch_trace_rays_counts(const SceneView& sc, const float* ox, const float* oy, const float* oz, const float* dx,
-                              const float* dy, const float* dz, const float* tmax, uint64_t n, int32_t* prim,
-                              float* t, uint32_t* nodes, uint32_t* prims, uint32_t* err, cudaStream_t st) {
-    if (n == 0) return;
-    k_trace_rays_counts<<<(unsigned)((n + 127) / 128), 128, 0, st>>>(sc, ox, oy, oz, dx, dy, dz, tmax, n, prim, t,
-                                                                     nodes, prims, err);
-}
-
 void launch_trace_rays(const SceneView& sc, const float* ox, const float* oy, const float* oz, const float* dx,
                        const float* dy, const float* dz, const float* tmax, uint64_t n, int32_t* prim, float* t,
-                       float* ng, uint32_t* err, int block, cudaStream_t st) {
-    (void)block;
+                       float* ng, uint32_t* err, unsigned long long* counter, int refill, int grid, cudaStream_t st) {
     if (n == 0) return;
-    k_trace_rays<<<(unsigned)((n + 127) / 128), 128, 0, st>>>(sc, ox, oy, oz, dx, dy, dz, tmax, n, prim, t, ng, err);
+    RayBatch b{ox, oy, oz, dx, dy, dz, tmax, n, prim, t, ng, nullptr, nullptr, err, counter, refill};
+    cudaMemsetAsync(counter, 0, sizeof(unsigned long long), st);
+    k_trace_rays<false><<<grid, 256, 0, st>>>(sc, b);
+}
+
+void launch_trace_rays_counts(const SceneView& sc, const float* ox, const float* oy, const float* oz, const float* dx,
+                              const float* dy, const float* dz, const float* tmax, uint64_t n, int32_t* prim,
+                              float* t, uint32_t* nodes, uint32_t* prims, uint32_t* err, unsigned long long* counter,
+                              int grid, cudaStream_t st) {
+    if (n == 0) return;
+    RayBatch b{ox, oy, oz, dx, dy, dz, tmax, n, prim, t, nullptr, nodes, prims, err, counter, 16};
+    cudaMemsetAsync(counter, 0, sizeof(unsigned long long), st);
+    k_trace_rays<true><<<grid, 256, 0, st>>>(sc, b);
+}
+
+int trace_rays_max_blocks_per_sm() {
+    int nb = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_trace_rays<false>, 256, 0);
+    return nb;
 }
 
 }  // namespace dev

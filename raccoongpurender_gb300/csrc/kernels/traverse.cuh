@@ -15,6 +15,12 @@
 // four 16-byte read-only loads), leaves encoded in the parent's link, and
 // primitives pre-gathered in leaf order as 48-byte records (v0, v1-v0, v2-v0:
 // the edge subtraction is done once on the host and is bit-identical).
+//
+// The state of one ray lives in TraceState so that a warp can run rounds
+// (inner nodes down to one leaf, then that leaf) and refill finished lanes
+// with new rays between rounds; the visit order of each ray is unchanged.
+// BVH loads carry an L2 evict-last policy so that streaming ray data does not
+// push the tree out of L2.
 #pragma once
 #include "rgr_device.cuh"
 
@@ -23,30 +29,57 @@ namespace dev {
 
 constexpr int kStackSize = 64;  // the builder limits tree depth to 63
 constexpr uint32_t kDone = 0xffffffffu;
+constexpr uint32_t kErrStackOverflow = 1u;
 
-struct Hit {
-    float t;
-    int32_t prim;
-};
+// ------------------------------------------------------------ cache policy
+RGR_DEV uint64_t l2_evict_last_policy() {
+    uint64_t p;
+    asm("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
+    return p;
+}
+// read-only 16-byte load with an L2 cache-eviction policy
+RGR_DEV float4 ld_keep(const float4* ptr, uint64_t pol) {
+    float4 v;
+    asm("ld.global.nc.L2::cache_hint.v4.f32 {%0, %1, %2, %3}, [%4], %5;"
+        : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
+        : "l"(ptr), "l"(pol));
+    return v;
+}
 
 // slabs_with_hit (extension_ray_cast_stackless.cl:35-50).  fminf/fmaxf have
 // the reference's NaN behaviour; their results only feed comparisons, so the
-// sign of a zero result cannot change a decision.
+// sign of a zero result cannot change a decision.  kNanCheck = false is the
+// same function for rays whose products (lo - ro) * inv cannot be NaN (see
+// ray_is_nan_free); the reference's select(t, -t', isnan(t)) is then the
+// identity.
+template <bool kNanCheck>
 RGR_DEV bool slab(float lox, float loy, float loz, float hix, float hiy, float hiz, f3 ro, f3 inv, float farclip,
                   float& h0, float& h1) {
     float t0x = (lox - ro.x) * inv.x, t0y = (loy - ro.y) * inv.y, t0z = (loz - ro.z) * inv.z;
     float t1x = (hix - ro.x) * inv.x, t1y = (hiy - ro.y) * inv.y, t1z = (hiz - ro.z) * inv.z;
-    t0x = isnan(t0x) ? -t1x : t0x;
-    t0y = isnan(t0y) ? -t1y : t0y;
-    t0z = isnan(t0z) ? -t1z : t0z;
-    t1x = isnan(t1x) ? -t0x : t1x;
-    t1y = isnan(t1y) ? -t0y : t1y;
-    t1z = isnan(t1z) ? -t0z : t1z;
+    if (kNanCheck) {
+        t0x = isnan(t0x) ? -t1x : t0x;
+        t0y = isnan(t0y) ? -t1y : t0y;
+        t0z = isnan(t0z) ? -t1z : t0z;
+        t1x = isnan(t1x) ? -t0x : t1x;
+        t1y = isnan(t1y) ? -t0y : t1y;
+        t1z = isnan(t1z) ? -t0z : t1z;
+    }
     float rmin = fmaxf(fmaxf(fminf(t0x, t1x), fminf(t0y, t1y)), fminf(t0z, t1z));
     float rmax = fminf(fminf(fmaxf(t0x, t1x), fmaxf(t0y, t1y)), fmaxf(t0z, t1z));
     h0 = fmaxf(0.0f, rmin);
     h1 = fminf(rmax, farclip);
     return rmin <= rmax && 0.0f <= rmax && rmin <= farclip;
+}
+
+// (lo - ro) * inv is never NaN when ro is finite and small, every inv
+// component is finite and non-zero, and the scene box is small (checked on
+// the host): the difference is finite and the product of two finite non-zero
+// numbers is a number or an infinity.
+RGR_DEV bool ray_is_nan_free(f3 ro, f3 inv, bool scene_small) {
+    const float kBig = 1.0e30f;
+    return scene_small && fabsf(ro.x) <= kBig && fabsf(ro.y) <= kBig && fabsf(ro.z) <= kBig &&
+           is_finite_nonzero(inv.x) && is_finite_nonzero(inv.y) && is_finite_nonzero(inv.z);
 }
 
 // intersect_ray_triangle (intersect_triangle.cl:7-44) with precomputed edges
@@ -94,73 +127,115 @@ RGR_DEV bool sphere_test(f3 ro, f3 rd, f3 o, float r, float& tmin) {
 struct TraceCounters {
     uint32_t nodes = 0, prims = 0;
 };
-constexpr uint32_t kErrStackOverflow = 1u;
 
-// Closest hit.  tmin in: the ray's far clip (ExtensionResult.tmin); out: the
-// hit distance (unchanged on a miss).  Returns the primitive id or -1.
+struct TraceState {
+    f3 ro, rd, inv;
+    float tmin;       // ExtensionResult.tmin: far clip in, hit distance out
+    int32_t prim;     // -1 until a primitive is hit
+    uint32_t link;    // next node link; kDone when the ray is finished
+    int sp;           // pending far links; the newest is in `top`, older ones in stack[0..sp-2]
+    uint32_t top;
+    bool nan_free;
+    uint32_t stack[kStackSize];
+};
+
+RGR_DEV void trace_begin(const SceneView& sc, TraceState& s, f3 ro, f3 rd, float tmax) {
+    s.ro = ro;
+    s.rd = rd;
+    s.inv = mk(1.0f / rd.x, 1.0f / rd.y, 1.0f / rd.z);
+    s.tmin = tmax;
+    s.prim = -1;
+    s.link = sc.num_prims == 0 ? kDone : sc.root_link;
+    s.sp = 0;
+    s.nan_free = ray_is_nan_free(ro, s.inv, sc.small_coords != 0);
+}
+
+// the newest pending far link, or kDone; the next one is fetched from local
+// memory now but needed only at the following pop
+RGR_DEV uint32_t pop(TraceState& s) {
+    if (s.sp == 0) return kDone;
+    const uint32_t link = s.top;
+    --s.sp;
+    if (s.sp > 0) s.top = s.stack[s.sp - 1];
+    return link;
+}
+
+// One round: inner nodes down to the next leaf, then that leaf.  On return
+// s.link is the next link to visit, or kDone.
+template <bool kNanCheck, bool kCount>
+RGR_DEV void trace_round_t(const SceneView& sc, TraceState& s, TraceCounters* cnt, uint32_t& err, uint64_t pol) {
+    const float4* __restrict__ nodes = sc.nodes;
+    uint32_t link = s.link;
+    while (!(link & kLeafFlag)) {
+        const float4* np = nodes + 4 * (size_t)link;
+        const float4 q0 = ld_keep(np + 0, pol);
+        const float4 q1 = ld_keep(np + 1, pol);
+        const float4 q2 = ld_keep(np + 2, pol);
+        const float4 q3 = ld_keep(np + 3, pol);
+        if (kCount) cnt->nodes++;
+        float L0, L1, R0, R1;
+        bool L = slab<kNanCheck>(q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, s.ro, s.inv, s.tmin, L0, L1);
+        bool R = slab<kNanCheck>(q1.z, q1.w, q2.x, q2.y, q2.z, q2.w, s.ro, s.inv, s.tmin, R0, R1);
+        const uint32_t cl = __float_as_uint(q3.x), cr = __float_as_uint(q3.y);
+        if (L && R) {
+            bool left_first = (L0 == R0) ? (L1 < R1) : (L0 < R0);
+            if (s.sp < kStackSize) {  // push the far child
+                if (s.sp > 0) s.stack[s.sp - 1] = s.top;
+                s.top = left_first ? cr : cl;
+                s.sp++;
+            } else {
+                err |= kErrStackOverflow;  // unreachable: tree depth <= 63
+            }
+            link = left_first ? cl : cr;
+        } else if (L) {
+            link = cl;
+        } else if (R) {
+            link = cr;
+        } else {
+            link = pop(s);
+        }
+    }
+    if (link != kDone) {
+        // leaf: primitives in the reference primitive_ids order
+        const float4* __restrict__ prims = sc.prims;
+        const uint32_t first = link & 0x0fffffffu;
+        const uint32_t count = ((link >> 28) & 7u) + 1u;
+        for (uint32_t k = 0; k < count; ++k) {
+            const float4* pp = prims + 3 * (size_t)(first + k);
+            const float4 a = ld_keep(pp + 0, pol);
+            const float4 b = ld_keep(pp + 1, pol);
+            if (kCount) cnt->prims++;
+            if (__float_as_uint(b.w) == 0u) {
+                const float4 c = ld_keep(pp + 2, pol);
+                if (tri_test(s.ro, s.rd, xyz(a), xyz(b), xyz(c), s.tmin)) s.prim = (int32_t)__float_as_uint(a.w);
+            } else {
+                if (sphere_test(s.ro, s.rd, xyz(a), b.x, s.tmin)) s.prim = (int32_t)__float_as_uint(a.w);
+            }
+        }
+        link = pop(s);
+    }
+    s.link = link;
+}
+
+template <bool kCount>
+RGR_DEV void trace_round(const SceneView& sc, TraceState& s, TraceCounters* cnt, uint32_t& err, uint64_t pol) {
+    if (s.nan_free) {
+        trace_round_t<false, kCount>(sc, s, cnt, err, pol);
+    } else {
+        trace_round_t<true, kCount>(sc, s, cnt, err, pol);
+    }
+}
+
+// Closest hit of one ray.  tmin in: the ray's far clip (ExtensionResult.tmin);
+// out: the hit distance (unchanged on a miss).  Returns the primitive id or -1.
 template <bool kCount>
 RGR_DEV int32_t trace_closest(const SceneView& sc, f3 ro, f3 rd, float& tmin, TraceCounters* cnt, uint32_t& err) {
-    if (sc.num_prims == 0) return -1;
-    const f3 inv = mk(1.0f / rd.x, 1.0f / rd.y, 1.0f / rd.z);
-    uint32_t stack[kStackSize];
-    int sp = 0;
-    int32_t prim = -1;
-    uint32_t link = sc.root_link;
-    const float4* __restrict__ nodes = sc.nodes;
-    const float4* __restrict__ prims = sc.prims;
-    for (;;) {
-        // inner nodes
-        while (!(link & kLeafFlag)) {
-            const float4* np = nodes + 4 * (size_t)link;
-            const float4 q0 = __ldg(np + 0);
-            const float4 q1 = __ldg(np + 1);
-            const float4 q2 = __ldg(np + 2);
-            const float4 q3 = __ldg(np + 3);
-            if (kCount) cnt->nodes++;
-            float L0, L1, R0, R1;
-            bool L = slab(q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, ro, inv, tmin, L0, L1);
-            bool R = slab(q1.z, q1.w, q2.x, q2.y, q2.z, q2.w, ro, inv, tmin, R0, R1);
-            const uint32_t cl = __float_as_uint(q3.x), cr = __float_as_uint(q3.y);
-            if (L && R) {
-                bool left_first = (L0 == R0) ? (L1 < R1) : (L0 < R0);
-                uint32_t near_l = left_first ? cl : cr;
-                uint32_t far_l = left_first ? cr : cl;
-                if (sp < kStackSize) {
-                    stack[sp++] = far_l;
-                } else {
-                    err |= kErrStackOverflow;  // unreachable: tree depth <= 63
-                }
-                link = near_l;
-            } else if (L) {
-                link = cl;
-            } else if (R) {
-                link = cr;
-            } else {
-                link = (sp == 0) ? kDone : stack[--sp];
-            }
-        }
-        if (link == kDone) break;
-        // leaf: primitives in the reference primitive_ids order
-        {
-            const uint32_t first = link & 0x0fffffffu;
-            const uint32_t count = ((link >> 28) & 7u) + 1u;
-            for (uint32_t k = 0; k < count; ++k) {
-                const float4* pp = prims + 3 * (size_t)(first + k);
-                const float4 a = __ldg(pp + 0);
-                const float4 b = __ldg(pp + 1);
-                if (kCount) cnt->prims++;
-                if (__float_as_uint(b.w) == 0u) {
-                    const float4 c = __ldg(pp + 2);
-                    if (tri_test(ro, rd, xyz(a), xyz(b), xyz(c), tmin)) prim = (int32_t)__float_as_uint(a.w);
-                } else {
-                    if (sphere_test(ro, rd, xyz(a), b.x, tmin)) prim = (int32_t)__float_as_uint(a.w);
-                }
-            }
-        }
-        if (sp == 0) break;
-        link = stack[--sp];
-    }
-    return prim;
+    TraceState s;
+    trace_begin(sc, s, ro, rd, tmin);
+    const uint64_t pol = l2_evict_last_policy();
+    while (s.link != kDone) trace_round<kCount>(sc, s, cnt, err, pol);
+    tmin = s.tmin;
+    return s.prim;
 }
 
 // geometric normal of a hit (extension_ray_cast_stackless.cl:224-239), from

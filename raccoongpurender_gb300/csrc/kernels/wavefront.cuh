@@ -74,10 +74,12 @@ void launch_accum_add(double* dst, const double* src, uint32_t npix, cudaStream_
 // trace.cu
 void launch_trace_rays(const SceneView& sc, const float* ox, const float* oy, const float* oz, const float* dx,
                        const float* dy, const float* dz, const float* tmax, uint64_t n, int32_t* prim, float* t,
-                       float* ng, uint32_t* err, int block, cudaStream_t st);
+                       float* ng, uint32_t* err, unsigned long long* counter, int refill, int grid, cudaStream_t st);
 void launch_trace_rays_counts(const SceneView& sc, const float* ox, const float* oy, const float* oz, const float* dx,
                               const float* dy, const float* dz, const float* tmax, uint64_t n, int32_t* prim,
-                              float* t, uint32_t* nodes, uint32_t* prims, uint32_t* err, cudaStream_t st);
+                              float* t, uint32_t* nodes, uint32_t* prims, uint32_t* err, unsigned long long* counter,
+                              int grid, cudaStream_t st);
+int trace_rays_max_blocks_per_sm();
 
 }  // namespace dev
 }  // namespace rgr
