@@ -162,6 +162,38 @@ int rgr_synchronize(rgr_context* c);
 /* capture the bounce loop in a CUDA graph (1) or launch stage by stage (0; default 1) */
 int rgr_set_graph_mode(rgr_context* c, int32_t enabled);
 
+/* merge_intermediate (accumlation.cl:27-49): a <- count-weighted merge of two
+   RGB16 intermediates (device arrays of RGR_FMT_RGB16 pixels), FP32 math,
+   half results, 16-bit counts; the reference's multi-device image merge. */
+int rgr_intermediate_merge_device(void* a, const void* b, uint64_t npix, void* stream);
+
+/* ---- batched requests --------------------------------------------------
+   Many renders of uneven resolution, spp and scene share one resident path
+   pool and one bounce loop (no reference counterpart: the reference renders
+   one scene per lane).  Each request owns a range of the global sample index
+   in run order; free slots go to the requests in that order. */
+typedef struct rgr_batch rgr_batch;
+#define RGR_ORDER_FIFO 0            /* submission order */
+#define RGR_ORDER_SHORTEST_FIRST 1  /* fewest samples first */
+typedef struct rgr_request_stats {
+    double complete_ms;   /* device time from the start of the run to the request's last path; -1 if unfinished */
+    uint64_t samples;     /* W*H*spp */
+    uint64_t pixels;
+    uint32_t order;       /* position in the run order */
+} rgr_request_stats;
+int rgr_batch_create(rgr_batch** out, int32_t device, uint32_t path_count);
+void rgr_batch_destroy(rgr_batch* b);
+/* the scene is uploaded once per distinct scene; cfg->spp must be > 0 */
+int rgr_batch_add(rgr_batch* b, const rgr_scene* scene, const rgr_camera* cam, const rgr_render_config* cfg,
+                  int32_t* request_id);
+/* render every request to completion, replaying a CUDA graph of steps_per_launch bounces */
+int rgr_batch_run(rgr_batch* b, int32_t order_policy, int32_t steps_per_launch, int32_t max_steps,
+                  int32_t* steps_done);
+int rgr_batch_readback(rgr_batch* b, int32_t request_id, int32_t fmt, void* dst, uint64_t dst_bytes);
+int rgr_batch_request_stats(rgr_batch* b, int32_t request_id, rgr_request_stats* st);
+/* the batch's context (its stream, stats, slot state, launch tuning) */
+rgr_context* rgr_batch_context(rgr_batch* b);
+
 /* ---- closest hit as a service (extension_ray_cast_stackless.cl:202-246) */
 typedef struct rgr_ray_soa {
     const float *ox, *oy, *oz, *dx, *dy, *dz, *tmax;

@@ -56,6 +56,7 @@ _ORC_SIGS = {
     "orc_trace": (None, [VP, VP, U64, VP, VP, VP, VP, VP, I32]),
     "orc_envmap_build": (I32, [VP, I32, I32, VP, VP, VP, VP]),
     "orc_render": (U64, [VP, VP, VP, U32, I32, VP, VP, I32]),
+    "orc_render_batch": (U64, [VP, VP, VP, VP, VP, I32, U32, I32, VP, VP, I32]),
     "orc_intermediate": (None, [VP, U64, VP]),
     "orc_tonemap": (None, [VP, U64, VP]),
     "orc_float_to_half": (C.c_uint16, [F32C]),
@@ -206,6 +207,28 @@ class OracleScene:
         nxt = lib().orc_render(C.byref(self.s), C.byref(cam), C.byref(cfg), npaths, steps, P(accum), P(slots),
                                threads)
         return accum, slots, int(nxt)
+
+
+def render_batch(oscenes, cams, cfgs, npaths: int, steps: int, threads: int = 8):
+    """Oracle of a batch: requests in run order, request r owning the next
+    W*H*spp global samples.  Returns (list of FP64 accumulations, slots)."""
+    n = len(oscenes)
+    sc_ptrs = (C.c_void_p * n)(*[C.addressof(o.s) for o in oscenes])
+    cam_arr = (orc_camera * n)(*cams)
+    cfg_arr = (orc_config * n)(*cfgs)
+    sizes = [int(f.sample_limit) for f in cfgs]  # W*H*spp of each request
+    begin = np.zeros(n, np.uint64)
+    end = np.zeros(n, np.uint64)
+    acc = 0
+    for r in range(n):
+        begin[r] = acc
+        acc += sizes[r]
+        end[r] = acc
+    accs = [np.zeros((int(c.image_w) * int(c.image_h), 4), np.float64) for c in cams]
+    acc_ptrs = (C.c_void_p * n)(*[a.ctypes.data for a in accs])
+    slots = np.zeros(npaths, ORC_SLOT_DTYPE)
+    lib().orc_render_batch(sc_ptrs, cam_arr, cfg_arr, P(begin), P(end), n, npaths, steps, acc_ptrs, P(slots), threads)
+    return accs, slots
 
 
 def camera_from_rgr(cam) -> orc_camera:

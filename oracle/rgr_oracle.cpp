@@ -466,6 +466,7 @@ struct Slot {
     int32_t vol_count = 0;
     int32_t vols[7] = {0, 0, 0, 0, 0, 0, 0};
     int32_t queue = 0;  // next-step queue id; 0 = new path; -1 idle
+    int32_t req = 0;    // request (batched renders)
 };
 struct Incident {
     f3 wi{0, 0, 0};
@@ -1069,22 +1070,28 @@ int32_t orc_envmap_build(const float* rgba, int32_t w, int32_t h, float* pdf, fl
     return 0;
 }
 
-uint64_t orc_render(const orc_scene* s, const orc_camera* cam, const orc_config* cfg, uint32_t npaths,
-                    int32_t steps, double* accum, orc_slot* slots_out, int32_t nthreads) {
-    Ctx c{s, cam, cfg, s->env_rgba != nullptr && s->env_w > 0};
+// One pool of npaths slots serving nreq requests in order: request r owns the
+// global sample indices [begin[r], end[r]); a new path takes the request
+// whose range holds its index (the single-request render is nreq = 1).
+static uint64_t render_impl(const Ctx* ctxs, const uint64_t* begin, const uint64_t* end, int nreq,
+                            uint32_t seed_offset, uint64_t limit, uint32_t npaths, int32_t steps,
+                            double* const* accums, orc_slot* slots_out, int32_t nthreads) {
     std::vector<Slot> slots(npaths);
     for (uint32_t i = 0; i < npaths; ++i) {
-        random_initialize_one(slots[i].rng.s, (uint64_t)cfg->seed_offset + i);
+        random_initialize_one(slots[i].rng.s, (uint64_t)seed_offset + i);
         slots[i].queue = 0;  // initialize_all_as_new_path (new_path.cl:9-15)
     }
-    uint64_t npix = (uint64_t)cam->image_w * cam->image_h;
-    memset(accum, 0, sizeof(double) * 4 * npix);
     uint64_t next_pixel = 0;
     std::vector<uint64_t> gpix(npaths);
     std::vector<uint8_t> is_new(npaths);
     if (nthreads < 1) nthreads = 1;
     // per-thread private accumulators keep the sums deterministic
-    std::vector<std::vector<double>> acc(nthreads, std::vector<double>(4 * npix, 0.0));
+    std::vector<std::vector<std::vector<double>>> acc(nthreads);
+    for (int k = 0; k < nthreads; ++k) {
+        acc[k].resize(nreq);
+        for (int r = 0; r < nreq; ++r)
+            acc[k][r].assign(4 * (size_t)ctxs[r].cam->image_w * ctxs[r].cam->image_h, 0.0);
+    }
     for (int st = 0; st < steps; ++st) {
         // new-path queue in slot order (new_path.cl:41-43, finalize_new_path :85-88)
         uint64_t rank = 0;
@@ -1093,18 +1100,22 @@ uint64_t orc_render(const orc_scene* s, const orc_camera* cam, const orc_config*
             if (slots[i].queue != 0) continue;
             uint64_t g = next_pixel + rank;
             rank++;
-            if (cfg->sample_limit != 0 && g >= cfg->sample_limit) {
+            if (limit != 0 && g >= limit) {
                 slots[i].queue = -1;  // idle: the sample budget is exhausted
                 continue;
             }
+            int r = 0;
+            while (r + 1 < nreq && g >= end[r]) ++r;
+            slots[i].req = r;
             is_new[i] = 1;
-            gpix[i] = g;
+            gpix[i] = g - begin[r];
         }
         next_pixel += rank;
         auto work = [&](int k, uint32_t b, uint32_t e) {
             for (uint32_t i = b; i < e; ++i) {
                 if (slots[i].queue < 0) continue;
-                step_slot(c, slots[i], acc[k].data(), is_new[i] != 0, gpix[i]);
+                const int r = slots[i].req;
+                step_slot(ctxs[r], slots[i], acc[k][r].data(), is_new[i] != 0, gpix[i]);
             }
         };
         if (nthreads == 1) {
@@ -1119,11 +1130,34 @@ uint64_t orc_render(const orc_scene* s, const orc_camera* cam, const orc_config*
             for (auto& x : th) x.join();
         }
     }
-    for (int k = 0; k < nthreads; ++k)
-        for (size_t i = 0; i < 4 * npix; ++i) accum[i] += acc[k][i];
+    for (int r = 0; r < nreq; ++r) {
+        size_t n4 = 4 * (size_t)ctxs[r].cam->image_w * ctxs[r].cam->image_h;
+        memset(accums[r], 0, sizeof(double) * n4);
+        for (int k = 0; k < nthreads; ++k)
+            for (size_t i = 0; i < n4; ++i) accums[r][i] += acc[k][r][i];
+    }
     if (slots_out)
         for (uint32_t i = 0; i < npaths; ++i) dump_slot(slots[i], slots_out + i);
     return next_pixel;
+}
+
+uint64_t orc_render(const orc_scene* s, const orc_camera* cam, const orc_config* cfg, uint32_t npaths,
+                    int32_t steps, double* accum, orc_slot* slots_out, int32_t nthreads) {
+    Ctx c{s, cam, cfg, s->env_rgba != nullptr && s->env_w > 0};
+    uint64_t begin = 0, end = cfg->sample_limit ? cfg->sample_limit : ~0ull;
+    double* accs[1] = {accum};
+    return render_impl(&c, &begin, &end, 1, cfg->seed_offset, cfg->sample_limit, npaths, steps, accs, slots_out,
+                       nthreads);
+}
+
+uint64_t orc_render_batch(const orc_scene* const* scenes, const orc_camera* cams, const orc_config* cfgs,
+                          const uint64_t* begin, const uint64_t* end, int32_t nreq, uint32_t npaths, int32_t steps,
+                          double* const* accums, orc_slot* slots_out, int32_t nthreads) {
+    std::vector<Ctx> ctxs(nreq);
+    for (int r = 0; r < nreq; ++r)
+        ctxs[r] = Ctx{scenes[r], cams + r, cfgs + r, scenes[r]->env_rgba != nullptr && scenes[r]->env_w > 0};
+    return render_impl(ctxs.data(), begin, end, nreq, cfgs[0].seed_offset, end[nreq - 1], npaths, steps, accums,
+                       slots_out, nthreads);
 }
 
 // accumlation_to_intermediate (accumlation.cl:6-25) on FP64 sums: mean in

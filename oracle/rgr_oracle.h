@@ -118,6 +118,12 @@ uint64_t orc_render(const orc_scene* s, const orc_camera* cam, const orc_config*
                     uint32_t npaths, int32_t steps, double* accum, orc_slot* slots,
                     int32_t nthreads);
 
+/* batched requests sharing one pool: request r owns global samples
+   [begin[r], end[r]) in order; accums[r] gets its FP64 sums */
+uint64_t orc_render_batch(const orc_scene* const* scenes, const orc_camera* cams, const orc_config* cfgs,
+                          const uint64_t* begin, const uint64_t* end, int32_t nreq, uint32_t npaths, int32_t steps,
+                          double* const* accums, orc_slot* slots, int32_t nthreads);
+
 /* readback helpers (accumlation.cl) */
 void orc_intermediate(const double* accum, uint64_t npix, uint16_t* rgb16c);
 void orc_tonemap(const uint16_t* rgb16c, uint64_t npix, uint8_t* rgba8);

@@ -76,6 +76,10 @@ class rgr_stats(C.Structure):
                 ("error_flags", C.c_uint32)]
 
 
+class rgr_request_stats(C.Structure):
+    _fields_ = [("complete_ms", C.c_double), ("samples", C.c_uint64), ("pixels", C.c_uint64), ("order", C.c_uint32)]
+
+
 class rgr_ray_soa(C.Structure):
     _fields_ = [(n, C.c_void_p) for n in ("ox", "oy", "oz", "dx", "dy", "dz", "tmax")]
 
@@ -121,6 +125,14 @@ _SIGS = {
     "rgr_trace_closest_counts_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p, C.c_void_p,
                                                   C.c_void_p, C.c_void_p, C.c_void_p]),
     "rgr_set_trace_tuning": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32]),
+    "rgr_batch_create": (C.c_int, [C.c_void_p, C.c_int32, C.c_uint32]),
+    "rgr_batch_destroy": (None, [C.c_void_p]),
+    "rgr_batch_add": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "rgr_batch_run": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_void_p]),
+    "rgr_batch_readback": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_void_p, C.c_uint64]),
+    "rgr_batch_request_stats": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p]),
+    "rgr_batch_context": (C.c_void_p, [C.c_void_p]),
+    "rgr_intermediate_merge_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p]),
     "rgr_render_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_int32, C.c_void_p,
                                      C.c_void_p]),
 }
@@ -422,6 +434,12 @@ class WavefrontLane:
                                                   stream or None), "rgr_trace_closest_device")
 
 
+def merge_intermediate_device(a_ptr: int, b_ptr: int, npix: int, stream: int = 0) -> None:
+    """a <- merge of two device RGB16 intermediates (merge_intermediate, accumlation.cl:27-49)."""
+    _check(load_library().rgr_intermediate_merge_device(a_ptr, b_ptr, npix, stream or None),
+           "rgr_intermediate_merge_device")
+
+
 def slots_from_words(raw: np.ndarray) -> dict:
     out = {}
     for k, (a, b) in SLOT_FIELDS.items():
@@ -432,6 +450,68 @@ def slots_from_words(raw: np.ndarray) -> dict:
             v = v.view(np.int32)
         out[k] = v if b - a > 1 else v[:, 0]
     return out
+
+
+ORDER_FIFO, ORDER_SHORTEST_FIRST = 0, 1
+
+
+class Batch:
+    """Many render requests of uneven size sharing one path pool and one
+    graph-replayed bounce loop."""
+
+    def __init__(self, device: int = 0, path_count: int = 1 << 22):
+        self._lib = load_library()
+        self._h = C.c_void_p()
+        _check(self._lib.rgr_batch_create(C.byref(self._h), device, path_count), "rgr_batch_create")
+        self.path_count = path_count
+        self.requests = []  # (scene, camera, config)
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h and h.value:
+            self._lib.rgr_batch_destroy(h)
+            self._h = C.c_void_p()
+
+    def add(self, scene: SceneManager, camera: rgr_camera, config: rgr_render_config) -> int:
+        rid = C.c_int32()
+        _check(self._lib.rgr_batch_add(self._h, scene.handle, C.byref(camera), C.byref(config), C.byref(rid)),
+               "rgr_batch_add")
+        self.requests.append((scene, camera, config))
+        return rid.value
+
+    def run(self, order: int = ORDER_FIFO, steps_per_launch: int = 8, max_steps: int = 100000) -> int:
+        n = C.c_int32()
+        _check(self._lib.rgr_batch_run(self._h, order, steps_per_launch, max_steps, C.byref(n)), "rgr_batch_run")
+        return n.value
+
+    def accumulation(self, rid: int) -> np.ndarray:
+        cam = self.requests[rid][1]
+        out = np.zeros((cam.image_h, cam.image_w, 4), np.float64)
+        _check(self._lib.rgr_batch_readback(self._h, rid, RGR_FMT_FP64_SUMS, _ptr(out), out.nbytes),
+               "rgr_batch_readback")
+        return out
+
+    def color(self, rid: int) -> np.ndarray:
+        cam = self.requests[rid][1]
+        out = np.zeros((cam.image_h, cam.image_w, 4), np.uint8)
+        _check(self._lib.rgr_batch_readback(self._h, rid, RGR_FMT_RGBA8, _ptr(out), out.nbytes), "rgr_batch_readback")
+        return out
+
+    def request_stats(self, rid: int) -> rgr_request_stats:
+        st = rgr_request_stats()
+        _check(self._lib.rgr_batch_request_stats(self._h, rid, C.byref(st)), "rgr_batch_request_stats")
+        return st
+
+    def stats(self) -> rgr_stats:
+        st = rgr_stats()
+        _check(self._lib.rgr_render_stats(self._lib.rgr_batch_context(self._h), C.byref(st)), "rgr_render_stats")
+        return st
+
+    def debug_slots(self) -> dict:
+        raw = np.zeros((self.path_count, SLOT_WORDS), np.uint32)
+        _check(self._lib.rgr_debug_read_slots(self._lib.rgr_batch_context(self._h), _ptr(raw), self.path_count),
+               "rgr_debug_read_slots")
+        return slots_from_words(raw)
 
 
 class WavefrontPathTracing:

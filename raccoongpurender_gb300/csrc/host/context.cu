@@ -68,18 +68,139 @@ struct DevBuf {
 
 }  // namespace
 
+namespace {
+
+// A scene's device buffers and the SceneView the kernels read
+// (SceneManager::createBuffer / createMaterialBuffer / createEnvmapBuffer,
+// scene_manager.hpp:579-650).
+struct DeviceScene {
+    DevBuf nodes, prims, points, indices, spheres, materials, lambertians, wards, volumes;
+    DevBuf env_rgba, env_pdf, env_alias, env_frag;
+    SceneView sv{};
+    bool valid = false;
+
+    int upload(const rgr_scene* s, cudaStream_t st) {
+        if (!s->bvh.built) {
+            set_error("upload: build the BVH first");
+            return RGR_E_STATE;
+        }
+        const Bvh& b = s->bvh;
+        int r;
+#define UP(buf, ptr, bytes) \
+    if ((r = buf.upload((ptr), (bytes), st)) != RGR_OK) return r;
+        UP(nodes, b.nodes.data(), b.nodes.size() * sizeof(NodeD));
+        UP(prims, b.prims.data(), b.prims.size() * sizeof(PrimD));
+        const size_t nv = s->points.size() / 3, ntri = s->indices.size() / 3;
+        std::vector<float> p4(4 * nv);
+        for (size_t i = 0; i < nv; ++i) {
+            p4[4 * i] = s->points[3 * i];
+            p4[4 * i + 1] = s->points[3 * i + 1];
+            p4[4 * i + 2] = s->points[3 * i + 2];
+            p4[4 * i + 3] = 0.0f;
+        }
+        UP(points, p4.data(), p4.size() * 4);
+        UP(indices, s->indices.data(), s->indices.size() * 4);
+        UP(spheres, s->spheres.data(), s->spheres.size() * 4);
+        std::vector<MaterialRef> mats(s->tri_materials);
+        mats.insert(mats.end(), s->sphere_materials.begin(), s->sphere_materials.end());
+        UP(materials, mats.data(), mats.size() * sizeof(MaterialRef));
+        UP(lambertians, s->lambertians.data(), s->lambertians.size() * sizeof(LambertianD));
+        UP(wards, s->wards.data(), s->wards.size() * sizeof(WardD));
+        UP(volumes, s->volumes.data(), s->volumes.size() * sizeof(VolumeD));
+        const EnvTables& e = s->env;
+        std::vector<int32_t> alias2;
+        if (e.present) {
+            size_t n7 = e.alias.size();
+            alias2.resize(2 * n7);
+            for (size_t i = 0; i < n7; ++i) {
+                memcpy(&alias2[2 * i], &e.height[i], 4);
+                alias2[2 * i + 1] = e.alias[i];
+            }
+            UP(env_rgba, e.rgba.data(), e.rgba.size() * 4);
+            UP(env_pdf, e.pdf.data(), e.pdf.size() * 4);
+            UP(env_alias, alias2.data(), alias2.size() * 4);
+            UP(env_frag, e.frag.data(), e.frag.size() * 4);
+        } else {
+            UP(env_rgba, nullptr, 0);
+            UP(env_pdf, nullptr, 0);
+            UP(env_alias, nullptr, 0);
+            UP(env_frag, nullptr, 0);
+        }
+#undef UP
+        RGR_CUDA(cudaStreamSynchronize(st));  // host staging vectors go out of scope
+        SceneView& v = sv;
+        v.nodes = nodes.as<float4>();
+        v.prims = prims.as<float4>();
+        v.root_link = b.root_link;
+        v.num_prims = (uint32_t)b.prims.size();
+        v.points = points.as<float4>();
+        v.indices = indices.as<uint32_t>();
+        v.spheres = spheres.as<float4>();
+        v.sphere_begin = (int32_t)ntri;
+        v.materials = materials.as<int2>();
+        v.lambertians = lambertians.as<float4>();
+        v.wards = wards.as<float4>();
+        v.volumes = volumes.as<float4>();
+        v.env_rgba = env_rgba.as<float4>();
+        v.env_pdf = env_pdf.as<float>();
+        v.env_alias = env_alias.as<int2>();
+        v.env_frag = env_frag.as<float4>();
+        v.env_w = e.present ? e.w : 0;
+        v.env_h = e.present ? e.h : 0;
+        v.has_env = e.present ? 1 : 0;
+        bool small = true;
+        for (int k = 0; k < 6; ++k) small = small && std::fabs(b.bounds[k]) <= 1.0e30f;
+        v.small_coords = small ? 1 : 0;
+        valid = true;
+        return RGR_OK;
+    }
+};
+
+CameraD camera_d(const rgr_camera& cam) {
+    CameraD cd;
+    for (int i = 0; i < 3; ++i) {
+        cd.eye[i] = cam.eye[i];
+        cd.up[i] = cam.up[i];
+        cd.right[i] = cam.right[i];
+        cd.o[i] = cam.imageplane_o[i];
+        cd.r[i] = cam.imageplane_r[i];
+        cd.b[i] = cam.imageplane_b[i];
+    }
+    cd.w = cam.image_w;
+    cd.h = cam.image_h;
+    return cd;
+}
+
+RequestD request_d(const SceneView& sv, const rgr_camera& cam, const rgr_render_config& k, double* accum,
+                   unsigned long long begin, unsigned long long end, unsigned long long* done) {
+    RequestD q;
+    memset(&q, 0, sizeof(q));
+    q.sc = sv;
+    q.cam = camera_d(cam);
+    q.dof = k.dof;
+    q.rr_depth = k.rr_depth;
+    q.radiance_clamp = k.radiance_clamp;
+    q.env_p = k.env_select_prob;
+    q.max_depth = k.max_depth;
+    q.accum = accum;
+    q.sample_begin = begin;
+    q.sample_end = end;
+    q.done = done;
+    q.done_ns = done ? done + 1 : nullptr;
+    return q;
+}
+
+}  // namespace
+
 struct rgr_context {
     int device = 0;
     cudaStream_t stream = nullptr;
     int num_sms = 152;
     uint32_t npaths = 0, ntiles = 0;
-    // scene
-    DevBuf nodes, prims, points, indices, spheres, materials, lambertians, wards, volumes;
-    DevBuf env_rgba, env_pdf, env_alias, env_frag;
-    SceneView sv{};
-    bool uploaded = false;
+    DeviceScene scene;
     // paths
-    DevBuf ro, rd, T, L, ng, rng, vols, qid, queues[kNumQueues], counts, tile_new, scalars, accum, err;
+    DevBuf ro, rd, T, L, ng, rng, vols, qid, req, queues[kNumQueues], counts, tile_new, scalars, accum, err;
+    DevBuf reqtab, done;  // request table and its per-request (done, done_ns) counters
     PathsView pv{};
     QueueView qv{};
     RenderParams rp{};
@@ -87,8 +208,9 @@ struct rgr_context {
     uint64_t steps = 0;
     uint32_t npix = 0;
     int shade_grid = 0;
-    // CUDA graph of one bounce
+    // CUDA graph of `graph_steps` bounces
     bool graph_mode = true;
+    int graph_steps = 1;
     cudaGraphExec_t graph_exec = nullptr;
     // ray-cast service buffers
     DevBuf trays[7], tprim, tt, tread, tcounter;
@@ -99,13 +221,110 @@ struct rgr_context {
         if (graph_exec) cudaGraphExecDestroy(graph_exec);
         if (stream) cudaStreamDestroy(stream);
     }
+    // the resident path pool: state, queues, counters (WavefrontLane::setup, :451-522)
+    int alloc_pool() {
+        const size_t n = (size_t)ntiles * kTile;  // padded to whole tiles
+        int r;
+#define AL(buf, bytes) \
+    if ((r = buf.alloc(bytes)) != RGR_OK) return r;
+        AL(ro, 16 * n);
+        AL(rd, 16 * n);
+        AL(T, 16 * n);
+        AL(L, 16 * n);
+        AL(ng, 16 * n);
+        AL(rng, 16 * n);
+        AL(vols, 32 * n);
+        AL(qid, n);
+        AL(req, 2 * n);
+        for (int q = 0; q < kNumQueues; ++q) AL(queues[q], 4 * n);
+        AL(counts, 4 * 8);
+        AL(tile_new, 4 * (size_t)ntiles);
+        AL(scalars, 8 * 8);
+        AL(err, 16);
+#undef AL
+        PathsView& p = pv;
+        p.ro = ro.as<float4>();
+        p.rd = rd.as<float4>();
+        p.T = T.as<float4>();
+        p.L = L.as<float4>();
+        p.ng = ng.as<float4>();
+        p.rng = rng.as<uint4>();
+        p.vols = vols.as<int4>();
+        p.qid = qid.as<uint8_t>();
+        p.req = req.as<uint16_t>();
+        p.n = npaths;
+        QueueView& q = qv;
+        for (int i = 0; i < kNumQueues; ++i) q.items[i] = queues[i].as<uint32_t>();
+        q.counts = counts.as<uint32_t>();
+        q.tile_new = tile_new.as<uint32_t>();
+        q.ntiles = ntiles;
+        unsigned long long* sc = scalars.as<unsigned long long>();
+        q.next_pixel = sc + 0;
+        q.step_base = sc + 1;
+        rp.err = err.as<uint32_t>();
+        rp.rays = sc + 2;
+        return RGR_OK;
+    }
+    // reset the pool and counters for a new render with `nreq` requests in reqtab
+    int start(const RequestD* host_reqs, int nreq, unsigned long long limit, uint32_t seed_offset) {
+        cudaStream_t st = stream;
+        int r;
+        if ((r = reqtab.alloc(sizeof(RequestD) * nreq)) != RGR_OK) return r;
+        RGR_CUDA(cudaMemcpyAsync(reqtab.p, host_reqs, sizeof(RequestD) * nreq, cudaMemcpyHostToDevice, st));
+        rp.reqs = reqtab.as<RequestD>();
+        rp.nreq = nreq;
+        rp.sample_limit = limit;
+        RGR_CUDA(cudaMemsetAsync(counts.p, 0, 32, st));
+        RGR_CUDA(cudaMemsetAsync(scalars.p, 0, 64, st));
+        RGR_CUDA(cudaMemsetAsync(err.p, 0, 16, st));
+        launch_init(pv, qv, seed_offset, st);
+        RGR_CUDA(cudaGetLastError());
+        RGR_CUDA(cudaStreamSynchronize(st));  // host_reqs may be a temporary
+        shade_grid = num_sms * 8;
+        steps = 0;
+        begun = true;
+        drop_graph();
+        return RGR_OK;
+    }
     int step_launches(cudaStream_t st) {
         launch_compact_new(pv, qv, st);
-        launch_shade(sv, pv, qv, rp, shade_grid, st);
+        launch_shade(pv, qv, rp, shade_grid, st);
         RGR_CUDA(cudaMemsetAsync(qv.counts + 1, 0, sizeof(uint32_t) * (kNumQueues - 1), st));
         RGR_CUDA(cudaMemsetAsync(qv.tile_new, 0, sizeof(uint32_t) * ntiles, st));
-        launch_trace_logic(sv, pv, qv, rp, 128, st);
+        launch_trace_logic(pv, qv, rp, st);
         RGR_CUDA(cudaGetLastError());
+        return RGR_OK;
+    }
+    // run `n` bounces: replays of a graph of graph_steps bounces, then single ones
+    int run_steps(int n) {
+        cudaStream_t st = stream;
+        while (n > 0) {
+            if (graph_mode) {
+                const int k = n >= graph_steps ? graph_steps : 1;
+                if (k == graph_steps || graph_steps == 1) {
+                    if (!graph_exec) {
+                        cudaGraph_t g = nullptr;
+                        RGR_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+                        int r = RGR_OK;
+                        for (int i = 0; i < graph_steps && r == RGR_OK; ++i) r = step_launches(st);
+                        cudaError_t e = cudaStreamEndCapture(st, &g);
+                        if (r != RGR_OK) return r;
+                        RGR_CUDA(e);
+                        e = cudaGraphInstantiate(&graph_exec, g, 0);
+                        cudaGraphDestroy(g);
+                        RGR_CUDA(e);
+                    }
+                    RGR_CUDA(cudaGraphLaunch(graph_exec, st));
+                    n -= graph_steps;
+                    steps += graph_steps;
+                    continue;
+                }
+            }
+            int r = step_launches(st);
+            if (r != RGR_OK) return r;
+            n -= 1;
+            steps += 1;
+        }
         return RGR_OK;
     }
     void drop_graph() {
@@ -116,9 +335,9 @@ struct rgr_context {
 
 // read-only view of a context's uploaded scene, for rgr_render_noalloc (noalloc.cu)
 const rgr::dev::SceneView* rgr_context_scene_view(const rgr_context* c, int* device) {
-    if (!c || !c->uploaded) return nullptr;
+    if (!c || !c->scene.valid) return nullptr;
     if (device) *device = c->device;
-    return &c->sv;
+    return &c->scene.sv;
 }
 
 extern "C" {
@@ -164,88 +383,17 @@ int rgr_set_graph_mode(rgr_context* c, int32_t enabled) {
 
 int rgr_device_upload(rgr_context* c, const rgr_scene* s) {
     if (!c || !s) return RGR_E_INVALID;
-    if (!s->bvh.built) {
-        set_error("rgr_device_upload: build the BVH first");
-        return RGR_E_STATE;
-    }
     RGR_CUDA(cudaSetDevice(c->device));
-    cudaStream_t st = c->stream;
-    const Bvh& b = s->bvh;
-    int r;
-#define UP(buf, ptr, bytes)                                  \
-    if ((r = c->buf.upload((ptr), (bytes), st)) != RGR_OK) return r;
-    UP(nodes, b.nodes.data(), b.nodes.size() * sizeof(NodeD));
-    UP(prims, b.prims.data(), b.prims.size() * sizeof(PrimD));
-    const size_t nv = s->points.size() / 3, ntri = s->indices.size() / 3, nsph = s->spheres.size() / 4;
-    std::vector<float> p4(4 * nv);
-    for (size_t i = 0; i < nv; ++i) {
-        p4[4 * i] = s->points[3 * i];
-        p4[4 * i + 1] = s->points[3 * i + 1];
-        p4[4 * i + 2] = s->points[3 * i + 2];
-        p4[4 * i + 3] = 0.0f;
-    }
-    UP(points, p4.data(), p4.size() * 4);
-    UP(indices, s->indices.data(), s->indices.size() * 4);
-    UP(spheres, s->spheres.data(), s->spheres.size() * 4);
-    std::vector<MaterialRef> mats(s->tri_materials);
-    mats.insert(mats.end(), s->sphere_materials.begin(), s->sphere_materials.end());
-    UP(materials, mats.data(), mats.size() * sizeof(MaterialRef));
-    UP(lambertians, s->lambertians.data(), s->lambertians.size() * sizeof(LambertianD));
-    UP(wards, s->wards.data(), s->wards.size() * sizeof(WardD));
-    UP(volumes, s->volumes.data(), s->volumes.size() * sizeof(VolumeD));
-    const EnvTables& e = s->env;
-    std::vector<int32_t> alias2;
-    if (e.present) {
-        size_t n7 = e.alias.size();
-        alias2.resize(2 * n7);
-        for (size_t i = 0; i < n7; ++i) {
-            memcpy(&alias2[2 * i], &e.height[i], 4);
-            alias2[2 * i + 1] = e.alias[i];
-        }
-        UP(env_rgba, e.rgba.data(), e.rgba.size() * 4);
-        UP(env_pdf, e.pdf.data(), e.pdf.size() * 4);
-        UP(env_alias, alias2.data(), alias2.size() * 4);
-        UP(env_frag, e.frag.data(), e.frag.size() * 4);
-    } else {
-        UP(env_rgba, nullptr, 0);
-        UP(env_pdf, nullptr, 0);
-        UP(env_alias, nullptr, 0);
-        UP(env_frag, nullptr, 0);
-    }
-#undef UP
-    RGR_CUDA(cudaStreamSynchronize(st));  // host staging vectors go out of scope
-    SceneView& v = c->sv;
-    v.nodes = c->nodes.as<float4>();
-    v.prims = c->prims.as<float4>();
-    v.root_link = b.root_link;
-    v.num_prims = (uint32_t)b.prims.size();
-    v.points = c->points.as<float4>();
-    v.indices = c->indices.as<uint32_t>();
-    v.spheres = c->spheres.as<float4>();
-    v.sphere_begin = (int32_t)ntri;
-    (void)nsph;
-    v.materials = c->materials.as<int2>();
-    v.lambertians = c->lambertians.as<float4>();
-    v.wards = c->wards.as<float4>();
-    v.volumes = c->volumes.as<float4>();
-    v.env_rgba = c->env_rgba.as<float4>();
-    v.env_pdf = c->env_pdf.as<float>();
-    v.env_alias = c->env_alias.as<int2>();
-    v.env_frag = c->env_frag.as<float4>();
-    v.env_w = e.present ? e.w : 0;
-    v.env_h = e.present ? e.h : 0;
-    v.has_env = e.present ? 1 : 0;
-    bool small = true;
-    for (int k = 0; k < 6; ++k) small = small && std::fabs(b.bounds[k]) <= 1.0e30f;
-    v.small_coords = small ? 1 : 0;
-    c->uploaded = true;
+    int r = c->scene.upload(s, c->stream);
+    if (r != RGR_OK) return r;
+    c->begun = false;
     c->drop_graph();
     return RGR_OK;
 }
 
 int rgr_render_begin(rgr_context* c, const rgr_camera* cam, const rgr_render_config* cfg) {
     if (!c || !cam) return RGR_E_INVALID;
-    if (!c->uploaded) {
+    if (!c->scene.valid) {
         set_error("rgr_render_begin: upload a scene first");
         return RGR_E_STATE;
     }
@@ -255,105 +403,24 @@ int rgr_render_begin(rgr_context* c, const rgr_camera* cam, const rgr_render_con
     rgr_render_config_default(&d);
     const rgr_render_config& k = cfg ? *cfg : d;
     RGR_CUDA(cudaSetDevice(c->device));
-    cudaStream_t st = c->stream;
-    const size_t n = (size_t)c->ntiles * kTile;  // padded to whole tiles
-    int r;
-#define AL(buf, bytes)                                    \
-    if ((r = c->buf.alloc(bytes)) != RGR_OK) return r;
-    AL(ro, 16 * n);
-    AL(rd, 16 * n);
-    AL(T, 16 * n);
-    AL(L, 16 * n);
-    AL(ng, 16 * n);
-    AL(rng, 16 * n);
-    AL(vols, 32 * n);
-    AL(qid, n);
-    for (int q = 0; q < kNumQueues; ++q) AL(queues[q], 4 * n);
-    AL(counts, 4 * 8);
-    AL(tile_new, 4 * (size_t)c->ntiles);
-    AL(scalars, 8 * 8);
-    AL(err, 16);
+    int r = c->alloc_pool();
+    if (r != RGR_OK) return r;
     c->npix = cam->image_w * cam->image_h;
-    AL(accum, 32 * (size_t)c->npix);
-#undef AL
-    PathsView& p = c->pv;
-    p.ro = c->ro.as<float4>();
-    p.rd = c->rd.as<float4>();
-    p.T = c->T.as<float4>();
-    p.L = c->L.as<float4>();
-    p.ng = c->ng.as<float4>();
-    p.rng = c->rng.as<uint4>();
-    p.vols = c->vols.as<int4>();
-    p.qid = c->qid.as<uint8_t>();
-    p.n = c->npaths;
-    QueueView& q = c->qv;
-    for (int i = 0; i < kNumQueues; ++i) q.items[i] = c->queues[i].as<uint32_t>();
-    q.counts = c->counts.as<uint32_t>();
-    q.tile_new = c->tile_new.as<uint32_t>();
-    q.ntiles = c->ntiles;
-    unsigned long long* sc = c->scalars.as<unsigned long long>();
-    q.next_pixel = sc + 0;
-    q.step_base = sc + 1;
-    RenderParams& rp = c->rp;
-    CameraD& cd = rp.cam;
-    for (int i = 0; i < 3; ++i) {
-        cd.eye[i] = cam->eye[i];
-        cd.up[i] = cam->up[i];
-        cd.right[i] = cam->right[i];
-        cd.o[i] = cam->imageplane_o[i];
-        cd.r[i] = cam->imageplane_r[i];
-        cd.b[i] = cam->imageplane_b[i];
-    }
-    cd.w = cam->image_w;
-    cd.h = cam->image_h;
-    rp.dof = k.dof;
-    rp.rr_depth = k.rr_depth;
-    rp.radiance_clamp = k.radiance_clamp;
-    rp.env_p = k.env_select_prob;
-    rp.max_depth = k.max_depth;
-    rp.sample_limit = k.spp ? (unsigned long long)k.spp * c->npix : 0ull;
-    rp.accum = c->accum.as<double>();
-    rp.err = c->err.as<uint32_t>();
-    rp.rays = sc + 2;
-    RGR_CUDA(cudaMemsetAsync(c->accum.p, 0, 32 * (size_t)c->npix, st));
-    RGR_CUDA(cudaMemsetAsync(c->counts.p, 0, 32, st));
-    RGR_CUDA(cudaMemsetAsync(c->scalars.p, 0, 64, st));
-    RGR_CUDA(cudaMemsetAsync(c->err.p, 0, 16, st));
-    launch_init(p, q, k.seed_offset, st);
-    RGR_CUDA(cudaGetLastError());
-    c->shade_grid = c->num_sms * 8;
-    c->steps = 0;
-    c->begun = true;
-    c->drop_graph();
-    return RGR_OK;
+    if ((r = c->accum.alloc(32 * (size_t)c->npix)) != RGR_OK) return r;
+    if ((r = c->done.alloc(16)) != RGR_OK) return r;
+    RGR_CUDA(cudaMemsetAsync(c->accum.p, 0, 32 * (size_t)c->npix, c->stream));
+    RGR_CUDA(cudaMemsetAsync(c->done.p, 0, 16, c->stream));
+    const unsigned long long limit = k.spp ? (unsigned long long)k.spp * c->npix : 0ull;
+    RequestD q = request_d(c->scene.sv, *cam, k, c->accum.as<double>(), 0ull, limit ? limit : ~0ull,
+                           c->done.as<unsigned long long>());
+    return c->start(&q, 1, limit, k.seed_offset);
 }
 
 int rgr_render_step(rgr_context* c, int32_t steps) {
     if (!c || steps < 0) return RGR_E_INVALID;
     if (!c->begun) return RGR_E_STATE;
     RGR_CUDA(cudaSetDevice(c->device));
-    cudaStream_t st = c->stream;
-    for (int32_t i = 0; i < steps; ++i) {
-        if (c->graph_mode) {
-            if (!c->graph_exec) {
-                cudaGraph_t g = nullptr;
-                RGR_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-                int r = c->step_launches(st);
-                cudaError_t e = cudaStreamEndCapture(st, &g);
-                if (r != RGR_OK) return r;
-                RGR_CUDA(e);
-                e = cudaGraphInstantiate(&c->graph_exec, g, 0);
-                cudaGraphDestroy(g);
-                RGR_CUDA(e);
-            }
-            RGR_CUDA(cudaGraphLaunch(c->graph_exec, st));
-        } else {
-            int r = c->step_launches(st);
-            if (r != RGR_OK) return r;
-        }
-        c->steps++;
-    }
-    return RGR_OK;
+    return c->run_steps(steps);
 }
 
 int rgr_synchronize(rgr_context* c) {
@@ -463,7 +530,7 @@ int rgr_accum_merge(rgr_context* dst, rgr_context* src) {
 int rgr_trace_closest_device(rgr_context* c, const rgr_ray_soa* rays, uint64_t n, int32_t* prim, float* t,
                              float* ng_xyz, void* stream) {
     if (!c || !rays || !prim || !t) return RGR_E_INVALID;
-    if (!c->uploaded) return RGR_E_STATE;
+    if (!c->scene.valid) return RGR_E_STATE;
     if (n == 0) return RGR_OK;
     if (!rays->ox || !rays->oy || !rays->oz || !rays->dx || !rays->dy || !rays->dz || !rays->tmax)
         return RGR_E_INVALID;
@@ -472,8 +539,16 @@ int rgr_trace_closest_device(rgr_context* c, const rgr_ray_soa* rays, uint64_t n
     int r = c->err.alloc(16);
     if (r != RGR_OK) return r;
     if ((r = c->tcounter.alloc(8)) != RGR_OK) return r;
-    launch_trace_rays(c->sv, rays->ox, rays->oy, rays->oz, rays->dx, rays->dy, rays->dz, rays->tmax, n, prim, t, ng_xyz,
+    launch_trace_rays(c->scene.sv, rays->ox, rays->oy, rays->oz, rays->dx, rays->dy, rays->dz, rays->tmax, n, prim, t, ng_xyz,
                       c->err.as<uint32_t>(), c->tcounter.as<unsigned long long>(), c->trace_refill, c->trace_grid, st);
+    RGR_CUDA(cudaGetLastError());
+    return RGR_OK;
+}
+
+int rgr_intermediate_merge_device(void* a, const void* b, uint64_t npix, void* stream) {
+    if (!a || !b || npix > 0xffffffffull) return RGR_E_INVALID;
+    if (npix == 0) return RGR_OK;
+    launch_merge_intermediate(a, b, (uint32_t)npix, (cudaStream_t)stream);
     RGR_CUDA(cudaGetLastError());
     return RGR_OK;
 }
@@ -490,14 +565,14 @@ int rgr_set_trace_tuning(rgr_context* c, int32_t refill, int32_t blocks_per_sm) 
 int rgr_trace_closest_counts_device(rgr_context* c, const rgr_ray_soa* rays, uint64_t n, int32_t* prim, float* t,
                                     uint32_t* node_visits, uint32_t* prim_tests, void* stream) {
     if (!c || !rays || !prim || !t || !node_visits || !prim_tests) return RGR_E_INVALID;
-    if (!c->uploaded) return RGR_E_STATE;
+    if (!c->scene.valid) return RGR_E_STATE;
     if (n == 0) return RGR_OK;
     RGR_CUDA(cudaSetDevice(c->device));
     cudaStream_t st = stream ? (cudaStream_t)stream : c->stream;
     int r = c->err.alloc(16);
     if (r != RGR_OK) return r;
     if ((r = c->tcounter.alloc(8)) != RGR_OK) return r;
-    launch_trace_rays_counts(c->sv, rays->ox, rays->oy, rays->oz, rays->dx, rays->dy, rays->dz, rays->tmax, n, prim, t,
+    launch_trace_rays_counts(c->scene.sv, rays->ox, rays->oy, rays->oz, rays->dx, rays->dy, rays->dz, rays->tmax, n, prim, t,
                              node_visits, prim_tests, c->err.as<uint32_t>(), c->tcounter.as<unsigned long long>(),
                              c->trace_grid, st);
     RGR_CUDA(cudaGetLastError());
@@ -506,7 +581,7 @@ int rgr_trace_closest_counts_device(rgr_context* c, const rgr_ray_soa* rays, uin
 
 int rgr_trace_closest(rgr_context* c, const rgr_ray_soa* rays, uint64_t n, int32_t* prim, float* t) {
     if (!c || !rays || !prim || !t) return RGR_E_INVALID;
-    if (!c->uploaded) return RGR_E_STATE;
+    if (!c->scene.valid) return RGR_E_STATE;
     if (n == 0) return RGR_OK;
     RGR_CUDA(cudaSetDevice(c->device));
     cudaStream_t st = c->stream;
@@ -550,5 +625,202 @@ int rgr_debug_read_slots(rgr_context* c, uint32_t* out, uint64_t nslots) {
     RGR_CUDA(cudaMemcpyAsync(out, c->tread.p, bytes, cudaMemcpyDeviceToHost, st));
     return rgr_synchronize(c);
 }
+
+}  // extern "C"
+
+// ======================================================================
+// Batched requests: many renders of uneven size share one path pool.  Each
+// request owns a range of the global sample index (in run order), so the
+// new-path compaction hands free slots to the requests in that order and a
+// slot renders its request's scene with its camera and constants.  The
+// bounce loop is replayed from a CUDA graph; every request's last finished
+// path stamps %globaltimer, giving per-request completion latency.
+struct rgr_batch {
+    rgr_context* ctx = nullptr;
+    struct Req {
+        const rgr_scene* scene;
+        int scene_index;
+        rgr_camera cam;
+        rgr_render_config cfg;
+        uint64_t npix, samples;
+        DevBuf accum;
+        double complete_ms = -1.0;
+        uint32_t order = 0;
+        uint64_t accumulated = 0;
+    };
+    std::vector<std::unique_ptr<DeviceScene>> scenes;
+    std::vector<const rgr_scene*> scene_keys;
+    std::vector<std::unique_ptr<Req>> reqs;
+    DevBuf stamp;  // start time of the run (%globaltimer)
+    ~rgr_batch() { delete ctx; }
+};
+
+namespace {
+__global__ void k_stamp(unsigned long long* out) {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    *out = t;
+}
+}  // namespace
+
+extern "C" {
+
+int rgr_batch_create(rgr_batch** out, int32_t device, uint32_t path_count) {
+    if (!out) return RGR_E_INVALID;
+    rgr_batch* b = new (std::nothrow) rgr_batch();
+    if (!b) return RGR_E_OOM;
+    int r = rgr_context_create(&b->ctx, device, path_count);
+    if (r != RGR_OK) {
+        delete b;
+        return r;
+    }
+    *out = b;
+    return RGR_OK;
+}
+
+void rgr_batch_destroy(rgr_batch* b) {
+    if (!b) return;
+    if (b->ctx) {
+        cudaSetDevice(b->ctx->device);
+        cudaStreamSynchronize(b->ctx->stream);
+    }
+    delete b;
+}
+
+int rgr_batch_add(rgr_batch* b, const rgr_scene* s, const rgr_camera* cam, const rgr_render_config* cfg,
+                  int32_t* id) {
+    if (!b || !s || !cam || !cfg || cfg->spp == 0) {
+        set_error("rgr_batch_add: every request needs a scene, a camera and spp > 0");
+        return RGR_E_INVALID;
+    }
+    if (b->reqs.size() >= 65535) return RGR_E_INVALID;
+    if (cam->image_w == 0 || cam->image_h == 0 || (uint64_t)cam->image_w * cam->image_h > (1ull << 31))
+        return RGR_E_INVALID;
+    rgr_context* c = b->ctx;
+    RGR_CUDA(cudaSetDevice(c->device));
+    int si = -1;
+    for (size_t i = 0; i < b->scene_keys.size(); ++i)
+        if (b->scene_keys[i] == s) si = (int)i;
+    if (si < 0) {
+        std::unique_ptr<DeviceScene> ds(new DeviceScene());
+        int r = ds->upload(s, c->stream);
+        if (r != RGR_OK) return r;
+        si = (int)b->scenes.size();
+        b->scenes.push_back(std::move(ds));
+        b->scene_keys.push_back(s);
+    }
+    std::unique_ptr<rgr_batch::Req> q(new rgr_batch::Req());
+    q->scene = s;
+    q->scene_index = si;
+    q->cam = *cam;
+    q->cfg = *cfg;
+    q->npix = (uint64_t)cam->image_w * cam->image_h;
+    q->samples = q->npix * cfg->spp;
+    int r = q->accum.alloc(32 * q->npix);
+    if (r != RGR_OK) return r;
+    if (id) *id = (int32_t)b->reqs.size();
+    b->reqs.push_back(std::move(q));
+    return RGR_OK;
+}
+
+int rgr_batch_run(rgr_batch* b, int32_t order_policy, int32_t steps_per_launch, int32_t max_steps,
+                  int32_t* steps_done) {
+    if (!b || b->reqs.empty() || steps_per_launch < 1 || max_steps < 1) return RGR_E_INVALID;
+    rgr_context* c = b->ctx;
+    RGR_CUDA(cudaSetDevice(c->device));
+    cudaStream_t st = c->stream;
+    const int n = (int)b->reqs.size();
+    // run order: submission order, or fewest samples first (shortest job first)
+    std::vector<int> order(n);
+    for (int i = 0; i < n; ++i) order[i] = i;
+    if (order_policy == RGR_ORDER_SHORTEST_FIRST)
+        std::stable_sort(order.begin(), order.end(),
+                         [&](int x, int y) { return b->reqs[x]->samples < b->reqs[y]->samples; });
+    int r = c->alloc_pool();
+    if (r != RGR_OK) return r;
+    if ((r = c->done.alloc(16 * (size_t)n)) != RGR_OK) return r;
+    if ((r = b->stamp.alloc(8)) != RGR_OK) return r;
+    RGR_CUDA(cudaMemsetAsync(c->done.p, 0, 16 * (size_t)n, st));
+    std::vector<RequestD> table(n);
+    unsigned long long begin = 0;
+    for (int k = 0; k < n; ++k) {
+        rgr_batch::Req& q = *b->reqs[order[k]];
+        q.order = (uint32_t)k;
+        RGR_CUDA(cudaMemsetAsync(q.accum.p, 0, 32 * q.npix, st));
+        table[k] = request_d(b->scenes[q.scene_index]->sv, q.cam, q.cfg, q.accum.as<double>(), begin,
+                             begin + q.samples, c->done.as<unsigned long long>() + 2 * k);
+        begin += q.samples;
+    }
+    c->npix = 0;
+    r = c->start(table.data(), n, begin, b->reqs[order[0]]->cfg.seed_offset);
+    if (r != RGR_OK) return r;
+    c->graph_steps = steps_per_launch;
+    k_stamp<<<1, 1, 0, st>>>(b->stamp.as<unsigned long long>());
+    std::vector<unsigned long long> done(2 * n);
+    int32_t ran = 0;
+    bool all = false;
+    while (ran < max_steps && !all) {
+        r = c->run_steps(steps_per_launch);
+        if (r != RGR_OK) return r;
+        ran += steps_per_launch;
+        RGR_CUDA(cudaMemcpyAsync(done.data(), c->done.p, 16 * (size_t)n, cudaMemcpyDeviceToHost, st));
+        RGR_CUDA(cudaStreamSynchronize(st));
+        all = true;
+        for (int k = 0; k < n; ++k) all = all && done[2 * k] == table[k].sample_end - table[k].sample_begin;
+    }
+    c->graph_steps = 1;
+    c->drop_graph();
+    unsigned long long t0 = 0;
+    RGR_CUDA(cudaMemcpy(&t0, b->stamp.p, 8, cudaMemcpyDeviceToHost));
+    for (int k = 0; k < n; ++k) {
+        rgr_batch::Req& q = *b->reqs[order[k]];
+        const bool fin = done[2 * k] == table[k].sample_end - table[k].sample_begin;
+        q.complete_ms = fin ? (double)(done[2 * k + 1] - t0) * 1e-6 : -1.0;
+    }
+    if (steps_done) *steps_done = ran;
+    uint32_t err = 0;
+    RGR_CUDA(cudaMemcpy(&err, c->err.p, 4, cudaMemcpyDeviceToHost));
+    if (err) {
+        set_error("device capacity check fired (flags " + std::to_string(err) + ")");
+        return RGR_E_OVERFLOW;
+    }
+    return all ? RGR_OK : RGR_E_STATE;
+}
+
+int rgr_batch_readback(rgr_batch* b, int32_t id, int32_t fmt, void* dst, uint64_t dst_bytes) {
+    if (!b || !dst || id < 0 || id >= (int32_t)b->reqs.size()) return RGR_E_INVALID;
+    rgr_context* c = b->ctx;
+    rgr_batch::Req& q = *b->reqs[id];
+    RGR_CUDA(cudaSetDevice(c->device));
+    cudaStream_t st = c->stream;
+    if (fmt == RGR_FMT_FP64_SUMS) {
+        if (dst_bytes < 32 * q.npix) return RGR_E_INVALID;
+        RGR_CUDA(cudaMemcpyAsync(dst, q.accum.p, 32 * q.npix, cudaMemcpyDeviceToHost, st));
+    } else if (fmt == RGR_FMT_RGBA8 || fmt == RGR_FMT_RGB16) {
+        size_t bytes = (fmt == RGR_FMT_RGBA8 ? 4 : 8) * q.npix;
+        if (dst_bytes < bytes) return RGR_E_INVALID;
+        int r = c->tread.alloc(bytes);
+        if (r != RGR_OK) return r;
+        launch_readback(fmt, q.accum.as<double>(), (uint32_t)q.npix, c->tread.p, st);
+        RGR_CUDA(cudaGetLastError());
+        RGR_CUDA(cudaMemcpyAsync(dst, c->tread.p, bytes, cudaMemcpyDeviceToHost, st));
+    } else {
+        return RGR_E_INVALID;
+    }
+    RGR_CUDA(cudaStreamSynchronize(st));
+    return RGR_OK;
+}
+
+int rgr_batch_request_stats(rgr_batch* b, int32_t id, rgr_request_stats* out) {
+    if (!b || !out || id < 0 || id >= (int32_t)b->reqs.size()) return RGR_E_INVALID;
+    const rgr_batch::Req& q = *b->reqs[id];
+    out->complete_ms = q.complete_ms;
+    out->samples = q.samples;
+    out->order = q.order;
+    out->pixels = q.npix;
+    return RGR_OK;
+}
+
+rgr_context* rgr_batch_context(rgr_batch* b) { return b ? b->ctx : nullptr; }
 
 }  // extern "C"

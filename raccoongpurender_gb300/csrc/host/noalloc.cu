@@ -54,12 +54,14 @@ constexpr size_t kOffNg = kOffL + align256(16 * kN);
 constexpr size_t kOffRng = kOffNg + align256(16 * kN);
 constexpr size_t kOffVols = kOffRng + align256(16 * kN);
 constexpr size_t kOffQid = kOffVols + align256(32 * kN);
-constexpr size_t kOffQueues = kOffQid + align256(kN);
+constexpr size_t kOffReq = kOffQid + align256(kN);
+constexpr size_t kOffQueues = kOffReq + align256(2 * kN);
 constexpr size_t kOffCounts = kOffQueues + align256(4 * kN) * kNumQueues;
 constexpr size_t kOffTiles = kOffCounts + 256;
 constexpr size_t kOffScalars = kOffTiles + align256(4 * kNoAllocTiles);
 constexpr size_t kOffErr = kOffScalars + 256;
-constexpr size_t kScratchBytes = kOffErr + 256;
+constexpr size_t kOffRequest = kOffErr + 256;
+constexpr size_t kScratchBytes = kOffRequest + align256(sizeof(RequestD));
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 
@@ -128,6 +130,7 @@ extern "C" int rgr_render_noalloc(rgr_context* c, const rgr_camera* cam, const r
     p.rng = reinterpret_cast<uint4*>(base + kOffRng);
     p.vols = reinterpret_cast<int4*>(base + kOffVols);
     p.qid = base + kOffQid;
+    p.req = reinterpret_cast<uint16_t*>(base + kOffReq);
     p.n = path_count;
     QueueView q;
     for (int i = 0; i < kNumQueues; ++i) q.items[i] = reinterpret_cast<uint32_t*>(base + kOffQueues + align256(4 * kN) * i);
@@ -137,8 +140,11 @@ extern "C" int rgr_render_noalloc(rgr_context* c, const rgr_camera* cam, const r
     unsigned long long* scal = reinterpret_cast<unsigned long long*>(base + kOffScalars);
     q.next_pixel = scal + 0;
     q.step_base = scal + 1;
-    RenderParams rp;
-    CameraD& cd = rp.cam;
+    // the one-request table (kernels read scene, camera and constants from it)
+    RequestD rq;
+    memset(&rq, 0, sizeof(rq));
+    rq.sc = *sv;
+    CameraD& cd = rq.cam;
     for (int i = 0; i < 3; ++i) {
         cd.eye[i] = cam->eye[i];
         cd.up[i] = cam->up[i];
@@ -149,13 +155,21 @@ extern "C" int rgr_render_noalloc(rgr_context* c, const rgr_camera* cam, const r
     }
     cd.w = cam->image_w;
     cd.h = cam->image_h;
-    rp.dof = k.dof;
-    rp.rr_depth = k.rr_depth;
-    rp.radiance_clamp = k.radiance_clamp;
-    rp.env_p = k.env_select_prob;
-    rp.max_depth = k.max_depth;
-    rp.sample_limit = k.spp ? (unsigned long long)k.spp * npix : 0ull;
-    rp.accum = accum_out;
+    rq.dof = k.dof;
+    rq.rr_depth = k.rr_depth;
+    rq.radiance_clamp = k.radiance_clamp;
+    rq.env_p = k.env_select_prob;
+    rq.max_depth = k.max_depth;
+    rq.accum = accum_out;
+    const unsigned long long limit = k.spp ? (unsigned long long)k.spp * npix : 0ull;
+    rq.sample_begin = 0;
+    rq.sample_end = limit ? limit : ~0ull;
+    rq.done = nullptr;
+    rq.done_ns = nullptr;
+    RenderParams rp;
+    rp.reqs = reinterpret_cast<const RequestD*>(base + kOffRequest);
+    rp.nreq = 1;
+    rp.sample_limit = limit;
     rp.err = reinterpret_cast<uint32_t*>(base + kOffErr);
     rp.rays = scal + 2;
 
@@ -163,18 +177,19 @@ extern "C" int rgr_render_noalloc(rgr_context* c, const rgr_camera* cam, const r
     if (!ok(cudaMemsetAsync(base + kOffCounts, 0, 256, st), "cudaMemsetAsync") ||
         !ok(cudaMemsetAsync(base + kOffScalars, 0, 256, st), "cudaMemsetAsync") ||
         !ok(cudaMemsetAsync(base + kOffErr, 0, 256, st), "cudaMemsetAsync") ||
-        !ok(cudaMemsetAsync(accum_out, 0, sizeof(double) * 4 * (size_t)npix, st), "cudaMemsetAsync"))
+        !ok(cudaMemsetAsync(accum_out, 0, sizeof(double) * 4 * (size_t)npix, st), "cudaMemsetAsync") ||
+        !ok(cudaMemcpyAsync(base + kOffRequest, &rq, sizeof(rq), cudaMemcpyHostToDevice, st), "cudaMemcpyAsync"))
         return RGR_E_CUDA;
     launch_init(p, q, k.seed_offset, st);
     int sms = 152;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
     for (int32_t i = 0; i < steps; ++i) {
         launch_compact_new(p, q, st);
-        launch_shade(*sv, p, q, rp, sms * 8, st);
+        launch_shade(p, q, rp, sms * 8, st);
         if (!ok(cudaMemsetAsync(q.counts + 1, 0, sizeof(uint32_t) * (kNumQueues - 1), st), "cudaMemsetAsync") ||
             !ok(cudaMemsetAsync(q.tile_new, 0, sizeof(uint32_t) * ntiles, st), "cudaMemsetAsync"))
             return RGR_E_CUDA;
-        launch_trace_logic(*sv, p, q, rp, 128, st);
+        launch_trace_logic(p, q, rp, st);
     }
     if (!ok(cudaGetLastError(), "kernel launch")) return RGR_E_CUDA;
     uint32_t err = 0;

@@ -214,8 +214,8 @@ RGR_DEV float incident_pdf(const Incident& is) {  // types.cl:65-71
 
 // One slot's share of a step, from new_path to homogeneous_volume_through.
 // k: the queue the slot came from (0 = new path, else its material type).
-RGR_DEV void shade_slot(const SceneView& sc, const PathsView& P, const RenderParams& rp, int k, uint32_t slot,
-                        unsigned long long gpix) {
+RGR_DEV void shade_slot(const RequestD& rq, const PathsView& P, int k, uint32_t slot, unsigned long long gpix) {
+    const SceneView& sc = rq.sc;
     float4 ro4 = P.ro[slot], rd4 = P.rd[slot], T4 = P.T[slot], L4 = P.L[slot], ng4 = P.ng[slot];
     int4 va = P.vols[2 * (size_t)slot], vb = P.vols[2 * (size_t)slot + 1];
     Rng rng = rng_load(P.rng, slot);
@@ -228,7 +228,7 @@ RGR_DEV void shade_slot(const SceneView& sc, const PathsView& P, const RenderPar
     int vcount = vb.w;
 
     if (k == 0) {  // new_path (new_path.cl:17-83)
-        const CameraD& cam = rp.cam;
+        const CameraD& cam = rq.cam;
         T = mk(1, 1, 1);
         L = mk(0, 0, 0);
         logic_i = 0;
@@ -245,8 +245,8 @@ RGR_DEV void shade_slot(const SceneView& sc, const PathsView& P, const RenderPar
         float theta = (float)((double)u1 * kPiD * 2.0);
         float s, c;
         sincos_(theta, &s, &c);
-        float lensx = rp.dof * r * c;
-        float lensy = rp.dof * r * s;
+        float lensx = rq.dof * r * c;
+        float lensy = rq.dof * r * s;
         f3 lens = mk(cam.eye[0], cam.eye[1], cam.eye[2]) + mk(cam.up[0], cam.up[1], cam.up[2]) * lensx +
                   mk(cam.right[0], cam.right[1], cam.right[2]) * lensy;
         ro = lens;
@@ -266,7 +266,7 @@ RGR_DEV void shade_slot(const SceneView& sc, const PathsView& P, const RenderPar
     const bool surface_hit = 0 <= hs, volume_hit = 0 <= hv;
     int envq = -1;
     if (surface_hit || volume_hit) {
-        const float env_p = sc.has_env ? rp.env_p : 0.0f;
+        const float env_p = sc.has_env ? rq.env_p : 0.0f;
         if (surface_hit) {
             int mt = __ldg(sc.materials + hs).x;
             if (mt == kMatLambertian || mt == kMatWard) {
@@ -534,6 +534,7 @@ __global__ void k_init(PathsView P, QueueView Q, uint32_t seed_offset) {
     P.vols[2 * (size_t)i] = make_int4(0, 0, 0, 0);
     P.vols[2 * (size_t)i + 1] = make_int4(0, 0, 0, 0);
     P.qid[i] = 0;  // initialize_all_as_new_path (new_path.cl:9-15)
+    P.req[i] = 0;
 }
 
 // Ordered compaction of new-path slots: block t owns slots [t*4096, (t+1)*4096).
@@ -595,7 +596,7 @@ __global__ void __launch_bounds__(256) k_compact_new(PathsView P, QueueView Q) {
     }
 }
 
-__global__ void __launch_bounds__(256) k_shade(SceneView sc, PathsView P, QueueView Q, RenderParams rp) {
+__global__ void __launch_bounds__(256) k_shade(PathsView P, QueueView Q, RenderParams rp) {
     uint32_t off[kNumQueues + 1];
     off[0] = 0;
 #pragma unroll
@@ -609,14 +610,22 @@ __global__ void __launch_bounds__(256) k_shade(SceneView sc, PathsView P, QueueV
         for (int j = 1; j < kNumQueues; ++j) k += (i >= off[j]) ? 1 : 0;
         const uint32_t slot = Q.items[k][i - off[k]];
         unsigned long long gpix = 0;
+        int r;
         if (k == 0) {
             gpix = base_pixel + (i - off[0]);
             if (rp.sample_limit != 0ull && gpix >= rp.sample_limit) {
                 P.qid[slot] = kQueueIdle;  // sample budget reached: the slot retires
                 continue;
             }
+            // the request whose sample range holds this global sample index
+            r = 0;
+            while (r + 1 < rp.nreq && gpix >= rp.reqs[r].sample_end) ++r;
+            P.req[slot] = (uint16_t)r;
+            gpix -= rp.reqs[r].sample_begin;
+        } else {
+            r = P.req[slot];
         }
-        shade_slot(sc, P, rp, k, slot, gpix);
+        shade_slot(rp.reqs[r], P, k, slot, gpix);
     }
 }
 
@@ -632,11 +641,14 @@ RGR_DEV void enqueue(const QueueView& Q, int q, uint32_t slot, unsigned active) 
     Q.items[q][base + rank] = slot;
 }
 
-__global__ void __launch_bounds__(128) k_trace_logic(SceneView sc, PathsView P, QueueView Q, RenderParams rp) {
+__global__ void __launch_bounds__(128) k_trace_logic(PathsView P, QueueView Q, RenderParams rp) {
     const uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x;
     const bool live = slot < P.n && P.qid[slot] != kQueueIdle;
     const unsigned active = __ballot_sync(0xffffffffu, live);
     if (!live) return;
+    const int req = P.req[slot];
+    const RequestD& rq = rp.reqs[req];
+    const SceneView& sc = rq.sc;
     float4 ro4 = P.ro[slot], rd4 = P.rd[slot];
     f3 ro = xyz(ro4), rd = xyz(rd4);
     float tmin = ro4.w;
@@ -663,7 +675,7 @@ __global__ void __launch_bounds__(128) k_trace_logic(SceneView sc, PathsView P, 
     }
     float lum = 0.2126f * T.x + 0.7152f * T.y + 0.0722f * T.z;
     float cp = 1.0f;
-    if ((long long)rp.rr_depth < (long long)logic_i) cp = fmin_(lum, 1.0f);
+    if ((long long)rq.rr_depth < (long long)logic_i) cp = fmin_(lum, 1.0f);
     float u = rng.uniform();
     if (u < cp) {
         T = T / cp;
@@ -674,7 +686,7 @@ __global__ void __launch_bounds__(128) k_trace_logic(SceneView sc, PathsView P, 
     if (evalEnv && sc.has_env) L = L + T * envmap_value(sc, rd, logic_i == 0);
     // depth limit: end after segment max_depth, adding the emission that the
     // next material stage would add (lambertian.cl:395)
-    if (rp.max_depth > 0 && !newPath && (long long)logic_i >= (long long)rp.max_depth) {
+    if (rq.max_depth > 0 && !newPath && (long long)logic_i >= (long long)rq.max_depth) {
         if (0 <= hs) {
             int2 m = __ldg(sc.materials + hs);
             f3 Le = mk(0, 0, 0);
@@ -684,9 +696,9 @@ __global__ void __launch_bounds__(128) k_trace_logic(SceneView sc, PathsView P, 
         newPath = true;
     }
     if (newPath) {
-        const float cl = rp.radiance_clamp;
+        const float cl = rq.radiance_clamp;
         if (is_finite(L.x) && is_finite(L.y) && is_finite(L.z) && L.x < cl && L.y < cl && L.z < cl) {
-            double* a = rp.accum + 4 * (size_t)__float_as_uint(T4.w);
+            double* a = rq.accum + 4 * (size_t)__float_as_uint(T4.w);
             atomicAdd(a + 0, (double)L.x);
             atomicAdd(a + 1, (double)L.y);
             atomicAdd(a + 2, (double)L.z);
@@ -721,6 +733,20 @@ __global__ void __launch_bounds__(128) k_trace_logic(SceneView sc, PathsView P, 
         int leader = __ffs(active) - 1;
         if (lane == leader) atomicAdd(rp.rays, (unsigned long long)__popc(active));
         if (err) atomicOr(rp.err, err);
+        // finished paths per request; the last one of a request stamps its completion time
+        const unsigned donemask = __ballot_sync(active, newPath);
+        if (newPath && rq.done != nullptr) {
+            unsigned peers = __match_any_sync(donemask, req);
+            if (lane == __ffs(peers) - 1) {
+                const unsigned long long n = __popc(peers);
+                const unsigned long long old = atomicAdd(rq.done, n);
+                if (old + n == rq.sample_end - rq.sample_begin) {
+                    unsigned long long t;
+                    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+                    *rq.done_ns = t;
+                }
+            }
+        }
     }
 }
 
@@ -766,6 +792,29 @@ __global__ void k_sum_counts(const double* accum, uint32_t npix, unsigned long l
     if ((threadIdx.x & 31) == 0) atomicAdd(out, s);
 }
 
+// merge_intermediate (accumlation.cl:27-49): count-weighted merge of two RGB16
+// intermediates in FP32, result stored as half into a
+__global__ void k_merge_intermediate(ushort4* a, const ushort4* b, uint32_t n) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    ushort4 va = a[i], vb = b[i];
+    const unsigned short sa = va.w, sb = vb.w;
+    const unsigned short sab = (unsigned short)(sa + sb);
+    if (sab == 0) {
+        a[i] = make_ushort4(0, 0, 0, 0);
+        return;
+    }
+    const float one_over_sab = 1.0f / (float)sab;
+    const unsigned short ha[3] = {va.x, va.y, va.z}, hb[3] = {vb.x, vb.y, vb.z};
+    unsigned short out[3];
+    for (int k = 0; k < 3; ++k) {
+        float m = (__half2float(__ushort_as_half(ha[k])) * (float)sa + __half2float(__ushort_as_half(hb[k])) * (float)sb) *
+                  one_over_sab;
+        out[k] = __half_as_ushort(__float2half_rn(m));
+    }
+    a[i] = make_ushort4(out[0], out[1], out[2], sab);
+}
+
 __global__ void k_accum_add(double* dst, const double* src, uint32_t n4) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n4) dst[i] += src[i];
@@ -809,14 +858,11 @@ void launch_init(const PathsView& p, const QueueView& q, uint32_t seed_offset, c
 void launch_compact_new(const PathsView& p, const QueueView& q, cudaStream_t st) {
     k_compact_new<<<q.ntiles, 256, 0, st>>>(p, q);
 }
-void launch_shade(const SceneView& sc, const PathsView& p, const QueueView& q, const RenderParams& rp, int grid,
-                  cudaStream_t st) {
-    k_shade<<<grid, 256, 0, st>>>(sc, p, q, rp);
+void launch_shade(const PathsView& p, const QueueView& q, const RenderParams& rp, int grid, cudaStream_t st) {
+    k_shade<<<grid, 256, 0, st>>>(p, q, rp);
 }
-void launch_trace_logic(const SceneView& sc, const PathsView& p, const QueueView& q, const RenderParams& rp,
-                        int block, cudaStream_t st) {
-    (void)block;
-    k_trace_logic<<<(p.n + 127) / 128, 128, 0, st>>>(sc, p, q, rp);
+void launch_trace_logic(const PathsView& p, const QueueView& q, const RenderParams& rp, cudaStream_t st) {
+    k_trace_logic<<<(p.n + 127) / 128, 128, 0, st>>>(p, q, rp);
 }
 void launch_readback(int fmt, const double* accum, uint32_t npix, void* out, cudaStream_t st) {
     k_readback<<<(npix + 255) / 256, 256, 0, st>>>(fmt, accum, npix, out);
@@ -826,6 +872,10 @@ void launch_sum_counts(const double* accum, uint32_t npix, unsigned long long* o
 }
 void launch_debug_slots(const PathsView& p, uint32_t* out, cudaStream_t st) {
     k_debug_slots<<<(p.n + 255) / 256, 256, 0, st>>>(p, out);
+}
+void launch_merge_intermediate(void* a, const void* b, uint32_t n, cudaStream_t st) {
+    k_merge_intermediate<<<(n + 255) / 256, 256, 0, st>>>(reinterpret_cast<ushort4*>(a),
+                                                          reinterpret_cast<const ushort4*>(b), n);
 }
 void launch_accum_add(double* dst, const double* src, uint32_t npix, cudaStream_t st) {
     uint32_t n4 = npix * 4;

@@ -29,6 +29,7 @@ struct PathsView {
     uint4* rng;
     int4* vols;
     uint8_t* qid;    // queue of the next step, kQueueIdle when done
+    uint16_t* req;   // request of the path in the slot
     uint32_t n;
 };
 
@@ -47,15 +48,30 @@ struct CameraD {
     uint32_t w, h;
 };
 
-struct RenderParams {
+// One render request: its scene, camera, the reference constants of
+// rgr_render_config, its accumulation buffer and its range of the global
+// sample index.  A single render is a table of one request; a batch of
+// requests shares one path pool, each slot carrying its request id.
+struct RequestD {
+    SceneView sc;
     CameraD cam;
     float dof;
     int32_t rr_depth;
     float radiance_clamp;
     float env_p;
     int32_t max_depth;
-    unsigned long long sample_limit;  // 0 = none
-    double* accum;                    // 4 doubles per pixel: r, g, b, count
+    int32_t pad;
+    double* accum;                     // 4 doubles per pixel: r, g, b, count
+    unsigned long long sample_begin;   // global sample indices [begin, end) are this request's
+    unsigned long long sample_end;     // ~0: progressive, no end
+    unsigned long long* done;          // paths of this request that finished (kept or discarded)
+    unsigned long long* done_ns;       // %globaltimer when the last one finished
+};
+
+struct RenderParams {
+    const RequestD* reqs;             // device table, nreq entries, sample ranges ascending
+    int32_t nreq;
+    unsigned long long sample_limit;  // end of the last range; 0 = progressive
     uint32_t* err;
     unsigned long long* rays;         // extension rays cast
 };
@@ -63,14 +79,13 @@ struct RenderParams {
 // launchers (wavefront.cu)
 void launch_init(const PathsView& p, const QueueView& q, uint32_t seed_offset, cudaStream_t st);
 void launch_compact_new(const PathsView& p, const QueueView& q, cudaStream_t st);
-void launch_shade(const SceneView& sc, const PathsView& p, const QueueView& q, const RenderParams& rp, int grid,
-                  cudaStream_t st);
-void launch_trace_logic(const SceneView& sc, const PathsView& p, const QueueView& q, const RenderParams& rp,
-                        int block, cudaStream_t st);
+void launch_shade(const PathsView& p, const QueueView& q, const RenderParams& rp, int grid, cudaStream_t st);
+void launch_trace_logic(const PathsView& p, const QueueView& q, const RenderParams& rp, cudaStream_t st);
 void launch_readback(int fmt, const double* accum, uint32_t npix, void* dev_out, cudaStream_t st);
 void launch_sum_counts(const double* accum, uint32_t npix, unsigned long long* out, cudaStream_t st);
 void launch_debug_slots(const PathsView& p, uint32_t* out, cudaStream_t st);
 void launch_accum_add(double* dst, const double* src, uint32_t npix, cudaStream_t st);
+void launch_merge_intermediate(void* a, const void* b, uint32_t n, cudaStream_t st);
 // trace.cu
 void launch_trace_rays(const SceneView& sc, const float* ox, const float* oy, const float* oz, const float* dx,
                        const float* dy, const float* dz, const float* tmax, uint64_t n, int32_t* prim, float* t,
