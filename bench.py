@@ -163,6 +163,47 @@ def render_bench(dev_index: int, which: str, repeats: int = 2) -> dict:
             "config": f"{camd['w']}x{camd['h']}, {spp} spp, max depth {depth}, {mesh.ntris} triangles"}
 
 
+def batch_bench(dev_index: int, n: int = 32) -> dict:
+    """Batched uneven requests: n requests (square side log-uniform 64..1024,
+    spp log-uniform 1..256, 1k..2M triangles, full-render material mix and
+    envmap, half with a volume box) rendered to completion in one shared path
+    pool, shortest request first, bounce loop replayed from a CUDA graph;
+    pool size, graph length and shade grid from the autotuner."""
+    import numpy as np
+    import raccoongpurender_gb300 as rg
+    from raccoongpurender_gb300 import autotune, scenes
+    reqs = scenes.batch_requests(n)
+    env = scenes.sky_envmap()
+    built = []
+    t0 = time.time()
+    for r in reqs:
+        sm = rg.SceneManager()
+        sm.addMesh(r["mesh"])
+        sm.setEnvmap(env)
+        sm.buildBVH(max_leaf_size=4)
+        c = r["camera"]
+        cam = rg.camera_look_at(c["eye"], c["target"], c["up"], c["vfov"], c["w"], c["h"])
+        built.append((sm, cam, rg.render_config(spp=r["spp"], max_depth=r["max_depth"])))
+    setup_s = time.time() - t0
+    tuned = autotune.tune_batch(built, device=dev_index, log=lambda *_: None)
+    b = rg.Batch(dev_index, tuned["path_count"])
+    b.set_render_tuning(tuned["shade_blocks"], tuned["graph_steps"])
+    ids = [b.add(sm, cam, cfg) for sm, cam, cfg in built]
+    b.run(order=rg.ORDER_SHORTEST_FIRST, steps_per_launch=tuned["graph_steps"], max_steps=200)  # warm
+    t0 = time.perf_counter()
+    steps = b.run(order=rg.ORDER_SHORTEST_FIRST, steps_per_launch=tuned["graph_steps"])
+    dt = time.perf_counter() - t0
+    lat = np.array([b.request_stats(i).complete_ms for i in ids])
+    samples = sum(b.request_stats(i).samples for i in ids)
+    st = b.stats()
+    return {"requests": n, "samples": int(samples), "ms": round(dt * 1e3, 1), "steps": steps,
+            "mpaths_s": round(samples / dt / 1e6, 1), "mrays_s": round(st.rays_traced / dt / 1e6, 1),
+            "latency_ms": {"p50": round(float(np.percentile(lat, 50)), 2),
+                           "p99": round(float(np.percentile(lat, 99)), 2), "max": round(float(lat.max()), 2)},
+            "triangles": int(sum(r["mesh"].ntris for r in reqs)), "autotuned": tuned,
+            "setup_s": round(setup_s, 1)}
+
+
 def cpu_baseline(mesh, sm, coherent, incoherent, sample: int = 1048576) -> dict:
     """The oracle traversal (kernels/extension_ray_cast_stackless.cl restated)
     on all host threads over a bounded sample: the first `sample` rays of each
@@ -344,7 +385,8 @@ def main() -> None:
     render = None
     if not args.no_render:
         render = {"cornell_256_4spp": render_bench(local, "cornell"),
-                  "mixed_1080p_64spp": render_bench(local, "mixed")}
+                  "mixed_1080p_64spp": render_bench(local, "mixed"),
+                  "batch_32_requests": batch_bench(local)}
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cpu = cpu_baseline(mesh, sm, coherent, incoherent)

@@ -228,6 +228,11 @@ int rgr_trace_closest_counts_device(rgr_context* c, const rgr_ray_soa* rays, uin
 int rgr_render_noalloc(rgr_context* c, const rgr_camera* cam, const rgr_render_config* cfg, uint32_t path_count,
                        int32_t steps, double* accum_out, void* stream);
 
+/* Launch shape of the bounce loop: resident 256-thread shade blocks per SM
+   (1..64) and bounces per replayed CUDA graph (1..256).  Chosen by the
+   autotuner (raccoongpurender_gb300/autotune.py). */
+int rgr_set_render_tuning(rgr_context* c, int32_t shade_blocks_per_sm, int32_t graph_steps);
+
 /* Launch shape of the closest-hit kernel: refill a warp with new rays when at
    least `refill` of its 32 lanes are idle (1..32); `blocks_per_sm` resident
    256-thread blocks per SM (0 = as many as fit).  Chosen by the autotuner. */

@@ -121,39 +121,32 @@ def P(a: np.ndarray | None) -> int | None:
     return None if a is None else a.ctypes.data
 
 
-def reference_materials(mats: list[dict]):
+def reference_materials(mats):
     """MaterialStorage layout (scene_manager.hpp:106-172): per-primitive (type,
-    index) and the per-type arrays in the reference structs."""
-    n = len(mats)
+    index) and the per-type arrays in the reference structs.  `mats` is the
+    per-primitive material array of the scene (MATERIAL_DTYPE)."""
+    from raccoongpurender_gb300 import materials as M
+    a = M.as_array(mats)
+    n = a.shape[0]
     ref = np.zeros((max(n, 1), 2), np.int32)
-    lam, ward, vol = [], [], []
-    cnt = {1: 0, 2: 0, 3: 0, 4: 0, 5: 0}
-    for i, m in enumerate(mats):
-        t = m["type"]
-        ref[i] = (t, cnt[t])
-        cnt[t] += 1
-        if t == 1:
-            rec = np.zeros(12, np.float32)
-            rec[0:3] = m.get("le", (0, 0, 0))
-            rec[4:7] = m.get("r", (1, 1, 1))
-            lam.append(rec)
-        elif t == 4:
-            rec = np.zeros(16, np.float32)
-            rec[0] = m.get("alpha", 0.1)
-            rec[4:7] = m.get("r", (1, 1, 1))
-            rec[8:11] = m.get("edgetint", (1, 1, 1))
-            rec[12] = m.get("falloff", 0.5)
-            ward.append(rec)
-        elif t == 5:
-            rec = np.zeros(8, np.float32)
-            rec[0] = m.get("c", 1.0)
-            rec[4:7] = m.get("r", (1, 1, 1))
-            vol.append(rec)
-
-    def stack(lst, width):
-        return np.stack(lst).astype(np.float32) if lst else np.zeros((1, width), np.float32)
-
-    return ref, stack(lam, 12), stack(ward, 16), stack(vol, 8)
+    t = a["type"].astype(np.int32)
+    ref[:n, 0] = t
+    for k in (1, 2, 3, 4, 5):
+        sel = t == k
+        ref[:n, 1][sel] = np.arange(sel.sum(), dtype=np.int32)
+    la, wa, va = a[t == 1], a[t == 4], a[t == 5]
+    lam = np.zeros((max(len(la), 1), 12), np.float32)
+    lam[:len(la), 0:3] = la["le"]
+    lam[:len(la), 4:7] = la["r"]
+    ward = np.zeros((max(len(wa), 1), 16), np.float32)
+    ward[:len(wa), 0] = wa["alpha"]
+    ward[:len(wa), 4:7] = wa["r"]
+    ward[:len(wa), 8:11] = wa["edgetint"]
+    ward[:len(wa), 12] = wa["falloff"]
+    vol = np.zeros((max(len(va), 1), 8), np.float32)
+    vol[:len(va), 0] = va["c"]
+    vol[:len(va), 4:7] = va["r"]
+    return ref, lam, ward, vol
 
 
 class OracleScene:

@@ -125,6 +125,7 @@ _SIGS = {
     "rgr_trace_closest_counts_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p, C.c_void_p,
                                                   C.c_void_p, C.c_void_p, C.c_void_p]),
     "rgr_set_trace_tuning": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32]),
+    "rgr_set_render_tuning": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32]),
     "rgr_batch_create": (C.c_int, [C.c_void_p, C.c_int32, C.c_uint32]),
     "rgr_batch_destroy": (None, [C.c_void_p]),
     "rgr_batch_add": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
@@ -169,7 +170,9 @@ def _ptr(a: np.ndarray) -> int:
     return a.ctypes.data
 
 
-def _materials_to_c(mats) -> C.Array:
+def _materials_to_c(mats):
+    if isinstance(mats, np.ndarray):
+        return materials.as_array(mats)
     arr = (rgr_material * max(1, len(mats)))()
     for i, m in enumerate(mats):
         x = arr[i]
@@ -194,7 +197,7 @@ class SceneManager:
         self._lib = load_library()
         self._h = C.c_void_p()
         _check(self._lib.rgr_scene_create(C.byref(self._h)), "rgr_scene_create")
-        self.materials: list[dict] = []     # per primitive, triangles then spheres
+        self.materials = materials.as_array([])  # per primitive (MATERIAL_DTYPE), triangles then spheres
         self.num_triangles = 0
         self.envmap = None
 
@@ -215,9 +218,10 @@ class SceneManager:
         if len(materials) != I.shape[0]:
             raise ValueError("one material per triangle")
         cm = _materials_to_c(materials)
-        _check(self._lib.rgr_scene_add_mesh(self._h, _ptr(P), P.shape[0], _ptr(I), I.shape[0], C.addressof(cm)),
+        mp = _ptr(cm) if isinstance(cm, np.ndarray) else C.addressof(cm)
+        _check(self._lib.rgr_scene_add_mesh(self._h, _ptr(P), P.shape[0], _ptr(I), I.shape[0], mp),
                "rgr_scene_add_mesh")
-        self.materials.extend(materials)
+        self._append_materials(materials)
         self.num_triangles += I.shape[0]
 
     def addMesh(self, mesh) -> None:
@@ -227,9 +231,13 @@ class SceneManager:
         """SceneManager::addPointPrimitive (scene_manager.hpp:372-431)."""
         S = np.ascontiguousarray(xyzr, dtype=np.float32).reshape(-1, 4)
         cm = _materials_to_c(materials)
-        _check(self._lib.rgr_scene_add_spheres(self._h, _ptr(S), S.shape[0], C.addressof(cm)),
-               "rgr_scene_add_spheres")
-        self.materials.extend(materials)
+        mp = _ptr(cm) if isinstance(cm, np.ndarray) else C.addressof(cm)
+        _check(self._lib.rgr_scene_add_spheres(self._h, _ptr(S), S.shape[0], mp), "rgr_scene_add_spheres")
+        self._append_materials(materials)
+
+    def _append_materials(self, mats) -> None:
+        arr = materials.as_array(mats)
+        self.materials = arr if len(self.materials) == 0 else np.concatenate([materials.as_array(self.materials), arr])
 
     def setEnvmap(self, rgba, clamp_max: float = 3.4028234663852886e38, scale: float = 1.0) -> None:
         """The ImageEnvmap point of SceneManager::addPoint (scene_manager.hpp:432-497)."""
@@ -417,6 +425,9 @@ class WavefrontLane:
         _check(self._lib.rgr_trace_closest(self._h, C.byref(r), n, _ptr(prim), _ptr(t)), "rgr_trace_closest")
         return prim, t
 
+    def set_render_tuning(self, shade_blocks_per_sm: int = 8, graph_steps: int = 1) -> None:
+        _check(self._lib.rgr_set_render_tuning(self._h, shade_blocks_per_sm, graph_steps), "rgr_set_render_tuning")
+
     def set_trace_tuning(self, refill: int = 16, blocks_per_sm: int = 0) -> None:
         _check(self._lib.rgr_set_trace_tuning(self._h, refill, blocks_per_sm), "rgr_set_trace_tuning")
 
@@ -496,6 +507,10 @@ class Batch:
         out = np.zeros((cam.image_h, cam.image_w, 4), np.uint8)
         _check(self._lib.rgr_batch_readback(self._h, rid, RGR_FMT_RGBA8, _ptr(out), out.nbytes), "rgr_batch_readback")
         return out
+
+    def set_render_tuning(self, shade_blocks_per_sm: int = 8, graph_steps: int = 8) -> None:
+        _check(self._lib.rgr_set_render_tuning(self._lib.rgr_batch_context(self._h), shade_blocks_per_sm,
+                                               graph_steps), "rgr_set_render_tuning")
 
     def request_stats(self, rid: int) -> rgr_request_stats:
         st = rgr_request_stats()

@@ -1,0 +1,106 @@
+"""Project autotuner: picks the launch shape of the renderer by timing it.
+
+Knobs (all results are bit-identical across knob values; only speed changes):
+  * path_count     — resident paths in the pool (queue capacities follow it);
+  * graph_steps    — bounces per replayed CUDA graph;
+  * shade_blocks   — resident 256-thread blocks per SM of the shade kernel;
+  * trace_refill / trace_blocks — closest-hit kernel launch shape.
+Coordinate descent from a default point: each knob in turn is swept over its
+candidates with the others fixed, keeping the fastest.  Each trial runs a
+proxy of the real workload (the same scenes and cameras with the samples per
+pixel capped) and is timed on the device.  Results are cached per GPU model
+and workload signature in a JSON file (default: next to this module,
+_tuned.json, git-ignored).
+"""
+from __future__ import annotations
+
+import hashlib
+import json
+import os
+import time
+from pathlib import Path
+
+DEFAULTS = dict(path_count=1 << 22, graph_steps=8, shade_blocks=8)
+CANDIDATES = dict(path_count=[1 << 20, 1 << 21, 1 << 22], graph_steps=[4, 8, 16], shade_blocks=[4, 8, 16])
+
+
+def _gpu_name(device: int) -> str:
+    try:
+        import torch
+        return torch.cuda.get_device_name(device)
+    except Exception:  # noqa: BLE001
+        return "unknown-gpu"
+
+
+class Autotuner:
+    def __init__(self, device: int = 0, cache_path: str | None = None, log=print):
+        self.device = device
+        self.cache_path = Path(cache_path) if cache_path else Path(__file__).resolve().parent / "_tuned.json"
+        self.log = log
+        self.trials = []
+
+    def _load(self) -> dict:
+        if self.cache_path.exists():
+            try:
+                return json.loads(self.cache_path.read_text())
+            except ValueError:
+                return {}
+        return {}
+
+    def _store(self, key: str, value: dict) -> None:
+        d = self._load()
+        d[key] = value
+        tmp = self.cache_path.with_suffix(".tmp")
+        tmp.write_text(json.dumps(d, indent=1, sort_keys=True))
+        os.replace(tmp, self.cache_path)
+
+    def tune(self, signature: str, run_trial, use_cache: bool = True) -> dict:
+        """run_trial(params) -> seconds.  Returns the best params."""
+        key = hashlib.sha1((_gpu_name(self.device) + "|" + signature).encode()).hexdigest()[:16]
+        if use_cache:
+            cached = self._load().get(key)
+            if cached:
+                return dict(cached["params"])
+        best = dict(DEFAULTS)
+        best_t = self._time(run_trial, best)
+        for knob, values in CANDIDATES.items():
+            for v in values:
+                if v == best[knob]:
+                    continue
+                p = dict(best)
+                p[knob] = v
+                t = self._time(run_trial, p)
+                if t < best_t:
+                    best, best_t = p, t
+        self._store(key, dict(params=best, seconds=best_t, signature=signature, gpu=_gpu_name(self.device),
+                              trials=self.trials, when=time.strftime("%Y-%m-%dT%H:%M:%SZ", time.gmtime())))
+        return best
+
+    def _time(self, run_trial, params: dict) -> float:
+        t = run_trial(params)
+        self.trials.append(dict(params=params, seconds=round(t, 6)))
+        self.log(f"autotune {params} -> {t * 1e3:.2f} ms")
+        return t
+
+
+def tune_batch(scenes_and_requests, device: int = 0, spp_cap: int = 4, use_cache: bool = True, log=print) -> dict:
+    """Tune the batched renderer on a proxy of `scenes_and_requests`, a list of
+    (SceneManager, rgr_camera, rgr_render_config)."""
+    import raccoongpurender_gb300 as rg
+
+    sig = "batch|" + "|".join(f"{c.image_w}x{c.image_h}:{f.spp}:{s.info().num_triangles}"
+                              for s, c, f in scenes_and_requests)
+
+    def trial(p):
+        b = rg.Batch(device, p["path_count"])
+        b.set_render_tuning(p["shade_blocks"], p["graph_steps"])
+        for s, c, f in scenes_and_requests:
+            g = rg.render_config(dof=f.dof, rr_depth=f.rr_depth, radiance_clamp=f.radiance_clamp,
+                                 env_select_prob=f.env_select_prob, max_depth=f.max_depth,
+                                 seed_offset=f.seed_offset, spp=min(int(f.spp), spp_cap))
+            b.add(s, c, g)
+        t0 = time.perf_counter()
+        b.run(order=rg.ORDER_SHORTEST_FIRST, steps_per_launch=p["graph_steps"])
+        return time.perf_counter() - t0
+
+    return Autotuner(device, log=log).tune(sig, trial, use_cache=use_cache)

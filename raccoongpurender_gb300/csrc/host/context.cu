@@ -208,9 +208,11 @@ struct rgr_context {
     uint64_t steps = 0;
     uint32_t npix = 0;
     int shade_grid = 0;
+    int shade_blocks_per_sm = 8;
     // CUDA graph of `graph_steps` bounces
     bool graph_mode = true;
     int graph_steps = 1;
+    int graph_steps_default = 1;
     cudaGraphExec_t graph_exec = nullptr;
     // ray-cast service buffers
     DevBuf trays[7], tprim, tt, tread, tcounter;
@@ -280,7 +282,8 @@ struct rgr_context {
         launch_init(pv, qv, seed_offset, st);
         RGR_CUDA(cudaGetLastError());
         RGR_CUDA(cudaStreamSynchronize(st));  // host_reqs may be a temporary
-        shade_grid = num_sms * 8;
+        shade_grid = num_sms * shade_blocks_per_sm;
+        graph_steps = graph_steps_default;
         steps = 0;
         begun = true;
         drop_graph();
@@ -553,6 +556,17 @@ int rgr_intermediate_merge_device(void* a, const void* b, uint64_t npix, void* s
     return RGR_OK;
 }
 
+int rgr_set_render_tuning(rgr_context* c, int32_t shade_blocks_per_sm, int32_t graph_steps) {
+    if (!c || shade_blocks_per_sm < 1 || shade_blocks_per_sm > 64 || graph_steps < 1 || graph_steps > 256)
+        return RGR_E_INVALID;
+    c->shade_blocks_per_sm = shade_blocks_per_sm;
+    c->shade_grid = c->num_sms * shade_blocks_per_sm;
+    c->graph_steps_default = graph_steps;
+    c->graph_steps = graph_steps;
+    c->drop_graph();
+    return RGR_OK;
+}
+
 int rgr_set_trace_tuning(rgr_context* c, int32_t refill, int32_t blocks_per_sm) {
     if (!c || refill < 1 || refill > 32 || blocks_per_sm < 0) return RGR_E_INVALID;
     int maxb = std::max(1, trace_rays_max_blocks_per_sm());
@@ -768,7 +782,7 @@ int rgr_batch_run(rgr_batch* b, int32_t order_policy, int32_t steps_per_launch, 
         all = true;
         for (int k = 0; k < n; ++k) all = all && done[2 * k] == table[k].sample_end - table[k].sample_begin;
     }
-    c->graph_steps = 1;
+    c->graph_steps = c->graph_steps_default;
     c->drop_graph();
     unsigned long long t0 = 0;
     RGR_CUDA(cudaMemcpy(&t0, b->stamp.p, 8, cudaMemcpyDeviceToHost));

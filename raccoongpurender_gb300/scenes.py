@@ -327,26 +327,88 @@ def mixed_scene(level: int = 8, seed: int = 3, volume: bool = True, env: bool = 
     P = [sph.points, ground_P]
     I = [sph.indices, ground_I + sph.points.shape[0]]
     ntri = sph.ntris + 2
-    u = rng.random(ntri)
-    alb = 0.1 + 0.8 * rng.random((ntri, 3))
-    alpha = 0.05 + 0.45 * rng.random(ntri)
-    mats = []
-    for i in range(ntri):
-        if u[i] < 0.5:
-            mats.append(M.lambertian(r=tuple(alb[i])))
-        elif u[i] < 0.85:
-            mats.append(M.ward(alpha=float(alpha[i]), reflectance=(0.04, 0.04, 0.04), edgetint=(0.04, 0.04, 0.04)))
-        else:
-            mats.append(M.dielectric())
+    mats = M.random_mix(ntri, rng)
     if volume:
         bp, bi = _box([1.0, -1.2, 0.2], [2.2, 0.0, 1.4])
         bi = orient(bp, bi, bp.mean(0), outward=True)
         base = sum(p.shape[0] for p in P)
         P.append(bp)
         I.append(bi + base)
-        vol = M.homogeneous_volume(c=0.55, r=(0.5 / 0.55,) * 3)
-        mats += [vol] * bi.shape[0]
+        vol = M.as_array([M.homogeneous_volume(c=0.55, r=(0.5 / 0.55,) * 3)] * bi.shape[0])
+        mats = np.concatenate([mats, vol])
     mesh = Mesh(np.concatenate(P).astype(F32), np.concatenate(I).astype(np.uint32), mats)
     envmap = sky_envmap() if env else None
     camera = dict(eye=(0.0, 0.6, 4.6), target=(0.2, -0.25, 0.0), up=(0.0, 1.0, 0.0), vfov=38.0, w=1920, h=1080)
     return mesh, envmap, camera
+
+
+# ------------------------------------------------------------------ batched requests
+_ICO = {}
+
+
+def _ico(level: int) -> Mesh:
+    if level not in _ICO:
+        _ICO[level] = displaced_icosphere(level, seed=7)
+    return _ICO[level]
+
+
+def _loguniform(rng, lo: float, hi: float) -> float:
+    return float(np.exp(rng.uniform(np.log(lo), np.log(hi))))
+
+
+def request_scene(target_tris: int, rng, volume: bool) -> tuple:
+    """A scene of about `target_tris` triangles: displaced icospheres of the
+    levels that sum to the target (each level L has 20 * 4^L triangles),
+    scattered above a ground quad, with the full-render material mix and,
+    optionally, a homogeneous-volume box.  Returns (mesh, camera dict)."""
+    P, I = [], []
+    remaining = max(int(target_tris), 1280)
+    base = 0
+    centres = []
+    while remaining >= 1280 or not P:
+        level = int(min(8, max(3, np.floor(np.log(max(remaining, 1280) / 20.0) / np.log(4.0)))))
+        m = _ico(level)
+        r = 0.3 + 0.7 * rng.random()
+        c = np.array([rng.uniform(-2.5, 2.5), r - 1.2, rng.uniform(-2.5, 2.5)])
+        centres.append(c)
+        P.append((m.points * r + c).astype(F32))
+        I.append(m.indices + base)
+        base += m.points.shape[0]
+        remaining -= m.ntris
+    gp = np.array([[-8, -1.2, -8], [8, -1.2, -8], [8, -1.2, 8], [-8, -1.2, 8]], dtype=F32)
+    P.append(gp)
+    I.append(orient(gp, np.array([[0, 1, 2], [0, 2, 3]], np.uint32), np.array([0, -5, 0], F32), True) + base)
+    base += 4
+    ntri = int(sum(x.shape[0] for x in I))
+    mats = M.random_mix(ntri, rng)
+    if volume:
+        lo = np.array([rng.uniform(-2, 1), -1.2, rng.uniform(-2, 1)])
+        bp, bi = _box(lo, lo + np.array([1.0, 1.2, 1.0]))
+        bi = orient(bp, bi, bp.mean(0), outward=True)
+        P.append(bp)
+        I.append(bi + base)
+        mats = np.concatenate([mats, M.as_array([M.homogeneous_volume(c=0.55, r=(0.5 / 0.55,) * 3)] * 12)])
+    mesh = Mesh(np.concatenate(P).astype(F32), np.concatenate(I).astype(np.uint32), mats)
+    look = np.mean(centres, axis=0)
+    ang = rng.uniform(0, 2 * np.pi)
+    eye = look + np.array([6.0 * np.sin(ang), 2.5, 6.0 * np.cos(ang)])
+    cam = dict(eye=tuple(eye), target=tuple(look), up=(0.0, 1.0, 0.0), vfov=45.0)
+    return mesh, cam
+
+
+def batch_requests(n: int = 32, seed: int = 21, max_tris: int = 2_000_000):
+    """The batched-requests workload: `n` requests with resolution (square
+    side) log-uniform in 64..1024, spp log-uniform in 1..256, triangles
+    log-uniform in 1k..max_tris, the full-render material mix and envmap,
+    half of them with a volume box.  Returns a list of dicts."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(n):
+        side = int(round(_loguniform(rng, 64, 1024)))
+        spp = int(round(_loguniform(rng, 1, 256)))
+        tris = int(round(_loguniform(rng, 1000, max_tris)))
+        volume = (i % 2) == 1
+        mesh, cam = request_scene(tris, rng, volume)
+        cam.update(w=side, h=side)
+        out.append(dict(mesh=mesh, camera=cam, spp=spp, max_depth=8, volume=volume))
+    return out
