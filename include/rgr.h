@@ -121,7 +121,21 @@ typedef struct rgr_render_config {
     uint32_t seed_offset;   /* random_initialize seed offset (lane_index * pool, :544-548) */
     uint64_t spp;           /* 0 = progressive round robin forever (reference); else stop
                                generating paths after W*H*spp samples */
+    uint32_t flags;         /* RGR_RENDER_* below; 0 = the reference's behaviour */
+    uint32_t reserved;
 } rgr_render_config;
+
+/* Evaluate the 6-axis envmap pdf of a BSDF-sampled direction with the normal
+   flipped toward the viewer, as the envmap sampler does.  The reference uses
+   the raw normal there (envmap_sampling.cl:263-265 vs :195-198), so back-face
+   hits are weighted with a pdf that is not the one they were sampled from.
+   Guided renders always apply it; plain renders do when this flag is set. */
+#define RGR_RENDER_FIX_BACKSIDE_ENV_PDF 1u
+/* Sample the Lambertian BSDF around the normal flipped toward the viewer.  The
+   reference samples around the raw normal (lambertian.cl:49-68) but evaluates
+   with the flipped one (:98-102), so at a back-face hit no BSDF sample carries
+   light.  Guided renders always apply it; plain renders do when this flag is set. */
+#define RGR_RENDER_TWO_SIDED_LAMBERTIAN 2u
 
 typedef struct rgr_stats {
     uint64_t steps;             /* bounces of the whole pool run since render_begin */
@@ -237,6 +251,72 @@ int rgr_set_render_tuning(rgr_context* c, int32_t shade_blocks_per_sm, int32_t g
    least `refill` of its 32 lanes are idle (1..32); `blocks_per_sm` resident
    256-thread blocks per SM (0 = as many as fit).  Chosen by the autotuner. */
 int rgr_set_trace_tuning(rgr_context* c, int32_t refill, int32_t blocks_per_sm);
+
+/* ---- learned path guiding (no counterpart in the reference) --------------
+   A small MLP maps a shading vertex (frequency-encoded position, normal and
+   outgoing direction: 36 inputs) through 4 hidden layers of 64 (ReLU) to an
+   8-lobe von Mises-Fisher mixture over the incident direction (40 outputs).
+   It runs in BF16 on the tensor cores with FP32 accumulation.  Attached to a
+   context, it becomes a third strategy of the one-sample MIS at Lambertian,
+   Ward and (optionally) in-volume vertices, next to BSDF and envmap
+   sampling: p = s_bsdf p_bsdf + s_guide p_guide + s_env p_env, so the
+   estimator stays unbiased for any network state.  While rendering, each
+   path records its first guided vertices; when it ends, the radiance that
+   arrived along each sampled direction becomes a training sample, and after
+   every bounce one Adam step on up to batch_samples samples (loss: the KL
+   divergence to f cos L_i, estimated as -w log q) runs in the same CUDA graph. */
+typedef struct rgr_guide rgr_guide;
+typedef struct rgr_guide_config {
+    float learning_rate;     /* Adam (1e-3) */
+    float beta1, beta2;      /* Adam (0.9, 0.999) */
+    float epsilon;           /* Adam (1e-8) */
+    uint32_t batch_samples;  /* training samples per iteration (2^18) */
+    float guide_fraction;    /* share of the non-envmap selection probability given to the guide (0.5) */
+    int32_t train;           /* train online while rendering (1), or keep the weights fixed (0) */
+    int32_t guide_volumes;   /* guide in-volume scattering too (1) */
+    uint32_t train_interval; /* bounces per training iteration (1): samples of all of them feed it */
+    uint32_t reserved;
+    uint64_t seed;           /* weight initialisation (1) */
+} rgr_guide_config;
+typedef struct rgr_guide_stats {
+    uint64_t iterations;     /* Adam steps taken */
+    float last_loss;         /* loss of the last iteration (sum over its samples of -w log q, w normalised) */
+    float accept;            /* probability with which a finished record is offered as a sample */
+} rgr_guide_stats;
+#define RGR_GUIDE_LAYERS 5
+#define RGR_GUIDE_WIDTH 64   /* every layer is stored as a zero-padded 64 x 64 W[in][out] */
+
+void rgr_guide_config_default(rgr_guide_config* c);
+/* the network on `device`, weights initialised from cfg->seed (He uniform) */
+int rgr_guide_create(rgr_guide** out, int32_t device, const rgr_guide_config* cfg);
+void rgr_guide_destroy(rgr_guide* g);
+int rgr_guide_set_config(rgr_guide* g, const rgr_guide_config* cfg);
+/* position normalisation of the input encoding; by default the bounds of the
+   scene uploaded to the context it is first rendered with */
+int rgr_guide_set_bounds(rgr_guide* g, const float lo[3], const float hi[3]);
+/* FP32 weights W[l][in][out] (5*64*64 floats) and biases b[l][out] (5*64);
+   set also resets the Adam state */
+int rgr_guide_get_weights(rgr_guide* g, float* w, float* b);
+int rgr_guide_set_weights(rgr_guide* g, const float* w, const float* b);
+/* Use the guide in the context's next rgr_render_begin (NULL: plain rendering).
+   The guide must live on the context's device and outlive its renders. */
+int rgr_context_set_guide(rgr_context* c, rgr_guide* g);
+/* Raw network outputs, 40 floats per row, of rows of 16 floats whose first 9
+   are (position, normal, outgoing direction); device pointers, on `stream`. */
+int rgr_guide_infer_device(rgr_guide* g, const float* rows, uint32_t n, float* out, void* stream);
+/* One training step on n samples of 16 floats (position, normal, outgoing,
+   incident direction, weight, 3 unused), each weight multiplied by
+   weight_scale.  grads (device, may be NULL) receives the gradient of the
+   loss, weights then biases (5*64*64 + 5*64 floats); *loss (host, may be NULL)
+   the loss.  apply_adam = 0 leaves the network unchanged. Synchronous. */
+int rgr_guide_train_device(rgr_guide* g, const float* samples, uint32_t n, float weight_scale, int32_t apply_adam,
+                           float* grads, float* loss, void* stream);
+int rgr_guide_stats_get(rgr_guide* g, rgr_guide_stats* st);
+/* losses of the last min(max, iterations) iterations, oldest first; *count receives how many */
+int rgr_guide_loss_history(rgr_guide* g, float* out, uint32_t max, uint32_t* count);
+/* the training samples of the last iteration of a guided render (16 floats each, as
+   rgr_guide_train_device takes them), at most max; *count receives how many */
+int rgr_guide_last_batch(rgr_guide* g, float* out, uint32_t max, uint32_t* count);
 
 /* ---- diagnostics --------------------------------------------------------- */
 const char* rgr_status_string(int status);

@@ -42,7 +42,8 @@ class orc_camera(C.Structure):
 class orc_config(C.Structure):
     _fields_ = [("dof", C.c_float), ("rr_depth", C.c_int32), ("radiance_clamp", C.c_float),
                 ("env_select_prob", C.c_float), ("max_depth", C.c_int32), ("seed_offset", C.c_uint32),
-                ("sample_limit", C.c_uint64), ("new_path_y_first", C.c_int32)]
+                ("sample_limit", C.c_uint64), ("new_path_y_first", C.c_int32), ("fix_backside_env_pdf", C.c_int32),
+                ("two_sided_lambertian", C.c_int32)]
 
 
 _lib = None
@@ -240,4 +241,6 @@ def config_from_rgr(cfg, npix: int) -> orc_config:
     o.dof, o.rr_depth, o.radiance_clamp = cfg.dof, cfg.rr_depth, cfg.radiance_clamp
     o.env_select_prob, o.max_depth, o.seed_offset = cfg.env_select_prob, cfg.max_depth, cfg.seed_offset
     o.sample_limit = cfg.spp * npix if cfg.spp else 0
+    o.fix_backside_env_pdf = 1 if (cfg.flags & 1) else 0
+    o.two_sided_lambertian = 1 if (cfg.flags & 2) else 0
     return o

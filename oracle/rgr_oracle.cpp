@@ -601,7 +601,8 @@ void step_slot(const Ctx& c, Slot& p, double* accum, bool is_new, uint64_t gpix)
     }
     // sample or eval BSDF
     if (mq == kMatLambertian) {  // lambertian.cl:34-71
-        f3 Ng = p.Ng;
+        f3 Ng = p.Ng;  // the raw Ng (lambertian.cl:49-68), or flipped toward the viewer
+        if (c.cfg->two_sided_lambertian && dot(Ng, -p.rd) < 0.0f) Ng = -Ng;
         float cosTheta;
         if (is.strategy == kStrategyBxdf) {
             float u0 = p.rng.uniform();
@@ -640,7 +641,9 @@ void step_slot(const Ctx& c, Slot& p, double* accum, bool is_new, uint64_t gpix)
     }
     // evaluate env pdf, envmap_sampling.cl:250-281
     if (envq == 3) {
-        is.pdf[kStrategyEnv] = envmap_pdf_six_axis(s, is.wi, p.Ng);
+        f3 n = p.Ng;  // the raw Ng (envmap_sampling.cl:263), or flipped like the sampler
+        if (c.cfg->fix_backside_env_pdf && dot(n, -p.rd) < 0.0f) n = -n;
+        is.pdf[kStrategyEnv] = envmap_pdf_six_axis(s, is.wi, n);
     } else if (envq == 1) {
         is.pdf[kStrategyEnv] = s->env_pdf[envmap_index(is.wi, s->env_w, s->env_h)];
     }

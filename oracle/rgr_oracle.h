@@ -80,6 +80,13 @@ typedef struct orc_config {
        compilers (and the CUDA path) evaluate left to right: x first (0).  GCC,
        which compiles the reference kernels here, evaluates y first (1). */
     int32_t new_path_y_first;
+    /* 1: evaluate the 6-axis envmap pdf of a BSDF-sampled direction with the
+       normal flipped toward the viewer, as the sampler does (the reference
+       uses the raw normal, envmap_sampling.cl:263 vs :195-198) */
+    int32_t fix_backside_env_pdf;
+    /* 1: sample the Lambertian BSDF around the normal flipped toward the viewer
+       (the reference samples around the raw normal, lambertian.cl:49-68) */
+    int32_t two_sided_lambertian;
 } orc_config;
 
 /* per-slot state in a canonical layout used to compare with the GPU */

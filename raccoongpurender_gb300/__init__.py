@@ -67,7 +67,22 @@ class rgr_camera(C.Structure):
 class rgr_render_config(C.Structure):
     _fields_ = [("dof", C.c_float), ("rr_depth", C.c_int32), ("radiance_clamp", C.c_float),
                 ("env_select_prob", C.c_float), ("max_depth", C.c_int32), ("seed_offset", C.c_uint32),
-                ("spp", C.c_uint64)]
+                ("spp", C.c_uint64), ("flags", C.c_uint32), ("reserved", C.c_uint32)]
+
+
+RENDER_FIX_BACKSIDE_ENV_PDF = 1  # RGR_RENDER_FIX_BACKSIDE_ENV_PDF
+RENDER_TWO_SIDED_LAMBERTIAN = 2  # RGR_RENDER_TWO_SIDED_LAMBERTIAN
+
+
+class rgr_guide_config(C.Structure):
+    _fields_ = [("learning_rate", C.c_float), ("beta1", C.c_float), ("beta2", C.c_float), ("epsilon", C.c_float),
+                ("batch_samples", C.c_uint32), ("guide_fraction", C.c_float), ("train", C.c_int32),
+                ("guide_volumes", C.c_int32), ("train_interval", C.c_uint32), ("reserved", C.c_uint32),
+                ("seed", C.c_uint64)]
+
+
+class rgr_guide_stats(C.Structure):
+    _fields_ = [("iterations", C.c_uint64), ("last_loss", C.c_float), ("accept", C.c_float)]
 
 
 class rgr_stats(C.Structure):
@@ -136,6 +151,20 @@ _SIGS = {
     "rgr_intermediate_merge_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p]),
     "rgr_render_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_int32, C.c_void_p,
                                      C.c_void_p]),
+    "rgr_guide_config_default": (None, [C.c_void_p]),
+    "rgr_guide_create": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p]),
+    "rgr_guide_destroy": (None, [C.c_void_p]),
+    "rgr_guide_set_config": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "rgr_guide_set_bounds": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "rgr_guide_get_weights": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "rgr_guide_set_weights": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "rgr_context_set_guide": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "rgr_guide_infer_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p]),
+    "rgr_guide_train_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_float, C.c_int32, C.c_void_p,
+                                         C.c_void_p, C.c_void_p]),
+    "rgr_guide_stats_get": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "rgr_guide_loss_history": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p]),
+    "rgr_guide_last_batch": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p]),
 }
 
 _lib = None
@@ -296,7 +325,7 @@ class SceneManager:
 
 def render_config(**kw) -> rgr_render_config:
     """A render config with the reference defaults, overridden by keywords
-    (dof, rr_depth, radiance_clamp, env_select_prob, max_depth, seed_offset, spp)."""
+    (dof, rr_depth, radiance_clamp, env_select_prob, max_depth, seed_offset, spp, flags)."""
     c = rgr_render_config()
     load_library().rgr_render_config_default(C.byref(c))
     for k, v in kw.items():
@@ -428,6 +457,12 @@ class WavefrontLane:
     def set_render_tuning(self, shade_blocks_per_sm: int = 8, graph_steps: int = 1) -> None:
         _check(self._lib.rgr_set_render_tuning(self._h, shade_blocks_per_sm, graph_steps), "rgr_set_render_tuning")
 
+    def set_guide(self, guide: "Guide | None") -> None:
+        """Render with the learned guide from the next initialize() on (None: plain)."""
+        self._guide = guide  # keep it alive while the context refers to it
+        _check(self._lib.rgr_context_set_guide(self._h, guide.handle if guide is not None else None),
+               "rgr_context_set_guide")
+
     def set_trace_tuning(self, refill: int = 16, blocks_per_sm: int = 0) -> None:
         _check(self._lib.rgr_set_trace_tuning(self._h, refill, blocks_per_sm), "rgr_set_trace_tuning")
 
@@ -443,6 +478,96 @@ class WavefrontLane:
         r = rgr_ray_soa(*soa_ptrs)
         _check(self._lib.rgr_trace_closest_device(self._h, C.byref(r), n, prim_ptr, t_ptr, ng_ptr or None,
                                                   stream or None), "rgr_trace_closest_device")
+
+
+class Guide:
+    """The learned path-guiding network on one GPU (rgr_guide): 36 encoded
+    inputs -> 4 x 64 ReLU -> 8 vMF lobes (40 outputs), BF16 on the tensor
+    cores, trained online by Adam while a WavefrontLane renders with it."""
+
+    LAYERS, WIDTH, INPUTS, OUTPUTS, LOBES = 5, 64, 36, 40, 8
+    N_WEIGHTS = LAYERS * WIDTH * WIDTH
+    N_PARAMS = N_WEIGHTS + LAYERS * WIDTH
+
+    def __init__(self, device: int = 0, **cfg):
+        self._lib = load_library()
+        c = rgr_guide_config()
+        self._lib.rgr_guide_config_default(C.byref(c))
+        for k, v in cfg.items():
+            setattr(c, k, v)
+        self._h = C.c_void_p()
+        _check(self._lib.rgr_guide_create(C.byref(self._h), device, C.byref(c)), "rgr_guide_create")
+        self._cfg = c
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h and h.value:
+            self._lib.rgr_guide_destroy(h)
+            self._h = C.c_void_p()
+
+    @property
+    def handle(self):
+        return self._h
+
+    @property
+    def config(self) -> rgr_guide_config:
+        return self._cfg
+
+    def set_config(self, **kw) -> None:
+        c = rgr_guide_config()
+        C.memmove(C.byref(c), C.byref(self._cfg), C.sizeof(c))
+        for k, v in kw.items():
+            setattr(c, k, v)
+        _check(self._lib.rgr_guide_set_config(self._h, C.byref(c)), "rgr_guide_set_config")
+        self._cfg = c
+
+    def set_bounds(self, lo, hi) -> None:
+        f3 = C.c_float * 3
+        _check(self._lib.rgr_guide_set_bounds(self._h, f3(*lo), f3(*hi)), "rgr_guide_set_bounds")
+
+    def weights(self) -> tuple[np.ndarray, np.ndarray]:
+        """FP32 (W[5, 64, 64] as W[l][in][out], b[5, 64])."""
+        w = np.zeros((self.LAYERS, self.WIDTH, self.WIDTH), np.float32)
+        b = np.zeros((self.LAYERS, self.WIDTH), np.float32)
+        _check(self._lib.rgr_guide_get_weights(self._h, _ptr(w), _ptr(b)), "rgr_guide_get_weights")
+        return w, b
+
+    def set_weights(self, w: np.ndarray, b: np.ndarray) -> None:
+        w = np.ascontiguousarray(w, np.float32).reshape(self.LAYERS, self.WIDTH, self.WIDTH)
+        b = np.ascontiguousarray(b, np.float32).reshape(self.LAYERS, self.WIDTH)
+        _check(self._lib.rgr_guide_set_weights(self._h, _ptr(w), _ptr(b)), "rgr_guide_set_weights")
+
+    def infer_device(self, rows_ptr: int, n: int, out_ptr: int, stream: int = 0) -> None:
+        """Raw outputs (40 floats per row) of device rows of 16 floats (x, n, wo, ...)."""
+        _check(self._lib.rgr_guide_infer_device(self._h, rows_ptr, n, out_ptr, stream or None),
+               "rgr_guide_infer_device")
+
+    def train_device(self, samples_ptr: int, n: int, weight_scale: float = 1.0, apply_adam: bool = True,
+                     grads_ptr: int = 0, stream: int = 0) -> float:
+        """One training step on n device samples of 16 floats; returns the loss."""
+        loss = C.c_float()
+        _check(self._lib.rgr_guide_train_device(self._h, samples_ptr, n, weight_scale, int(apply_adam),
+                                                grads_ptr or None, C.byref(loss), stream or None),
+               "rgr_guide_train_device")
+        return loss.value
+
+    def stats(self) -> dict:
+        st = rgr_guide_stats()
+        _check(self._lib.rgr_guide_stats_get(self._h, C.byref(st)), "rgr_guide_stats_get")
+        return dict(iterations=st.iterations, last_loss=st.last_loss, accept=st.accept)
+
+    def last_batch(self, max_count: int = 1 << 18) -> np.ndarray:
+        """The training samples (n, 16) of the last iteration of a guided render."""
+        out = np.zeros((max_count, 16), np.float32)
+        n = C.c_uint32()
+        _check(self._lib.rgr_guide_last_batch(self._h, _ptr(out), max_count, C.byref(n)), "rgr_guide_last_batch")
+        return out[:n.value].copy()
+
+    def loss_history(self, max_count: int = 4096) -> np.ndarray:
+        out = np.zeros(max_count, np.float32)
+        n = C.c_uint32()
+        _check(self._lib.rgr_guide_loss_history(self._h, _ptr(out), max_count, C.byref(n)), "rgr_guide_loss_history")
+        return out[:n.value].copy()
 
 
 def merge_intermediate_device(a_ptr: int, b_ptr: int, npix: int, stream: int = 0) -> None:

@@ -13,60 +13,11 @@
 
 #include "../kernels/wavefront.cuh"
 #include "../rgr_internal.h"
+#include "devbuf.h"
+#include "guide_host.h"
 
 using namespace rgr;
 using namespace rgr::dev;
-
-namespace {
-
-bool cuda_ok(cudaError_t e, const char* what) {
-    if (e == cudaSuccess) return true;
-    set_error(std::string(what) + ": " + cudaGetErrorString(e));
-    return false;
-}
-#define RGR_CUDA(call)                                      \
-    do {                                                    \
-        if (!cuda_ok((call), #call)) return RGR_E_CUDA;     \
-    } while (0)
-
-struct DevBuf {
-    void* p = nullptr;
-    size_t bytes = 0;
-    DevBuf() = default;
-    DevBuf(const DevBuf&) = delete;
-    DevBuf& operator=(const DevBuf&) = delete;
-    ~DevBuf() { release(); }
-    void release() {
-        if (p) cudaFree(p);
-        p = nullptr;
-        bytes = 0;
-    }
-    int alloc(size_t n) {
-        if (n <= bytes && p) return RGR_OK;
-        release();
-        size_t b = std::max<size_t>(n, 256);
-        cudaError_t e = cudaMalloc(&p, b);
-        if (e != cudaSuccess) {
-            p = nullptr;
-            set_error(std::string("cudaMalloc: ") + cudaGetErrorString(e));
-            return e == cudaErrorMemoryAllocation ? RGR_E_OOM : RGR_E_CUDA;
-        }
-        bytes = b;
-        return RGR_OK;
-    }
-    int upload(const void* src, size_t n, cudaStream_t st) {
-        int r = alloc(n);
-        if (r != RGR_OK) return r;
-        if (n) RGR_CUDA(cudaMemcpyAsync(p, src, n, cudaMemcpyHostToDevice, st));
-        return RGR_OK;
-    }
-    template <class T>
-    T* as() const {
-        return reinterpret_cast<T*>(p);
-    }
-};
-
-}  // namespace
 
 namespace {
 
@@ -182,6 +133,7 @@ RequestD request_d(const SceneView& sv, const rgr_camera& cam, const rgr_render_
     q.radiance_clamp = k.radiance_clamp;
     q.env_p = k.env_select_prob;
     q.max_depth = k.max_depth;
+    q.flags = k.flags;
     q.accum = accum;
     q.sample_begin = begin;
     q.sample_end = end;
@@ -218,6 +170,11 @@ struct rgr_context {
     DevBuf trays[7], tprim, tt, tread, tcounter;
     int trace_grid = 0;      // persistent traversal grid (SMs x resident blocks)
     int trace_refill = 24;   // refill a warp when this many lanes are idle (measured best of 1..32)
+    // learned path guiding: the attached network and this render's per-slot buffers
+    rgr_guide* guide = nullptr;
+    bool guided = false;      // the current render uses `guide`
+    DevBuf globes, grecords, gnrec;
+    float scene_bounds[6] = {0, 0, 0, 0, 0, 0};
 
     ~rgr_context() {
         if (graph_exec) cudaGraphExecDestroy(graph_exec);
@@ -284,18 +241,62 @@ struct rgr_context {
         RGR_CUDA(cudaStreamSynchronize(st));  // host_reqs may be a temporary
         shade_grid = num_sms * shade_blocks_per_sm;
         graph_steps = graph_steps_default;
+        // a replayed graph holds whole training intervals
+        const int ti = train_interval();
+        graph_steps = (graph_steps + ti - 1) / ti * ti;
         steps = 0;
         begun = true;
         drop_graph();
         return RGR_OK;
     }
-    int step_launches(cudaStream_t st) {
+    // train_now: a guided render ends a training interval with this bounce
+    int step_launches(cudaStream_t st, bool train_now = true) {
         launch_compact_new(pv, qv, st);
+        if (guided) launch_guide_infer_paths(guide->view, pv, qv, rp.gd, num_sms * 3, st);
         launch_shade(pv, qv, rp, shade_grid, st);
         RGR_CUDA(cudaMemsetAsync(qv.counts + 1, 0, sizeof(uint32_t) * (kNumQueues - 1), st));
         RGR_CUDA(cudaMemsetAsync(qv.tile_new, 0, sizeof(uint32_t) * ntiles, st));
         launch_trace_logic(pv, qv, rp, st);
         RGR_CUDA(cudaGetLastError());
+        if (guided && train_now) return guide->train_launches(st);
+        return RGR_OK;
+    }
+    // bounces per training iteration of a guided render (1 otherwise)
+    int train_interval() const { return guided ? (int)guide->cfg.train_interval : 1; }
+    // per-slot guiding buffers and the kernels' view of them, or plain rendering
+    int setup_guiding() {
+        rp.gd = GuideRenderD{};
+        guided = false;
+        if (!guide) return RGR_OK;
+        if (guide->device != device) {
+            set_error("the guide lives on another device than the context");
+            return RGR_E_INVALID;
+        }
+        const size_t n = (size_t)ntiles * kTile;
+        int r;
+        if ((r = globes.alloc(16 * kGuideLobeVecs * n)) != RGR_OK) return r;
+        if ((r = grecords.alloc(16 * 5 * kGuideRecords * n)) != RGR_OK) return r;
+        if ((r = gnrec.alloc(n)) != RGR_OK) return r;
+        RGR_CUDA(cudaMemsetAsync(gnrec.p, 0, n, stream));
+        if (!guide->bounds_set) {
+            // the scene's bounds, widened by 1 % so that hit points stay inside
+            float lo[3], hi[3];
+            for (int k = 0; k < 3; ++k) {
+                const float e = std::max(scene_bounds[3 + k] - scene_bounds[k], 1.0e-3f);
+                lo[k] = scene_bounds[k] - 0.01f * e;
+                hi[k] = scene_bounds[3 + k] + 0.01f * e;
+            }
+            if ((r = guide->set_bounds(lo, hi)) != RGR_OK) return r;
+        }
+        GuideRenderD& gd = rp.gd;
+        gd.lobes = globes.as<float4>();
+        gd.records = grecords.as<float4>();
+        gd.nrec = gnrec.as<uint8_t>();
+        gd.train = guide->train;
+        gd.guide_frac = guide->cfg.guide_fraction;
+        gd.volumes = guide->cfg.guide_volumes ? 1 : 0;
+        gd.record = guide->cfg.train ? 1 : 0;
+        guided = true;
         return RGR_OK;
     }
     // run `n` bounces: replays of a graph of graph_steps bounces, then single ones
@@ -309,7 +310,8 @@ struct rgr_context {
                         cudaGraph_t g = nullptr;
                         RGR_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
                         int r = RGR_OK;
-                        for (int i = 0; i < graph_steps && r == RGR_OK; ++i) r = step_launches(st);
+                        for (int i = 0; i < graph_steps && r == RGR_OK; ++i)
+                            r = step_launches(st, (i + 1) % train_interval() == 0);
                         cudaError_t e = cudaStreamEndCapture(st, &g);
                         if (r != RGR_OK) return r;
                         RGR_CUDA(e);
@@ -323,7 +325,7 @@ struct rgr_context {
                     continue;
                 }
             }
-            int r = step_launches(st);
+            int r = step_launches(st, (steps + 1) % (uint64_t)train_interval() == 0);
             if (r != RGR_OK) return r;
             n -= 1;
             steps += 1;
@@ -389,6 +391,7 @@ int rgr_device_upload(rgr_context* c, const rgr_scene* s) {
     RGR_CUDA(cudaSetDevice(c->device));
     int r = c->scene.upload(s, c->stream);
     if (r != RGR_OK) return r;
+    for (int k = 0; k < 6; ++k) c->scene_bounds[k] = s->bvh.bounds[k];
     c->begun = false;
     c->drop_graph();
     return RGR_OK;
@@ -416,7 +419,23 @@ int rgr_render_begin(rgr_context* c, const rgr_camera* cam, const rgr_render_con
     const unsigned long long limit = k.spp ? (unsigned long long)k.spp * c->npix : 0ull;
     RequestD q = request_d(c->scene.sv, *cam, k, c->accum.as<double>(), 0ull, limit ? limit : ~0ull,
                            c->done.as<unsigned long long>());
+    if ((r = c->setup_guiding()) != RGR_OK) return r;
+    if (c->guided) q.flags |= kFlagFixBacksideEnvPdf | kFlagTwoSidedLambertian;
     return c->start(&q, 1, limit, k.seed_offset);
+}
+
+int rgr_context_set_guide(rgr_context* c, rgr_guide* g) {
+    if (!c) return RGR_E_INVALID;
+    if (g && g->device != c->device) {
+        set_error("rgr_context_set_guide: the guide lives on another device than the context");
+        return RGR_E_INVALID;
+    }
+    c->guide = g;
+    c->begun = false;  // takes effect at the next rgr_render_begin
+    c->guided = false;
+    c->rp.gd = GuideRenderD{};
+    c->drop_graph();
+    return RGR_OK;
 }
 
 int rgr_render_step(rgr_context* c, int32_t steps) {

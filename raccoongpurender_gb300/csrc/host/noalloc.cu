@@ -160,13 +160,14 @@ extern "C" int rgr_render_noalloc(rgr_context* c, const rgr_camera* cam, const r
     rq.radiance_clamp = k.radiance_clamp;
     rq.env_p = k.env_select_prob;
     rq.max_depth = k.max_depth;
+    rq.flags = k.flags;
     rq.accum = accum_out;
     const unsigned long long limit = k.spp ? (unsigned long long)k.spp * npix : 0ull;
     rq.sample_begin = 0;
     rq.sample_end = limit ? limit : ~0ull;
     rq.done = nullptr;
     rq.done_ns = nullptr;
-    RenderParams rp;
+    RenderParams rp{};  // value-initialised: no guiding (rp.gd.lobes == nullptr)
     rp.reqs = reinterpret_cast<const RequestD*>(base + kOffRequest);
     rp.nreq = 1;
     rp.sample_limit = limit;

@@ -258,6 +258,8 @@ void rgr_render_config_default(rgr_render_config* c) {
     c->max_depth = 0;
     c->seed_offset = 0;
     c->spp = 0;
+    c->flags = 0;
+    c->reserved = 0;
 }
 
 // A pinhole camera in the reference StandardCamera form (wavefront_path_tracing.hpp:103-118):

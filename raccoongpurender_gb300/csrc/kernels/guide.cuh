@@ -1,0 +1,137 @@
+// guide.cuh — learned path guiding: the network's device view, the
+// von Mises-Fisher mixture it parameterises, and the per-render buffers that
+// connect it to the wavefront (inference per bounce, training samples
+// recorded by the tracer).
+//
+// The network maps a shading vertex (position, normal facing the outgoing
+// direction, outgoing direction) to 8 vMF lobes over the incident direction.
+// At Lambertian, Ward and in-volume vertices the guided renderer adds it as a
+// third strategy of the one-sample MIS that already combines BSDF and
+// envmap sampling:  p(wi) = s_bsdf p_bsdf + s_guide p_guide + s_env p_env,
+// so every sample stays unbiased whatever the network has learned.
+#pragma once
+#include <cuda_bf16.h>
+
+#include "wavefront.cuh"
+
+namespace rgr {
+namespace dev {
+
+constexpr int kGuideLobes = 8;
+constexpr int kGuideLayers = 5;
+constexpr int kGuideWidth = 64;
+constexpr int kGuideWeights = kGuideLayers * kGuideWidth * kGuideWidth;  // W[l][in][out], zero padded
+constexpr int kGuideBiases = kGuideLayers * kGuideWidth;
+constexpr int kGuideParams = kGuideWeights + kGuideBiases;
+constexpr int kGuideInputs = 36;   // 9 coordinates x 2 octaves x (sin, cos)
+constexpr int kGuideOutputs = 40;  // 8 lobes x (mean xyz, concentration, weight)
+constexpr float kGuideKappaMax = 5000.0f;
+constexpr float kGuideLogitBound = 5.0f;    // lobe weight logits lie in (-5, 5)
+constexpr float kGuideNormPenalty = 0.01f;  // pull of each direction output's length toward 1
+
+// position normalisation of the input encoding (scene bounds)
+struct GuideParams {
+    float lo[3];
+    float inv_ext[3];
+};
+
+// the network and its optimiser state (device pointers)
+struct GuideView {
+    float* w;              // FP32 master weights, kGuideWeights
+    float* b;              // FP32 biases, kGuideBiases
+    __nv_bfloat16* wbf;    // BF16 copy of w that the tensor cores read
+    float* gW;             // gradient accumulators (zeroed by Adam)
+    float* gb;
+    float* m;              // Adam moments, kGuideParams each (weights then biases)
+    float* v;
+    float* loss;           // sum of sample losses of the last batch
+    GuideParams params;
+};
+
+// ------------------------------------------------------------ vMF mixture
+// vMF density on the sphere, kappa / (2 pi (1 - e^{-2 kappa})) e^{kappa (c - 1)}
+__device__ __forceinline__ float vmf_pdf(float kappa, float c) {
+    return kappa / (6.283185307179586f * -expm1f(-2.0f * kappa)) * expf(kappa * (c - 1.0f));
+}
+
+// Inferred mixture of one guided vertex: lobes[i] = (mean, kappa), weights in
+// w[0..7] (normalised).
+struct GuideMixture {
+    float4 lobe[kGuideLobes];
+    float w[kGuideLobes];
+};
+__device__ __forceinline__ void load_mixture(const float4* p, GuideMixture& m) {
+#pragma unroll
+    for (int i = 0; i < kGuideLobes; ++i) m.lobe[i] = p[i];
+    const float4 a = p[8], b = p[9];
+    m.w[0] = a.x;
+    m.w[1] = a.y;
+    m.w[2] = a.z;
+    m.w[3] = a.w;
+    m.w[4] = b.x;
+    m.w[5] = b.y;
+    m.w[6] = b.z;
+    m.w[7] = b.w;
+}
+__device__ __forceinline__ float mixture_pdf(const GuideMixture& m, float dx, float dy, float dz) {
+    float p = 0.0f;
+#pragma unroll
+    for (int i = 0; i < kGuideLobes; ++i) {
+        const float c = m.lobe[i].x * dx + m.lobe[i].y * dy + m.lobe[i].z * dz;
+        p += m.w[i] * vmf_pdf(m.lobe[i].w, c);
+    }
+    return p;
+}
+// Sample the mixture with three uniforms: lobe by weight, then the vMF
+// cosine by inversion (W = 1 + log(u + (1 - u) e^{-2 kappa}) / kappa) and a
+// uniform azimuth in the lobe's frame (Frisvad / Duff branchless basis).
+__device__ __forceinline__ void mixture_sample(const GuideMixture& m, float u0, float u1, float u2, float* d) {
+    int k = kGuideLobes - 1;
+    float acc = 0.0f;
+#pragma unroll
+    for (int i = 0; i < kGuideLobes - 1; ++i) {
+        acc += m.w[i];
+        if (u0 < acc && k == kGuideLobes - 1) k = i;
+    }
+    const float4 L = m.lobe[k];
+    const float kappa = L.w;
+    float w = 1.0f + logf(u1 + (1.0f - u1) * expf(-2.0f * kappa)) / kappa;
+    w = fminf(fmaxf(w, -1.0f), 1.0f);
+    const float s = sqrtf(fmaxf(0.0f, 1.0f - w * w));
+    float sp, cp;
+    sincospif(2.0f * u2, &sp, &cp);
+    const float sign = L.z >= 0.0f ? 1.0f : -1.0f;
+    const float a = -1.0f / (sign + L.z);
+    const float bb = L.x * L.y * a;
+    const float tx = 1.0f + sign * L.x * L.x * a, ty = sign * bb, tz = -sign * L.x;
+    const float bx = bb, by = sign + L.y * L.y * a, bz = -L.y;
+    float x = w * L.x + s * (cp * tx + sp * bx);
+    float y = w * L.y + s * (cp * ty + sp * by);
+    float z = w * L.z + s * (cp * tz + sp * bz);
+    const float n = sqrtf(x * x + y * y + z * z);
+    d[0] = x / n;
+    d[1] = y / n;
+    d[2] = z / n;
+}
+
+// ------------------------------------------------------------ launchers (guide_mlp.cu)
+size_t guide_infer_smem();
+size_t guide_train_smem();
+// opt the kernels into their dynamic shared memory on the current device (cudaError_t)
+int guide_kernel_attributes();
+// raw network outputs (40 floats per row) of rows of 16 floats (x, n, wo in the first 9)
+void launch_guide_infer(const GuideView& g, const float* rows, uint32_t n, float* out, int grid, cudaStream_t st);
+// mixtures of this bounce's guided queue items (Lambertian, Ward, in-volume when enabled)
+void launch_guide_infer_paths(const GuideView& g, const PathsView& p, const QueueView& q, const GuideRenderD& gd,
+                              int grid, cudaStream_t st);
+// one training iteration over min(*count, cap) samples: gradients into gW/gb, loss
+void launch_guide_train(const GuideView& g, const float* samples, const uint32_t* count, uint32_t cap,
+                        const float* wsum, float weight_scale, int grid, cudaStream_t st);
+// Adam on the accumulated gradients when *count > 0; iteration number from *iter + 1
+void launch_guide_adam(const GuideView& g, const uint32_t* count, const uint32_t* iter, float lr, float beta1,
+                       float beta2, float eps, cudaStream_t st);
+// after an iteration: advance *iter, log the loss, retune the acceptance, reset counters
+void launch_guide_finish(const GuideView& g, const GuideTrainD& t, cudaStream_t st);
+
+}  // namespace dev
+}  // namespace rgr

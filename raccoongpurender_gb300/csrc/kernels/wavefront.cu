@@ -19,6 +19,7 @@
 
 #include "wavefront.cuh"
 #include "traverse.cuh"
+#include "guide.cuh"
 
 namespace rgr {
 namespace dev {
@@ -32,8 +33,7 @@ constexpr float kFourPiF = 12.566371f;              // (float)(4.0 * M_PI)
 constexpr double kPiD = 3.14159265358979323846;     // M_PI
 constexpr float kFltMax = 3.40282347e+38f;
 
-enum { kBxdf = 0, kEnv = 1, kNone = 2 };
-enum { kMatLambertian = 1, kMatSpecular = 2, kMatDielectric = 3, kMatWard = 4, kMatVolume = 5, kMatVolumeInside = 6 };
+enum { kBxdf = 0, kEnv = 1, kNone = 2, kGuide = 3 };
 
 RGR_DEV f3 mix3(f3 a, f3 b, float t) { return mk(mix_(a.x, b.x, t), mix_(a.y, b.y, t), mix_(a.z, b.z, t)); }
 RGR_DEV float sqr(float x) { return x * x; }
@@ -200,21 +200,29 @@ RGR_DEV uint32_t volume_hash(float4 v) {  // types.cl:104-106 (C, R.x, R.y, R.z)
     return __float_as_uint(v.w) ^ __float_as_uint(v.x) ^ __float_as_uint(v.y) ^ __float_as_uint(v.z);
 }
 
+// sel0/pdf0: BSDF (or phase function), sel1/pdf1: envmap, sel2/pdf2: the
+// learned guide (guided renders only)
 struct Incident {
     f3 wi;
-    float sel0, sel1, pdf0, pdf1;
+    float sel0, sel1, pdf0, pdf1, sel2, pdf2;
     int strategy;
 };
+template <bool kGuided>
 RGR_DEV float incident_pdf(const Incident& is) {  // types.cl:65-71
     float pdf = 0.0f;
     pdf = pdf + is.sel0 * is.pdf0;
     pdf = pdf + is.sel1 * is.pdf1;
+    if (kGuided) pdf = pdf + is.sel2 * is.pdf2;
     return pdf;
 }
 
 // One slot's share of a step, from new_path to homogeneous_volume_through.
 // k: the queue the slot came from (0 = new path, else its material type).
-RGR_DEV void shade_slot(const RequestD& rq, const PathsView& P, int k, uint32_t slot, unsigned long long gpix) {
+// Guided renders: gi is the slot's index among this bounce's guided items
+// (its mixture in gd.lobes), ~0u when the vertex is not guided.
+template <bool kGuided>
+RGR_DEV void shade_slot(const RequestD& rq, const PathsView& P, int k, uint32_t slot, unsigned long long gpix,
+                        const GuideRenderD& gd, uint32_t gi) {
     const SceneView& sc = rq.sc;
     float4 ro4 = P.ro[slot], rd4 = P.rd[slot], T4 = P.T[slot], L4 = P.L[slot], ng4 = P.ng[slot];
     int4 va = P.vols[2 * (size_t)slot], vb = P.vols[2 * (size_t)slot + 1];
@@ -255,13 +263,14 @@ RGR_DEV void shade_slot(const RequestD& rq, const PathsView& P, int k, uint32_t 
         hs = -1;
         tmin = kFltMax;
         Ng = mk(0, 0, 0);
+        if (kGuided) gd.nrec[slot] = 0;
     }
     f3 shLe = mk(0, 0, 0), shT = mk(1, 1, 1);
 
     // strategy_selection (mixture_density.cl:7-133)
     Incident is;
     is.wi = mk(0, 0, 0);
-    is.sel0 = is.sel1 = is.pdf0 = is.pdf1 = 0.0f;
+    is.sel0 = is.sel1 = is.pdf0 = is.pdf1 = is.sel2 = is.pdf2 = 0.0f;
     is.strategy = kNone;
     const bool surface_hit = 0 <= hs, volume_hit = 0 <= hv;
     int envq = -1;
@@ -282,11 +291,31 @@ RGR_DEV void shade_slot(const RequestD& rq, const PathsView& P, int k, uint32_t 
             is.sel0 = bxdf_p;
             is.sel1 = 1.0f - bxdf_p;
         }
+        if (kGuided && gi != ~0u) {  // the guide takes its share of the non-envmap probability
+            is.sel2 = is.sel0 * gd.guide_frac;
+            is.sel0 = is.sel0 - is.sel2;
+        }
         float u = rng.uniform();
-        is.strategy = (u <= is.sel0) ? kBxdf : kEnv;
+        if (kGuided) {
+            is.strategy = (u <= is.sel0) ? kBxdf : ((u <= is.sel0 + is.sel2) ? kGuide : kEnv);
+        } else {
+            is.strategy = (u <= is.sel0) ? kBxdf : kEnv;
+        }
         if (is.sel1 != 0.0f) {
             const int sq = volume_hit ? 0 : 2, eq = volume_hit ? 1 : 3;
             envq = is.strategy == kEnv ? sq : eq;
+        }
+    }
+    GuideMixture mix;
+    if (kGuided && gi != ~0u) {
+        load_mixture(gd.lobes + (size_t)kGuideLobeVecs * gi, mix);
+        if (is.strategy == kGuide) {
+            const float u0 = rng.uniform();
+            const float u1 = rng.uniform();
+            const float u2 = rng.uniform();
+            float d[3];
+            mixture_sample(mix, u0, u1, u2, d);
+            is.wi = mk(d[0], d[1], d[2]);
         }
     }
     const size_t count = (size_t)sc.env_w * sc.env_h;
@@ -317,16 +346,18 @@ RGR_DEV void shade_slot(const RequestD& rq, const PathsView& P, int k, uint32_t 
     if (k >= 1 && k <= 5) mref = __ldg(sc.materials + hs);
     if (k == kMatLambertian) {  // sample_or_eval_lambertian_stage (lambertian.cl:34-71)
         float cosTheta;
+        f3 ns = Ng;  // the raw Ng, as the reference samples, unless two-sided sampling is on
+        if ((kGuided || (rq.flags & kFlagTwoSidedLambertian)) && dot(ns, -rd) < 0.0f) ns = -ns;
         if (is.strategy == kBxdf) {
             float u0 = rng.uniform();
             float u1 = rng.uniform();
             f3 wl = cosine_hemisphere(u0, u1);
             f3 xa, ya;
-            orthonormal_basis(Ng, xa, ya);
-            is.wi = xa * wl.x + ya * wl.y + Ng * wl.z;
+            orthonormal_basis(ns, xa, ya);
+            is.wi = xa * wl.x + ya * wl.y + ns * wl.z;
             cosTheta = wl.z;
         } else {
-            cosTheta = dot(Ng, is.wi);
+            cosTheta = dot(ns, is.wi);
         }
         is.pdf0 = fmax_(cosTheta, 0.0f) / kPiF;
     } else if (k == kMatWard) {  // sample_or_eval_ward_stage (ward.cl:76-117)
@@ -355,8 +386,10 @@ RGR_DEV void shade_slot(const RequestD& rq, const PathsView& P, int k, uint32_t 
     // evaluate_envmap_6axis_pdf_stage / evaluate_envmap_pdf_stage (envmap_sampling.cl:250-281)
     if (envq == 3) {
         size_t xb, yb, zb;
-        six_axis_bases(count, Ng, xb, yb, zb);  // the raw Ng, as the reference does
-        f3 ap = Ng * Ng;
+        f3 n = Ng;  // the raw Ng, as the reference does, unless the backside fix is on
+        if ((kGuided || (rq.flags & kFlagFixBacksideEnvPdf)) && dot(n, -rd) < 0.0f) n = -n;
+        six_axis_bases(count, n, xb, yb, zb);
+        f3 ap = n * n;
         int index = envmap_index(is.wi, sc.env_w, sc.env_h);
         float pdf = 0.0f;
         pdf = pdf + ap.x * __ldg(sc.env_pdf + xb + index);
@@ -366,13 +399,24 @@ RGR_DEV void shade_slot(const RequestD& rq, const PathsView& P, int k, uint32_t 
     } else if (envq == 1) {
         is.pdf1 = __ldg(sc.env_pdf + envmap_index(is.wi, sc.env_w, sc.env_h));
     }
+    if (kGuided && is.sel2 != 0.0f) is.pdf2 = mixture_pdf(mix, is.wi.x, is.wi.y, is.wi.z);
+    // the guided vertex as the network saw it (before the stage moves ro)
+    f3 gx = mk(0, 0, 0), gn = mk(0, 0, 0);
+    if (kGuided && is.sel2 != 0.0f) {
+        gx = ro + rd * tmin;
+        if (hs >= 0) {
+            gn = Ng;
+            if (dot(gn, -rd) < 0.0f) gn = -gn;
+        }
+    }
+    const f3 wo_in = -rd;
     // material stages
     if (k == kMatLambertian) {  // lambertian_stage (lambertian.cl:73-123)
         float4 le = __ldg(sc.lambertians + 2 * (size_t)mref.y), R = __ldg(sc.lambertians + 2 * (size_t)mref.y + 1);
         f3 n = Ng;
         if (dot(n, -rd) < 0.0f) n = -n;
         f3 wi = is.wi;
-        float pdf = incident_pdf(is);
+        float pdf = incident_pdf<kGuided>(is);
         float cosTheta = dot(wi, n);
         f3 Ts = mk(0, 0, 0);
         if (0.0f < cosTheta) Ts = xyz(R) / kPiF * cosTheta / pdf;
@@ -387,7 +431,7 @@ RGR_DEV void shade_slot(const RequestD& rq, const PathsView& P, int k, uint32_t 
         f3 wo = -rd;
         if (dot(n, wo) < 0.0f) n = -n;
         f3 wi = is.wi;
-        float pdf = incident_pdf(is);
+        float pdf = incident_pdf<kGuided>(is);
         float cosTheta = dot(wi, n);
         f3 Ts = mk(0, 0, 0);
         if (0.0f < cosTheta) {
@@ -433,7 +477,7 @@ RGR_DEV void shade_slot(const RequestD& rq, const PathsView& P, int k, uint32_t 
     } else if (k == kMatVolumeInside) {  // homogeneous_volume_inside_stage (homogeneous_volume.cl:90-129)
         int2 mi = __ldg(sc.materials + hv);
         float4 vol = __ldg(sc.volumes + mi.y);
-        float pdf = incident_pdf(is);
+        float pdf = incident_pdf<kGuided>(is);
         shT = xyz(vol) / kFourPiF / pdf;
         ro = ro + rd * tmin;
         rd = is.wi;
@@ -472,6 +516,23 @@ RGR_DEV void shade_slot(const RequestD& rq, const PathsView& P, int k, uint32_t 
     // logic.cl:31-33, applied here: the stage that made the shading result consumes it
     L = L + T * shLe;
     T = T * shT;
+    if (kGuided && is.sel2 != 0.0f && gd.record) {
+        // training record: the vertex, the sampled direction, the path's (L, T) just
+        // after this vertex, so that the logic can recover the radiance L_i that
+        // arrived along wi when the path ends, and cos / pdf of the sample
+        const uint32_t r = gd.nrec[slot];
+        if (r < (uint32_t)kGuideRecords) {
+            const float c = (hs >= 0) ? fmax_(dot(is.wi, gn), 0.0f) : 1.0f;
+            const float cp = c / incident_pdf<kGuided>(is);
+            float4* rec = gd.records + ((size_t)slot * kGuideRecords + r) * 5;
+            rec[0] = make_float4(gx.x, gx.y, gx.z, gn.x);
+            rec[1] = make_float4(gn.y, gn.z, wo_in.x, wo_in.y);
+            rec[2] = make_float4(wo_in.z, is.wi.x, is.wi.y, is.wi.z);
+            rec[3] = make_float4(L.x, L.y, L.z, T.x);
+            rec[4] = make_float4(T.y, T.z, cp, 0.0f);
+            gd.nrec[slot] = (uint8_t)(r + 1);
+        }
+    }
 
     // homogeneous_volume_through (homogeneous_volume_through.cl:7-44)
     hs = -1;
@@ -596,12 +657,16 @@ __global__ void __launch_bounds__(256) k_compact_new(PathsView P, QueueView Q) {
     }
 }
 
+template <bool kGuided>
 __global__ void __launch_bounds__(256) k_shade(PathsView P, QueueView Q, RenderParams rp) {
     uint32_t off[kNumQueues + 1];
     off[0] = 0;
 #pragma unroll
     for (int k = 0; k < kNumQueues; ++k) off[k + 1] = off[k] + Q.counts[k];
     const uint32_t total = off[kNumQueues];
+    // guided items are numbered Lambertian, Ward, in-volume (as the inference kernel does)
+    const uint32_t g4 = off[kMatLambertian + 1] - off[kMatLambertian];
+    const uint32_t g6 = g4 + (off[kMatWard + 1] - off[kMatWard]);
     const unsigned long long base_pixel = *Q.step_base;
     const uint32_t stride = gridDim.x * blockDim.x;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += stride) {
@@ -625,7 +690,13 @@ __global__ void __launch_bounds__(256) k_shade(PathsView P, QueueView Q, RenderP
         } else {
             r = P.req[slot];
         }
-        shade_slot(rp.reqs[r], P, k, slot, gpix);
+        uint32_t gi = ~0u;
+        if (kGuided) {
+            if (k == kMatLambertian) gi = i - off[kMatLambertian];
+            else if (k == kMatWard) gi = g4 + (i - off[kMatWard]);
+            else if (k == kMatVolumeInside && rp.gd.volumes) gi = g6 + (i - off[kMatVolumeInside]);
+        }
+        shade_slot<kGuided>(rp.reqs[r], P, k, slot, gpix, rp.gd, gi);
     }
 }
 
@@ -641,6 +712,56 @@ RGR_DEV void enqueue(const QueueView& Q, int q, uint32_t slot, unsigned active) 
     Q.items[q][base + rank] = slot;
 }
 
+RGR_DEV uint32_t mix32(uint32_t h) {  // murmur3 finaliser
+    h ^= h >> 16;
+    h *= 0x85ebca6bu;
+    h ^= h >> 13;
+    h *= 0xc2b2ae35u;
+    h ^= h >> 16;
+    return h;
+}
+
+// A guided path ended with radiance L: turn its training records into samples.
+// Record r holds the vertex, the sampled wi, the (L, T) of the path just after
+// the vertex (its emission added, its throughput factor applied) and cos / pdf
+// of wi, so the radiance that arrived along wi is L_i = (L_end - L_r) / T_r
+// per channel, and the sample's weight in the KL loss is lum(L_i) cos / pdf:
+// the guide learns the cosine-weighted incident radiance, which the MIS
+// combines with the BSDF (the network does not see the material).
+// Records are offered with the acceptance probability the last iteration set
+// (a hash of slot, record and iteration, not the path's RNG, so rendering is
+// unchanged) until `cap` samples are in.  Returns the records offered.
+RGR_DEV uint32_t guide_emit_samples(const GuideRenderD& gd, uint32_t slot, f3 L) {
+    const GuideTrainD& tr = gd.train;
+    const uint32_t nr = min((uint32_t)gd.nrec[slot], (uint32_t)kGuideRecords);
+    if (nr == 0u) return 0u;
+    const float accept = *tr.accept;
+    const uint32_t it = *tr.iter;
+    uint32_t offered = 0;
+    for (uint32_t r = 0; r < nr; ++r) {
+        const float4* rec = gd.records + ((size_t)slot * kGuideRecords + r) * 5;
+        const float4 d = rec[3], e = rec[4];
+        const float lx = d.w > 0.0f ? (L.x - d.x) / d.w : 0.0f;
+        const float ly = e.x > 0.0f ? (L.y - d.y) / e.x : 0.0f;
+        const float lz = e.y > 0.0f ? (L.z - d.z) / e.y : 0.0f;
+        const float w = (0.2126f * lx + 0.7152f * ly + 0.0722f * lz) * e.z;
+        if (!(w > 0.0f) || !is_finite(w)) continue;
+        ++offered;
+        const uint32_t h = mix32(slot * 0x9e3779b1u ^ (r + 1u) * 0x85ebca77u ^ (it + 1u) * 0xc2b2ae3du);
+        if ((float)(h >> 8) * (1.0f / 16777216.0f) >= accept) continue;
+        const uint32_t idx = atomicAdd(tr.count, 1u);
+        if (idx >= tr.cap) continue;
+        float4* dst = reinterpret_cast<float4*>(tr.samples + 16 * (size_t)idx);
+        dst[0] = rec[0];  // x, n.x
+        dst[1] = rec[1];  // n.yz, wo.xy
+        dst[2] = rec[2];  // wo.z, wi
+        dst[3] = make_float4(w, 0.0f, 0.0f, 0.0f);
+        atomicAdd(tr.wsum, w);
+    }
+    return offered;
+}
+
+template <bool kGuided>
 __global__ void __launch_bounds__(128) k_trace_logic(PathsView P, QueueView Q, RenderParams rp) {
     const uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x;
     const bool live = slot < P.n && P.qid[slot] != kQueueIdle;
@@ -704,6 +825,17 @@ __global__ void __launch_bounds__(128) k_trace_logic(PathsView P, QueueView Q, R
             atomicAdd(a + 2, (double)L.z);
             atomicAdd(a + 3, 1.0);
         }
+    }
+    if (kGuided) {
+        uint32_t offered = 0;
+        if (newPath && rp.gd.record) {
+            const float cl = rq.radiance_clamp;
+            if (is_finite(L.x) && is_finite(L.y) && is_finite(L.z) && L.x < cl && L.y < cl && L.z < cl)
+                offered = guide_emit_samples(rp.gd, slot, L);
+        }
+        offered = __reduce_add_sync(active, offered);
+        if ((int)(threadIdx.x & 31) == __ffs(active) - 1 && offered)
+            atomicAdd(rp.gd.train.candidates, (unsigned long long)offered);
     }
     P.T[slot] = f4(T, T4.w);
     P.L[slot] = f4(L, __uint_as_float(logic_i + 1));
@@ -859,10 +991,16 @@ void launch_compact_new(const PathsView& p, const QueueView& q, cudaStream_t st)
     k_compact_new<<<q.ntiles, 256, 0, st>>>(p, q);
 }
 void launch_shade(const PathsView& p, const QueueView& q, const RenderParams& rp, int grid, cudaStream_t st) {
-    k_shade<<<grid, 256, 0, st>>>(p, q, rp);
+    if (rp.gd.lobes)
+        k_shade<true><<<grid, 256, 0, st>>>(p, q, rp);
+    else
+        k_shade<false><<<grid, 256, 0, st>>>(p, q, rp);
 }
 void launch_trace_logic(const PathsView& p, const QueueView& q, const RenderParams& rp, cudaStream_t st) {
-    k_trace_logic<<<(p.n + 127) / 128, 128, 0, st>>>(p, q, rp);
+    if (rp.gd.lobes)
+        k_trace_logic<true><<<(p.n + 127) / 128, 128, 0, st>>>(p, q, rp);
+    else
+        k_trace_logic<false><<<(p.n + 127) / 128, 128, 0, st>>>(p, q, rp);
 }
 void launch_readback(int fmt, const double* accum, uint32_t npix, void* out, cudaStream_t st) {
     k_readback<<<(npix + 255) / 256, 256, 0, st>>>(fmt, accum, npix, out);

@@ -9,6 +9,8 @@ namespace dev {
 constexpr uint32_t kTile = 4096;         // slots per compaction tile
 constexpr uint8_t kQueueIdle = 0xff;     // slot finished its sample budget
 constexpr int kNumQueues = 7;            // 0 new path, 1..6 material types (logic.cl:317-331)
+// material types = queue numbers (kernels/types.cl:5-11)
+enum { kMatLambertian = 1, kMatSpecular = 2, kMatDielectric = 3, kMatWard = 4, kMatVolume = 5, kMatVolumeInside = 6 };
 
 // Path state, structure of arrays, one entry per resident path slot.
 // Reference fields (kernels/types.cl:18-63) are packed into 16-byte vectors:
@@ -60,12 +62,54 @@ struct RequestD {
     float radiance_clamp;
     float env_p;
     int32_t max_depth;
-    int32_t pad;
+    uint32_t flags;                    // kFlagFixBacksideEnvPdf | kFlagTwoSidedLambertian
     double* accum;                     // 4 doubles per pixel: r, g, b, count
     unsigned long long sample_begin;   // global sample indices [begin, end) are this request's
     unsigned long long sample_end;     // ~0: progressive, no end
     unsigned long long* done;          // paths of this request that finished (kept or discarded)
     unsigned long long* done_ns;       // %globaltimer when the last one finished
+};
+
+// RequestD.flags: evaluate the 6-axis envmap pdf of a BSDF-sampled direction
+// with the normal flipped toward the viewer, as the envmap sampler does
+// (the reference evaluates it with the raw normal, envmap_sampling.cl:263-265
+// vs :195-198, which biases back-face hits).  Always on in guided renders.
+constexpr uint32_t kFlagFixBacksideEnvPdf = 1u;
+// RequestD.flags: sample the Lambertian BSDF around the normal flipped toward
+// the viewer (the reference samples around the raw normal, lambertian.cl:49-68,
+// but evaluates with the flipped one, :98-102, so a back-face hit can never
+// reflect a BSDF sample).  Always on in guided renders.
+constexpr uint32_t kFlagTwoSidedLambertian = 2u;
+
+// ------------------------------------------------------------ path guiding
+// training-sample stream of a guided render, all counters on the device so
+// that the whole bounce (inference, shading, recording, training, Adam) is
+// one CUDA graph
+struct GuideTrainD {
+    float* samples;                 // 16 floats each: x, n, wo, wi, weight, 3 spare
+    uint32_t cap;                   // samples per training iteration
+    uint32_t* count;                // appended this iteration (may exceed cap; extra dropped)
+    float* wsum;                    // sum of appended weights
+    unsigned long long* candidates; // finished records offered this iteration
+    float* accept;                  // acceptance probability of a finished record
+    uint32_t* iter;                 // completed training iterations (Adam step)
+    uint32_t* last;                 // samples the last iteration trained on
+    float* loss_hist;               // loss of every iteration, ring of kLossHist
+};
+constexpr uint32_t kLossHist = 4096;
+constexpr int kGuideRecords = 3;   // training records kept per path (its first guided vertices)
+constexpr int kGuideLobeVecs = 10;  // float4 per inferred mixture: 8 x (mean, kappa) + 2 x 4 weights
+
+// per-render guiding state the wavefront kernels read
+struct GuideRenderD {
+    float4* lobes;        // kGuideLobeVecs per guided queue item of this bounce
+    float4* records;      // per slot kGuideRecords x 5 float4
+    uint8_t* nrec;        // records written on the slot's current path
+    GuideTrainD train;
+    float guide_frac;     // share of the non-envmap selection probability given to the guide
+    int32_t volumes;      // guide in-volume vertices too
+    int32_t record;       // record training samples
+    int32_t pad;
 };
 
 struct RenderParams {
@@ -74,6 +118,7 @@ struct RenderParams {
     unsigned long long sample_limit;  // end of the last range; 0 = progressive
     uint32_t* err;
     unsigned long long* rays;         // extension rays cast
+    GuideRenderD gd;                  // guided renders only (gd.lobes == nullptr otherwise)
 };
 
 // launchers (wavefront.cu)

@@ -342,6 +342,54 @@ def mixed_scene(level: int = 8, seed: int = 3, volume: bool = True, env: bool = 
     return mesh, envmap, camera
 
 
+def sky_room(level: int = 4, seed: int = 3):
+    """A closed room lit only through a skylight: Lambertian walls, floor and
+    ceiling (normals inward), a 1.2 x 1.2 opening in the ceiling, the
+    displaced sphere (radius ~0.55, full-render material mix) and a Ward box
+    inside, and the sky envmap (4x brighter) with a high sun whose patch falls
+    on the floor.
+    Most envmap directions from inside are blocked, so envmap and BSDF
+    sampling both waste samples: the case learned guiding is for."""
+    rng = np.random.default_rng(seed)
+    P, I, mats = [], [], []
+    center = np.array([0.0, 1.25, 0.0], dtype=F32)
+
+    def add(pts, tris, m, outward, inside):
+        base = sum(len(p) for p in P)
+        pts = np.asarray(pts, dtype=F32)
+        tris = orient(pts, np.asarray(tris, dtype=np.uint32), np.asarray(inside, dtype=F32), outward)
+        P.append(pts)
+        I.append(tris + base)
+        if isinstance(m, np.ndarray):
+            mats.append(m)
+        else:
+            mats.append(M.as_array([m] * len(tris)))
+
+    q = [[0, 1, 2], [0, 2, 3]]
+    wall = M.lambertian(r=(0.7, 0.7, 0.7))
+    floor = M.lambertian(r=(0.55, 0.5, 0.45))
+    X, Y, Z = 2.0, 2.5, 2.0
+    add([[-X, 0, -Z], [X, 0, -Z], [X, 0, Z], [-X, 0, Z]], q, floor, False, center)
+    add([[-X, 0, -Z], [X, 0, -Z], [X, Y, -Z], [-X, Y, -Z]], q, wall, False, center)
+    add([[-X, 0, Z], [X, 0, Z], [X, Y, Z], [-X, Y, Z]], q, wall, False, center)
+    add([[-X, 0, -Z], [-X, Y, -Z], [-X, Y, Z], [-X, 0, Z]], q, M.lambertian(r=(0.7, 0.25, 0.2)), False, center)
+    add([[X, 0, -Z], [X, Y, -Z], [X, Y, Z], [X, 0, Z]], q, M.lambertian(r=(0.2, 0.45, 0.7)), False, center)
+    # ceiling around the skylight x in [0.3, 1.1], z in [-1.2, -0.4]
+    wx0, wx1, wz0, wz1 = 0.1, 1.3, -1.4, -0.2
+    for x0, x1, z0, z1 in ((-X, wx0, -Z, Z), (wx1, X, -Z, Z), (wx0, wx1, -Z, wz0), (wx0, wx1, wz1, Z)):
+        add([[x0, Y, z0], [x1, Y, z0], [x1, Y, z1], [x0, Y, z1]], q, wall, False, center)
+    sph = displaced_icosphere(level, seed=7)
+    sp = sph.points * 0.55 + np.array([-0.4, 0.6, -0.2], dtype=F32)
+    add(sp, sph.indices, M.random_mix(sph.ntris, rng), True, sp.mean(axis=0))
+    bp, bi = _box([0.5, 0.0, 0.3], [1.2, 0.9, 1.0], (0.94, 0.34), (0.85, 0.65))
+    add(bp, bi, M.ward(alpha=0.15, reflectance=(0.04,) * 3, edgetint=(0.04,) * 3), True, bp.mean(axis=0))
+    mesh = Mesh(np.concatenate(P).astype(F32), np.concatenate(I).astype(np.uint32), np.concatenate(mats))
+    envmap = sky_envmap(sun_dir=(0.3, 0.9, 0.3))
+    envmap[..., :3] *= 4.0
+    camera = dict(eye=(-0.2, 1.4, 1.9), target=(0.0, 0.7, -0.6), up=(0.0, 1.0, 0.0), vfov=62.0, w=640, h=360)
+    return mesh, envmap, camera
+
+
 # ------------------------------------------------------------------ batched requests
 _ICO = {}
 

@@ -1,0 +1,148 @@
+"""The guiding network's CUDA kernels (BF16 tensor-core forward, backward,
+Adam) against the float64 oracle, and online training on a known
+distribution.  Tolerances: the kernels accumulate in FP32 and use FP32
+transcendental functions where the oracle uses float64, and a value that
+lands next to a BF16 rounding boundary can round the other way; 1 % relative
+L2 error per layer bounds both with room to spare."""
+import numpy as np
+import pytest
+
+from oracle import guide_oracle as go
+
+pytestmark = pytest.mark.gpu
+
+LO, HI = (-1.0, -1.0, -1.0), (1.0, 1.0, 1.0)
+IE = (0.5, 0.5, 0.5)
+
+
+def _torch():
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    return torch
+
+
+def _guide(rg, seed=3, **cfg):
+    g = rg.Guide(0, **cfg)
+    W, b = go.init_weights(seed)
+    g.set_weights(W, b)
+    g.set_bounds(LO, HI)
+    return g, W, b
+
+
+def _rel(a, b):
+    return float(np.linalg.norm(np.asarray(a, np.float64) - b) / max(np.linalg.norm(b), 1e-30))
+
+
+def test_forward_matches_oracle(rg):
+    torch = _torch()
+    g, W, b = _guide(rg)
+    s = go.random_samples(3000, seed=11)
+    rows = torch.from_numpy(s).cuda()
+    out = torch.zeros((len(s), go.OUTPUTS), dtype=torch.float32, device="cuda")
+    g.infer_device(rows.data_ptr(), len(s), out.data_ptr())
+    torch.cuda.synchronize()
+    got = out.cpu().numpy()
+    ref, _ = go.forward(W, b, go.encode(s[:, 0:9], LO, IE), bf16_round=True)
+    exact, _ = go.forward(W, b, go.encode(s[:, 0:9], LO, IE), bf16_round=False)
+    assert _rel(got, ref) < 1e-2
+    # BF16 is what separates the kernel from the exact network
+    assert _rel(got, exact) < 0.1
+
+
+def test_gradients_match_oracle(rg):
+    torch = _torch()
+    g, W, b = _guide(rg)
+    s = go.random_samples(4096, seed=12)
+    dev = torch.from_numpy(s).cuda()
+    grads = torch.zeros(rg.Guide.N_PARAMS, dtype=torch.float32, device="cuda")
+    scale = 1.0 / float(s[:, 12].sum())
+    loss = g.train_device(dev.data_ptr(), len(s), weight_scale=scale, apply_adam=False, grads_ptr=grads.data_ptr())
+    gg = grads.cpu().numpy()
+    dW = gg[:go.LAYERS * go.WIDTH * go.WIDTH].reshape(go.LAYERS, go.WIDTH, go.WIDTH)
+    db = gg[go.LAYERS * go.WIDTH * go.WIDTH:].reshape(go.LAYERS, go.WIDTH)
+    rloss, rdW, rdb = go.gradients(W, b, s, LO, IE, weight_scale=scale, bf16_round=True)
+    assert abs(loss - rloss) <= 1e-3 * abs(rloss)
+    for l in range(go.LAYERS):
+        assert _rel(dW[l], rdW[l]) < 1e-2, (l, _rel(dW[l], rdW[l]))
+        assert _rel(db[l], rdb[l]) < 1e-2, (l, _rel(db[l], rdb[l]))
+    # no gradient outside the 36-64x4-40 network
+    for l in range(go.LAYERS):
+        assert not dW[l, go.FAN_IN[l]:, :].any() and not dW[l, :, go.FAN_OUT[l]:].any()
+        assert not db[l, go.FAN_OUT[l]:].any()
+    # the weights did not move without Adam
+    W2, b2 = g.weights()
+    assert (W2 == W).all() and (b2 == b).all()
+
+
+def test_adam_step_matches_oracle(rg):
+    torch = _torch()
+    g, W, b = _guide(rg, learning_rate=1e-3)
+    s = go.random_samples(2048, seed=13)
+    dev = torch.from_numpy(s).cuda()
+    grads = torch.zeros(rg.Guide.N_PARAMS, dtype=torch.float32, device="cuda")
+    p = np.concatenate([W.ravel(), b.ravel()])
+    m = np.zeros_like(p)
+    v = np.zeros_like(p)
+    for t in (1, 2, 3):
+        g.train_device(dev.data_ptr(), len(s), weight_scale=1e-3, apply_adam=True, grads_ptr=grads.data_ptr())
+        prev = p
+        p, m, v = go.adam(p, grads.cpu().numpy(), m, v, t, lr=1e-3)
+        W2, b2 = g.weights()
+        got = np.concatenate([W2.ravel(), b2.ravel()])
+        # Each step moves a parameter by up to lr = 1e-3.  1 - beta2^t cancels
+        # catastrophically, so one ulp of FP32 pow between CUDA and numpy shifts
+        # an update by ~1e-5 of itself: compare the updates to 1e-4 of lr.
+        assert np.abs(p - prev).max() > 5e-4
+        np.testing.assert_allclose(got, p, rtol=0, atol=1e-7)
+    assert g.stats()["iterations"] == 3
+    # padding stays exactly zero
+    W2, b2 = g.weights()
+    for l in range(go.LAYERS):
+        assert not W2[l, go.FAN_IN[l]:, :].any() and not W2[l, :, go.FAN_OUT[l]:].any()
+        assert not b2[l, go.FAN_OUT[l]:].any()
+
+
+def _vmf_sample(rng, mu, kappa):
+    """Directions from vMF(mu[i], kappa) (Wood's method restated in numpy)."""
+    n = len(mu)
+    u = rng.random(n)
+    w = 1.0 + np.log(u + (1.0 - u) * np.exp(-2.0 * kappa)) / kappa
+    phi = 2 * np.pi * rng.random(n)
+    a = np.where(np.abs(mu[:, 0:1]) < 0.9, [[1.0, 0, 0]], [[0, 1.0, 0]])
+    t = np.cross(mu, a)
+    t /= np.linalg.norm(t, axis=1, keepdims=True)
+    bb = np.cross(mu, t)
+    s = np.sqrt(np.maximum(0.0, 1.0 - w * w))[:, None]
+    return w[:, None] * mu + s * (np.cos(phi)[:, None] * t + np.sin(phi)[:, None] * bb)
+
+
+def test_training_learns_a_direction_field(rg):
+    """Samples whose incident direction follows vMF(normalize(x + (0, 0.5, 0)), 20):
+    the network must learn the position-dependent lobe.  The loss is the
+    mean negative log-likelihood; a uniform guess scores log(4 pi) = 2.53,
+    the target's own entropy is -0.16."""
+    torch = _torch()
+    g = rg.Guide(0, learning_rate=5e-3, seed=7)
+    g.set_bounds(LO, HI)
+    rng = np.random.default_rng(21)
+    n = 1 << 14
+
+    def batch():
+        s = go.random_samples(n, seed=int(rng.integers(1 << 30)))
+        mu = s[:, 0:3].astype(np.float64) + np.array([0.0, 0.5, 0.0])
+        mu /= np.linalg.norm(mu, axis=1, keepdims=True)
+        s[:, 9:12] = _vmf_sample(rng, mu, 20.0)
+        s[:, 12] = 1.0
+        return s
+
+    evals = torch.from_numpy(batch()).cuda()
+    first = g.train_device(evals.data_ptr(), n, weight_scale=1.0 / n, apply_adam=False)
+    for it in range(400):
+        dev = torch.from_numpy(batch()).cuda()
+        g.train_device(dev.data_ptr(), n, weight_scale=1.0 / n, apply_adam=True)
+    last = g.train_device(evals.data_ptr(), n, weight_scale=1.0 / n, apply_adam=False)
+    assert first > 2.0
+    assert last < 0.8, (first, last)
+    hist = g.loss_history()
+    assert len(hist) == 400 and hist[-20:].mean() < hist[:20].mean() - 1.0
