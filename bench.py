@@ -204,6 +204,84 @@ def batch_bench(dev_index: int, n: int = 32) -> dict:
             "setup_s": round(setup_s, 1)}
 
 
+def guide_kernels_bench(dev_index: int) -> dict:
+    """The guiding network's kernels on 2^18 random samples: one training
+    iteration (forward + loss + backward on the tensor cores, gradient flush,
+    Adam) and inference, timed with CUDA events on the stream they run on.
+    FLOPs are the network's own (36-64-64-64-64-40: 34,304 per sample forward,
+    2x that backward), not the zero padding the kernels also multiply."""
+    import numpy as np
+    import torch
+    import raccoongpurender_gb300 as rg
+    n = 1 << 18
+    fwd = 2 * (36 * 64 + 3 * 64 * 64 + 64 * 40)
+    g = rg.Guide(dev_index)
+    g.set_bounds((-1, -1, -1), (1, 1, 1))
+    rng = np.random.default_rng(5)
+    rows = np.zeros((n, 16), np.float32)
+    rows[:, 0:3] = rng.uniform(-1, 1, (n, 3))
+    for c in (3, 6, 9):  # normal, outgoing and incident directions
+        v = rng.normal(size=(n, 3))
+        rows[:, c:c + 3] = v / np.linalg.norm(v, axis=1, keepdims=True)
+    rows[:, 12] = rng.uniform(0.1, 2.0, n)
+    s = torch.from_numpy(rows).cuda(dev_index)
+    out = torch.empty((n, 40), dtype=torch.float32, device=s.device)
+    st = torch.cuda.Stream(device=s.device)
+    sp = st.cuda_stream
+    for _ in range(3):
+        g.train_device(s.data_ptr(), n, weight_scale=1.0 / n, apply_adam=True, stream=sp)
+        g.infer_device(s.data_ptr(), n, out.data_ptr(), stream=sp)
+    torch.cuda.synchronize()
+    reps = 20
+    with torch.cuda.stream(st):
+        e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+        e0.record(st)
+        for _ in range(reps):
+            g.infer_device(s.data_ptr(), n, out.data_ptr(), stream=sp)
+        e1.record(st)
+    torch.cuda.synchronize()
+    infer_ms = e0.elapsed_time(e1) / reps
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        g.train_device(s.data_ptr(), n, weight_scale=1.0 / n, apply_adam=True, stream=sp)  # synchronous
+    train_ms = (time.perf_counter() - t0) * 1e3 / reps
+    return {"samples": n, "infer_ms": round(infer_ms, 4), "infer_tflops": round(n * fwd / infer_ms / 1e9, 1),
+            "train_iteration_ms": round(train_ms, 4),
+            "train_tflops": round(3 * n * fwd / train_ms / 1e9, 1),
+            "note": "train time is host wall time of a synchronous call (includes launch and sync overhead)"}
+
+
+def guiding_bench(dev_index: int, w: int = 960, h: int = 540, spp: int = 256, ref_spp: int = 16384) -> dict:
+    """Equal-time relMSE, guided vs plain, against a ref_spp FP64-accumulated
+    plain render, at w x h: plain rendering at `spp` against guided rendering
+    given the same wall time: "cold" (the guide starts untrained and trains
+    online on the render's own samples, inference and training inside the
+    time) and "warm" (the guide a cold run trained, frozen).  Medians over 3
+    seeds.  Scenes: the full-render glossy/volume scene (the 1.31M-triangle
+    sphere, ground, volume box, sky + sun) and the sky-lit room."""
+    import raccoongpurender_gb300 as rg
+    from raccoongpurender_gb300 import guiding, scenes
+    out = {}
+    for name in ("glossy_volume", "sky_room"):
+        if name == "glossy_volume":
+            mesh, env, camd = scenes.mixed_scene(level=8, seed=3)
+        else:
+            mesh, env, camd = scenes.sky_room(level=6)
+        sm = rg.SceneManager()
+        sm.addMesh(mesh)
+        sm.setEnvmap(env)
+        sm.buildBVH(max_leaf_size=4)
+        cam = rg.camera_look_at(camd["eye"], camd["target"], camd["up"], camd["vfov"], w, h)
+        t0 = time.perf_counter()
+        ref = guiding.render_mean(rg, sm, cam, spp=ref_spp, seed_offset=1 << 30, path_count=1 << 22)
+        ref_s = time.perf_counter() - t0
+        r = guiding.equal_time(rg, sm, cam, ref, spp, path_count=1 << 22)
+        r.update({"resolution": f"{w}x{h}", "reference_spp": ref_spp, "reference_s": round(ref_s, 2),
+                  "triangles": int(mesh.ntris)})
+        out[name] = r
+    return out
+
+
 def cpu_baseline(mesh, sm, coherent, incoherent, sample: int = 1048576) -> dict:
     """The oracle traversal (kernels/extension_ray_cast_stackless.cl restated)
     on all host threads over a bounded sample: the first `sample` rays of each
@@ -255,6 +333,7 @@ def main() -> None:
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--no-render", action="store_true", help="skip the full-render measurements")
+    ap.add_argument("--no-guiding", action="store_true", help="skip the learned-guiding measurements")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -387,6 +466,9 @@ def main() -> None:
         render = {"cornell_256_4spp": render_bench(local, "cornell"),
                   "mixed_1080p_64spp": render_bench(local, "mixed"),
                   "batch_32_requests": batch_bench(local)}
+    guide = None
+    if not args.no_guiding:
+        guide = {"kernels": guide_kernels_bench(local), "equal_time": guiding_bench(local)}
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cpu = cpu_baseline(mesh, sm, coherent, incoherent)
@@ -403,7 +485,7 @@ def main() -> None:
                 "e2e": {"value": round(e2e_value, 1), "unit": "Mrays/s", "h2d_bytes_per_step": rays_per_step * 28,
                         "d2h_bytes_per_step": rays_per_step * 8},
                 "gpu_launches": 2 * args.steps, "roofline": roof, "cpu_baseline": cpu, "clocks": clocks,
-                "render": render}
+                "render": render, "guiding": guide}
         print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()

@@ -273,9 +273,10 @@ typedef struct rgr_guide_config {
     uint32_t batch_samples;  /* training samples per iteration (2^18) */
     float guide_fraction;    /* share of the non-envmap selection probability given to the guide (0.5) */
     int32_t train;           /* train online while rendering (1), or keep the weights fixed (0) */
-    int32_t guide_volumes;   /* guide in-volume scattering too (1) */
+    int32_t guide_volumes;   /* guide in-volume scattering too (0: the isotropic phase function and
+                                envmap sampling stay; guiding it doubles the largest per-vertex weight) */
     uint32_t train_interval; /* bounces per training iteration (1): samples of all of them feed it */
-    uint32_t reserved;
+    uint32_t max_iterations; /* stop training (and recording samples) after this many iterations (0: never) */
     uint64_t seed;           /* weight initialisation (1) */
 } rgr_guide_config;
 typedef struct rgr_guide_stats {

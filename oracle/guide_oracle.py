@@ -14,7 +14,8 @@ CUDA kernels implement:
   that opposite directions, v = 0 and v = 1, encode differently);
 * an MLP 36 -> 64 -> 64 -> 64 -> 64 -> 40 with ReLU, stored as five
   zero-padded 64 x 64 matrices W[l][in][out] and biases b[l][64];
-* an 8-lobe von Mises-Fisher mixture read from the 40 outputs (per lobe: mean
+* an 8-lobe von Mises-Fisher mixture read from the 40 outputs, field-major
+  (output 8 f + i is field f of lobe i; per lobe: mean
   = o / |o|, kappa = min(softplus(o_k) + 0.01, 5000), weights = softmax of
   the logits bounded as 5 tanh(o_w / 5)), vMF density
   kappa / (2 pi (1 - e^{-2 kappa})) e^{kappa (mu.d - 1)};
@@ -97,10 +98,16 @@ def softplus(x):
     return np.where(x > 20.0, x, np.log1p(np.exp(np.minimum(x, 20.0))))
 
 
+def lobes(raw: np.ndarray) -> np.ndarray:
+    """Raw outputs (n, 40), field-major (output 8 f + i is field f of lobe i),
+    as (n, lobe, field)."""
+    return raw.reshape(-1, 5, LOBES).transpose(0, 2, 1)
+
+
 def mixture(raw: np.ndarray):
     """(mu (n,8,3), kappa (n,8), weights (n,8), |o| (n,8), tanh of the scaled
     logits (n,8)) of raw outputs."""
-    o = raw.reshape(-1, LOBES, 5)
+    o = lobes(raw)
     nrm = np.maximum(np.linalg.norm(o[:, :, 0:3], axis=2), 1e-12)
     mu = o[:, :, 0:3] / nrm[:, :, None]
     kappa = np.minimum(softplus(o[:, :, 3]) + 0.01, KAPPA_MAX)
@@ -123,14 +130,14 @@ def mixture_pdf(raw: np.ndarray, d: np.ndarray) -> np.ndarray:
 
 def penalty(raw: np.ndarray, w: np.ndarray) -> np.ndarray:
     """Per-sample w * NORM_PENALTY * sum over lobes of (|o| - 1)^2."""
-    nrm = np.linalg.norm(raw.reshape(-1, LOBES, 5)[:, :, 0:3], axis=2)
+    nrm = np.linalg.norm(lobes(raw)[:, :, 0:3], axis=2)
     return w * NORM_PENALTY * ((nrm - 1.0) ** 2).sum(axis=1)
 
 
 def loss_and_grad(raw: np.ndarray, d: np.ndarray, w: np.ndarray):
     """Per-sample loss -w log q(d), and the gradient of -w log q(d) + penalty
     with respect to the raw outputs (n, 40), analytic."""
-    o = raw.reshape(-1, LOBES, 5)
+    o = lobes(raw)
     mu, kappa, pi, nrm, th = mixture(raw)
     c = np.einsum("nkc,nc->nk", mu, d)
     f = vmf_pdf(kappa, c)
@@ -145,7 +152,7 @@ def loss_and_grad(raw: np.ndarray, d: np.ndarray, w: np.ndarray):
     gmu = (-W * r * kappa)[:, :, None] * d[:, None, :]
     gm = (gmu * mu).sum(axis=2, keepdims=True)
     g[:, :, 0:3] = (gmu - gm * mu) / nrm[:, :, None] + (2.0 * W * NORM_PENALTY * (nrm - 1.0))[:, :, None] * mu
-    return -w * np.log(q), g.reshape(-1, OUTPUTS)
+    return -w * np.log(q), g.transpose(0, 2, 1).reshape(-1, OUTPUTS)
 
 
 def backward(W: np.ndarray, acts, dy_out: np.ndarray, bf16_round: bool = True):

@@ -166,6 +166,7 @@ struct rgr_context {
     int graph_steps = 1;
     int graph_steps_default = 1;
     cudaGraphExec_t graph_exec = nullptr;
+    std::string graph_exec_key;  // graph_key() when graph_exec was captured
     // ray-cast service buffers
     DevBuf trays[7], tprim, tt, tread, tcounter;
     int trace_grid = 0;      // persistent traversal grid (SMs x resident blocks)
@@ -246,13 +247,12 @@ struct rgr_context {
         graph_steps = (graph_steps + ti - 1) / ti * ti;
         steps = 0;
         begun = true;
-        drop_graph();
         return RGR_OK;
     }
     // train_now: a guided render ends a training interval with this bounce
     int step_launches(cudaStream_t st, bool train_now = true) {
         launch_compact_new(pv, qv, st);
-        if (guided) launch_guide_infer_paths(guide->view, pv, qv, rp.gd, num_sms * 3, st);
+        if (guided) launch_guide_infer_paths(guide->view, pv, qv, rp.gd, guide_infer_grid(num_sms), st);
         launch_shade(pv, qv, rp, shade_grid, st);
         RGR_CUDA(cudaMemsetAsync(qv.counts + 1, 0, sizeof(uint32_t) * (kNumQueues - 1), st));
         RGR_CUDA(cudaMemsetAsync(qv.tile_new, 0, sizeof(uint32_t) * ntiles, st));
@@ -306,7 +306,10 @@ struct rgr_context {
             if (graph_mode) {
                 const int k = n >= graph_steps ? graph_steps : 1;
                 if (k == graph_steps || graph_steps == 1) {
+                    const std::string key = graph_key();
+                    if (graph_exec && key != graph_exec_key) drop_graph();
                     if (!graph_exec) {
+                        graph_exec_key = key;
                         cudaGraph_t g = nullptr;
                         RGR_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
                         int r = RGR_OK;
@@ -335,6 +338,27 @@ struct rgr_context {
     void drop_graph() {
         if (graph_exec) cudaGraphExecDestroy(graph_exec);
         graph_exec = nullptr;
+    }
+    // Everything a captured bounce graph bakes in: the kernels' parameter
+    // structs and launch shapes.  A new render whose key is unchanged (same
+    // pool, request table, sample limit and guide) replays the graph it has;
+    // the request table's contents (scene, camera, accumulation buffer) are
+    // read from device memory and may change freely.
+    std::string graph_key() const {
+        std::string k;
+        auto add = [&k](const void* p, size_t n) { k.append(static_cast<const char*>(p), n); };
+        add(&pv, sizeof(pv));
+        add(&qv, sizeof(qv));
+        add(&rp, sizeof(rp));
+        add(&shade_grid, sizeof(shade_grid));
+        add(&graph_steps, sizeof(graph_steps));
+        add(&guided, sizeof(guided));
+        if (guided) {
+            add(&guide->view, sizeof(guide->view));
+            add(&guide->cfg, sizeof(guide->cfg));
+            add(&num_sms, sizeof(num_sms));
+        }
+        return k;
     }
 };
 

@@ -98,9 +98,11 @@ int rgr_guide::init(const rgr_guide_config& c) {
         t.iter = reinterpret_cast<uint32_t*>(ctr + kCtrIter);
         t.last = reinterpret_cast<uint32_t*>(ctr + base + kCtrLast);
         t.loss_hist = loss_hist.as<float>();
+        t.max_iter = 0;
     };
     stream_at(0, train);
     stream_at(kCtrTest, test);
+    train.max_iter = cfg.max_iterations;
     // He-uniform initialisation of the real part of each layer (the output layer
     // scaled by 1/4 so that the first mixtures are broad), zero biases and padding
     std::vector<float> hw(kGuideWeights, 0.0f), hb(kGuideBiases, 0.0f);
@@ -147,9 +149,9 @@ void rgr_guide_config_default(rgr_guide_config* c) {
     c->batch_samples = 1u << 18;
     c->guide_fraction = 0.5f;
     c->train = 1;
-    c->guide_volumes = 1;
+    c->guide_volumes = 0;
     c->train_interval = 1;
-    c->reserved = 0;
+    c->max_iterations = 0;
     c->seed = 1;
 }
 
@@ -207,6 +209,7 @@ int rgr_guide_set_config(rgr_guide* g, const rgr_guide_config* cfg) {
         g->train.cap = g->test.cap = cfg->batch_samples;
     }
     g->cfg = *cfg;
+    g->train.max_iter = cfg->max_iterations;
     return RGR_OK;
 }
 
@@ -253,7 +256,7 @@ int rgr_guide_infer_device(rgr_guide* g, const float* rows, uint32_t n, float* o
     if (!g || (n && (!rows || !out))) return RGR_E_INVALID;
     if (n == 0) return RGR_OK;
     RGR_CUDA(cudaSetDevice(g->device));
-    const int grid = (int)std::min<uint32_t>((n + 63) / 64, (uint32_t)g->num_sms * 3u);
+    const int grid = (int)std::min<uint32_t>((n + 127) / 128, (uint32_t)guide_infer_grid(g->num_sms));
     launch_guide_infer(g->view, rows, n, out, grid, (cudaStream_t)stream);
     RGR_CUDA(cudaGetLastError());
     return RGR_OK;

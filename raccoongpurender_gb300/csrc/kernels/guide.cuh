@@ -24,7 +24,7 @@ constexpr int kGuideWeights = kGuideLayers * kGuideWidth * kGuideWidth;  // W[l]
 constexpr int kGuideBiases = kGuideLayers * kGuideWidth;
 constexpr int kGuideParams = kGuideWeights + kGuideBiases;
 constexpr int kGuideInputs = 36;   // 9 coordinates x 2 octaves x (sin, cos)
-constexpr int kGuideOutputs = 40;  // 8 lobes x (mean xyz, concentration, weight)
+constexpr int kGuideOutputs = 40;  // field-major: output 8 f + i is field f (mean xyz, concentration, weight) of lobe i
 constexpr float kGuideKappaMax = 5000.0f;
 constexpr float kGuideLogitBound = 5.0f;    // lobe weight logits lie in (-5, 5)
 constexpr float kGuideNormPenalty = 0.01f;  // pull of each direction output's length toward 1
@@ -119,6 +119,8 @@ size_t guide_infer_smem();
 size_t guide_train_smem();
 // opt the kernels into their dynamic shared memory on the current device (cudaError_t)
 int guide_kernel_attributes();
+// persistent grid of the inference kernels (resident CTAs)
+int guide_infer_grid(int num_sms);
 // raw network outputs (40 floats per row) of rows of 16 floats (x, n, wo in the first 9)
 void launch_guide_infer(const GuideView& g, const float* rows, uint32_t n, float* out, int grid, cudaStream_t st);
 // mixtures of this bounce's guided queue items (Lambertian, Ward, in-volume when enabled)

@@ -3,24 +3,34 @@
 //
 // Network: 36 frequency-encoding inputs (position, normal, outgoing
 // direction), four hidden layers of 64 with ReLU, 40 outputs = 8 von
-// Mises-Fisher lobes x (mean direction xyz, concentration, weight).  Every
-// layer is stored as a 64 x 64 matrix W[l][in][out] (padding rows and columns
-// are zero, receive zero gradient and stay zero under Adam), so one code path
-// serves all five layers.
+// Mises-Fisher lobes x (mean direction xyz, concentration, weight logit).
+// Every layer is stored as a 64 x 64 matrix W[l][in][out] (padding rows and
+// columns are zero, receive zero gradient and stay zero under Adam), so one
+// code path serves all five layers.  The outputs are field-major: output
+// 8 f + i is field f (0..2 mean, 3 concentration, 4 weight logit) of lobe i.
 //
-// Tensor-core tiling (mma.sync m16n8k16 bf16 -> f32): a warp owns 16 rows.
-// Forward keeps the activations in registers from layer to layer: the
-// accumulator fragment of two adjacent m16n8 tiles is exactly the A-operand
-// fragment of the next m16n8k16 product, so nothing moves between layers
-// except through bias + ReLU + bf16 conversion.  Weights live in shared
-// memory as W[in][out] (row stride 72 bf16, so the 8 rows an ldmatrix phase
-// reads fall in distinct banks); the forward B operand is loaded with
-// ldmatrix.trans, the backward one with plain 32-bit loads.  Training
-// processes 64-row chunks per CTA: the layer inputs of the chunk stay in
-// shared memory, dW = A^T dY runs on the tensor cores with the chunk's rows as
-// the reduction dimension, and each warp accumulates its 16 input rows of dW
-// in shared FP32 across all chunks of the CTA; one atomicAdd per weight per
-// CTA flushes it.
+// Tensor-core tiling (mma.sync m16n8k16 bf16 -> f32): a warp owns 16 rows;
+// lane (g, q) = (lane / 4, lane % 4) holds rows g and g + 8 of every
+// fragment.  Everything stays in registers from the input encoding to the
+// mixture:
+//  * each lane computes the encoding features its A fragment needs (sin/cos
+//    pairs 8 kt + q and 8 kt + 4 + q of its two rows), so no input tile is
+//    staged in shared memory;
+//  * the accumulator fragment of two adjacent m16n8 tiles is the A fragment
+//    of the next m16n8k16 product, so layers chain through bias + ReLU +
+//    bf16 conversion only;
+//  * with the field-major output order, the last layer's accumulators of a
+//    lane hold all five fields of lobes 2q and 2q + 1 for its two rows, and
+//    the mixture (softmax, densities, loss gradient) needs only shuffles
+//    within the quad.
+// Weights live in shared memory as W[in][out] (row stride 72 bf16, so the 8
+// rows an ldmatrix phase reads fall in distinct banks); the forward B operand
+// is loaded with ldmatrix.trans, the backward one with plain 32-bit loads.
+// Training processes 64-row chunks per CTA: each layer's input stays in
+// shared memory for the chunk, dW = A^T dY runs on the tensor cores with the
+// chunk's rows as the reduction dimension, and each warp accumulates its 16
+// input rows of dW in shared FP32 across all chunks of the CTA; one atomicAdd
+// per weight per CTA flushes it.
 #include <cuda_bf16.h>
 
 #include "guide.cuh"
@@ -32,8 +42,10 @@ namespace {
 constexpr int kH = kGuideWidth;  // padded width of every layer
 constexpr int kLayers = kGuideLayers;
 constexpr int kStride = 72;      // shared-memory row stride of bf16 tiles (elements)
-constexpr int kWarps = 4;        // warps per CTA (training and inference)
-constexpr int kRows = 16 * kWarps;
+constexpr int kTrainWarps = 4;   // warps per training CTA
+constexpr int kRows = 16 * kTrainWarps;
+constexpr int kInferWarps = 8;   // warps per inference CTA
+constexpr int kOutTiles = 5;     // n tiles (of 8) holding the 40 outputs
 
 __device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
     __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
@@ -60,103 +72,37 @@ __device__ __forceinline__ void ldsm_x4_trans(uint32_t* r, const void* smem_row)
 // Frequency encoding: for v in (position mapped to [0,1]^3, (n+1)/2,
 // (wo+1)/2) and octave k in {0, 1}: sin(2^k pi v_c), cos(2^k pi v_c).  The
 // lowest frequency has period 2, so that cos(pi v) is monotonic on [0, 1] and
-// opposite directions (v = 0 and v = 1) encode differently.
-__device__ __forceinline__ void encode(const float* x9, const GuideParams& gp, float* f36) {
-    float v[9];
+// opposite directions (v = 0 and v = 1) encode differently.  Feature pair p
+// (columns 2p = sin, 2p + 1 = cos) is coordinate p / 2 at octave p % 2.
+__device__ __forceinline__ void coords(const float* x9, const GuideParams& gp, float* v) {
     for (int c = 0; c < 3; ++c) {
         v[c] = (x9[c] - gp.lo[c]) * gp.inv_ext[c];
         v[3 + c] = 0.5f * (x9[3 + c] + 1.0f);
         v[6 + c] = 0.5f * (x9[6 + c] + 1.0f);
     }
-    int o = 0;
-    for (int i = 0; i < 9; ++i) {
-        for (int k = 0; k < 2; ++k) {
-            float s, c;
-            sincospif(v[i] * (float)(1 << k), &s, &c);
-            f36[o++] = s;
-            f36[o++] = c;
-        }
+}
+// Pair p = 8 kt + 4 h + q is coordinate 4 kt + 2 h + q / 2 at octave q % 2:
+// the coordinate is chosen between two registers, not indexed at run time.
+__device__ __forceinline__ uint32_t feature_pair(const float* v, int i0, int q) {
+    const int i = i0 + (q >> 1);
+    if (i >= 9) return 0u;  // padding columns 36..63
+    const float x = (q >> 1) ? v[i0 + 1 < 9 ? i0 + 1 : 8] : v[i0];
+    float s, c;
+    sincospif(x * ((q & 1) ? 2.0f : 1.0f), &s, &c);
+    return pack_bf16(s, c);
+}
+// the A fragments of the encoded inputs of this lane's rows g (v0) and g + 8 (v1)
+__device__ __forceinline__ void encode_frag(const float* v0, const float* v1, int q, uint32_t a[4][4]) {
+#pragma unroll
+    for (int kt = 0; kt < 4; ++kt) {
+        a[kt][0] = feature_pair(v0, 4 * kt, q);
+        a[kt][1] = feature_pair(v1, 4 * kt, q);
+        a[kt][2] = feature_pair(v0, 4 * kt + 2, q);
+        a[kt][3] = feature_pair(v1, 4 * kt + 2, q);
     }
 }
 
-// ---------------------------------------------------------------- vMF mixture
-__device__ __forceinline__ float softplus(float x) { return x > 20.0f ? x : log1pf(expf(x)); }
-__device__ __forceinline__ float sigmoid(float x) { return 1.0f / (1.0f + expf(-x)); }
-
-// raw outputs (5 per lobe: mean xyz, concentration, weight logit) -> mixture
-//   mean = o / |o|, kappa = min(softplus(o_k) + 0.01, kGuideKappaMax),
-//   weight = softmax over the 8 bounded logits kGuideLogitBound tanh(o_w / kGuideLogitBound)
-// (bounded so that no lobe's weight can saturate to zero and stop learning)
-__device__ __forceinline__ void mixture_from_raw(const float* o, GuideMixture& m, float* norms, float* th) {
-    float lg[kGuideLobes];
-    float mx = -3.0e38f;
-    for (int i = 0; i < kGuideLobes; ++i) {
-        th[i] = tanhf(o[5 * i + 4] * (1.0f / kGuideLogitBound));
-        lg[i] = kGuideLogitBound * th[i];
-        mx = fmaxf(mx, lg[i]);
-    }
-    float den = 0.0f;
-    for (int i = 0; i < kGuideLobes; ++i) {
-        const float x = o[5 * i], y = o[5 * i + 1], z = o[5 * i + 2];
-        const float n = fmaxf(sqrtf(x * x + y * y + z * z), 1.0e-12f);
-        norms[i] = n;
-        const float kappa = fminf(softplus(o[5 * i + 3]) + 0.01f, kGuideKappaMax);
-        m.lobe[i] = make_float4(x / n, y / n, z / n, kappa);
-        m.w[i] = expf(lg[i] - mx);
-        den += m.w[i];
-    }
-    for (int i = 0; i < kGuideLobes; ++i) m.w[i] /= den;
-}
-
-// Sample loss  -w log q(d)  and the gradient with respect to the 40 raw
-// outputs of  -w log q(d) + w kGuideNormPenalty sum_i (|o_i| - 1)^2,  the
-// second term holding the scale of each lobe's direction output near 1 (the
-// direction o / |o| does not depend on it, and the gradient of the first term
-// shrinks as 1 / |o|).  Returns the first term.
-__device__ __forceinline__ float vmf_loss_grad(const float* o, float dx, float dy, float dz, float w, float* g) {
-    GuideMixture M;
-    float norms[kGuideLobes], th[kGuideLobes];
-    mixture_from_raw(o, M, norms, th);
-    float f[kGuideLobes], q = 0.0f;
-    for (int i = 0; i < kGuideLobes; ++i) {
-        const float4 L = M.lobe[i];
-        f[i] = vmf_pdf(L.w, L.x * dx + L.y * dy + L.z * dz);
-        q += M.w[i] * f[i];
-    }
-    q = fmaxf(q, 1.0e-30f);
-    for (int i = 0; i < kGuideLobes; ++i) {
-        const float4 L = M.lobe[i];
-        const float r = M.w[i] * f[i] / q;  // responsibility of lobe i
-        // weight logit: d(-log q)/d l_i = -(r_i - pi_i), through l = B tanh(o / B)
-        g[5 * i + 4] = -w * (r - M.w[i]) * (1.0f - th[i] * th[i]);
-        // concentration: d log f / d kappa = 1/kappa - 2 e^{-2k} / (1 - e^{-2k}) + (mu.d - 1)
-        const float k = L.w;
-        const float e2 = expf(-2.0f * k);
-        const float md = L.x * dx + L.y * dy + L.z * dz;
-        const float dlogf = 1.0f / k - 2.0f * e2 / -expm1f(-2.0f * k) + (md - 1.0f);
-        const float raw_k = o[5 * i + 3];
-        const float dk = (softplus(raw_k) + 0.01f < kGuideKappaMax) ? sigmoid(raw_k) : 0.0f;
-        g[5 * i + 3] = -w * r * dlogf * dk;
-        // mean: d log f / d mu = kappa d, through mu = o / |o|: (I - mu mu^T) / |o|;
-        // plus the scale penalty 2 w c (|o| - 1) mu
-        const float gx = -w * r * k * dx, gy = -w * r * k * dy, gz = -w * r * k * dz;
-        const float gm = gx * L.x + gy * L.y + gz * L.z;
-        const float pen = 2.0f * w * kGuideNormPenalty * (norms[i] - 1.0f);
-        g[5 * i + 0] = (gx - gm * L.x) / norms[i] + pen * L.x;
-        g[5 * i + 1] = (gy - gm * L.y) / norms[i] + pen * L.y;
-        g[5 * i + 2] = (gz - gm * L.z) / norms[i] + pen * L.z;
-    }
-    return -w * logf(q);
-}
-
-// ---------------------------------------------------------------- shared tiles
-struct SmemFwd {
-    __nv_bfloat16 W[kLayers][kH][kStride];  // W[l][in][out]
-    float b[kLayers][kH];
-    __nv_bfloat16 x[kWarps][16][kStride];   // encoded inputs of each warp's rows
-    float out[kWarps][16][kH + 4];          // raw outputs
-};
-
+// ---------------------------------------------------------------- layers
 __device__ void load_weights(__nv_bfloat16 (*W)[kH][kStride], float (*b)[kH], const GuideView& g) {
     const uint32_t* src = reinterpret_cast<const uint32_t*>(g.wbf);
     for (int i = threadIdx.x; i < kLayers * kH * kH / 2; i += blockDim.x) {
@@ -177,14 +123,24 @@ __device__ __forceinline__ void load_a(uint32_t a[4][4], const __nv_bfloat16 (*t
         a[kt][3] = *reinterpret_cast<const uint32_t*>(&t[g + 8][16 * kt + 8 + 2 * q]);
     }
 }
+__device__ __forceinline__ void store_a(__nv_bfloat16 (*t)[kStride], const uint32_t a[4][4], int lane) {
+    const int g = lane >> 2, q = lane & 3;
+    for (int kt = 0; kt < 4; ++kt) {
+        *reinterpret_cast<uint32_t*>(&t[g][16 * kt + 2 * q]) = a[kt][0];
+        *reinterpret_cast<uint32_t*>(&t[g + 8][16 * kt + 2 * q]) = a[kt][1];
+        *reinterpret_cast<uint32_t*>(&t[g][16 * kt + 8 + 2 * q]) = a[kt][2];
+        *reinterpret_cast<uint32_t*>(&t[g + 8][16 * kt + 8 + 2 * q]) = a[kt][3];
+    }
+}
 
-// acc[16 x 64] = a[16 x 64] * W (B operand from W[in][out] via ldmatrix.trans)
+// acc[16 x 16 NP] = a[16 x 64] * W[:, 0 : 16 NP] (B operand via ldmatrix.trans)
+template <int NP>
 __device__ __forceinline__ void layer_fwd(float acc[8][4], const uint32_t a[4][4], const __nv_bfloat16 (*W)[kStride],
                                           int lane) {
-    for (int j = 0; j < 8; ++j) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.0f;
+    for (int j = 0; j < 2 * NP; ++j) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.0f;
     const int m = lane >> 3, r = lane & 7;
     for (int kt = 0; kt < 4; ++kt) {
-        for (int jp = 0; jp < 4; ++jp) {
+        for (int jp = 0; jp < NP; ++jp) {
             // 8x8 blocks m = 0..3: (k rows 16kt + 8(m&1) + r, n columns 16jp + 8(m>>1))
             uint32_t bq[4];
             ldsm_x4_trans(bq, &W[16 * kt + 8 * (m & 1) + r][16 * jp + 8 * (m >> 1)]);
@@ -194,17 +150,15 @@ __device__ __forceinline__ void layer_fwd(float acc[8][4], const uint32_t a[4][4
     }
 }
 
-// bias (+ ReLU) and repack the accumulator as the next layer's A operand
-__device__ __forceinline__ void activate(uint32_t a[4][4], float acc[8][4], const float* bias, bool relu, int lane) {
+// bias + ReLU, repacked as the next layer's A operand
+__device__ __forceinline__ void activate(uint32_t a[4][4], float acc[8][4], const float* bias, int lane) {
     const int q = lane & 3;
     for (int j = 0; j < 8; ++j) {
         const float b0 = bias[8 * j + 2 * q], b1 = bias[8 * j + 2 * q + 1];
-        acc[j][0] += b0;
-        acc[j][1] += b1;
-        acc[j][2] += b0;
-        acc[j][3] += b1;
-        if (relu)
-            for (int e = 0; e < 4; ++e) acc[j][e] = fmaxf(acc[j][e], 0.0f);
+        acc[j][0] = fmaxf(acc[j][0] + b0, 0.0f);
+        acc[j][1] = fmaxf(acc[j][1] + b1, 0.0f);
+        acc[j][2] = fmaxf(acc[j][2] + b0, 0.0f);
+        acc[j][3] = fmaxf(acc[j][3] + b1, 0.0f);
     }
     for (int kt = 0; kt < 4; ++kt) {
         a[kt][0] = pack_bf16(acc[2 * kt][0], acc[2 * kt][1]);
@@ -214,65 +168,142 @@ __device__ __forceinline__ void activate(uint32_t a[4][4], float acc[8][4], cons
     }
 }
 
-__device__ __forceinline__ void store_acc(float (*out)[kH + 4], const float acc[8][4], int lane) {
-    const int g = lane >> 2, q = lane & 3;
-    for (int j = 0; j < 8; ++j) {
-        out[g][8 * j + 2 * q] = acc[j][0];
-        out[g][8 * j + 2 * q + 1] = acc[j][1];
-        out[g + 8][8 * j + 2 * q] = acc[j][2];
-        out[g + 8][8 * j + 2 * q + 1] = acc[j][3];
-    }
-}
-
-__device__ __forceinline__ void store_inputs(__nv_bfloat16* row, const float* f) {
-    for (int c = 0; c < kH; c += 2)
-        *reinterpret_cast<uint32_t*>(row + c) =
-            pack_bf16(c < kGuideInputs ? f[c] : 0.0f, c + 1 < kGuideInputs ? f[c + 1] : 0.0f);
-}
-
-// forward of one warp's 16 staged rows; raw outputs into S.out[warp]
-__device__ __forceinline__ void forward_tile(SmemFwd& S, int warp, int lane) {
-    uint32_t a[4][4];
+// Raw outputs of the 16 rows whose input fragments are `a`: o[f][h][s] =
+// field f of lobe 2q + s of row g + 8h (bias added).  With keep != nullptr the
+// inputs of layers 1..4 are also stored there (training).
+__device__ __forceinline__ void forward_frag(uint32_t a[4][4], const __nv_bfloat16 (*W)[kH][kStride],
+                                             const float (*b)[kH], int lane, float o[kOutTiles][2][2],
+                                             __nv_bfloat16 (*keep)[kRows][kStride]) {
     float acc[8][4];
-    load_a(a, S.x[warp], lane);
-    for (int l = 0; l < kLayers; ++l) {
-        layer_fwd(acc, a, S.W[l], lane);
-        activate(a, acc, S.b[l], l + 1 < kLayers, lane);
+    for (int l = 0; l + 1 < kLayers; ++l) {
+        layer_fwd<4>(acc, a, W[l], lane);
+        activate(a, acc, b[l], lane);
+        if (keep) store_a(keep[l + 1], a, lane);
     }
-    store_acc(S.out[warp], acc, lane);
+    layer_fwd<3>(acc, a, W[kLayers - 1], lane);
+    const int q = lane & 3;
+    for (int f = 0; f < kOutTiles; ++f) {
+        const float b0 = b[kLayers - 1][8 * f + 2 * q], b1 = b[kLayers - 1][8 * f + 2 * q + 1];
+        o[f][0][0] = acc[f][0] + b0;
+        o[f][0][1] = acc[f][1] + b1;
+        o[f][1][0] = acc[f][2] + b0;
+        o[f][1][1] = acc[f][3] + b1;
+    }
+}
+
+// ---------------------------------------------------------------- vMF mixture
+__device__ __forceinline__ float softplus(float x) { return x > 20.0f ? x : log1pf(expf(x)); }
+__device__ __forceinline__ float sigmoid(float x) { return 1.0f / (1.0f + expf(-x)); }
+__device__ __forceinline__ float quad_max(float x) {
+    x = fmaxf(x, __shfl_xor_sync(0xffffffffu, x, 1));
+    return fmaxf(x, __shfl_xor_sync(0xffffffffu, x, 2));
+}
+__device__ __forceinline__ float quad_sum(float x) {
+    x += __shfl_xor_sync(0xffffffffu, x, 1);
+    return x + __shfl_xor_sync(0xffffffffu, x, 2);
+}
+
+// One lobe of the mixture from its five raw outputs:
+//   mean = o / |o|, kappa = min(softplus(o_3) + 0.01, kGuideKappaMax),
+//   logit = kGuideLogitBound tanh(o_4 / kGuideLogitBound)
+// (bounded so that no lobe's weight can saturate to zero and stop learning).
+struct LobeOut {
+    float mx, my, mz, kappa, norm, th, logit;
+};
+__device__ __forceinline__ LobeOut lobe_of(float o0, float o1, float o2, float o3, float o4) {
+    LobeOut L;
+    L.norm = fmaxf(sqrtf(o0 * o0 + o1 * o1 + o2 * o2), 1.0e-12f);
+    L.mx = o0 / L.norm;
+    L.my = o1 / L.norm;
+    L.mz = o2 / L.norm;
+    L.kappa = fminf(softplus(o3) + 0.01f, kGuideKappaMax);
+    L.th = tanhf(o4 * (1.0f / kGuideLogitBound));
+    L.logit = kGuideLogitBound * L.th;
+    return L;
+}
+
+// The mixture of row h of this lane (its lobes 2q, 2q + 1; weights by softmax
+// across the quad).  All 32 lanes must call it.
+__device__ __forceinline__ void mixture_quad(const float o[kOutTiles][2][2], int h, LobeOut L[2], float w[2]) {
+    for (int s = 0; s < 2; ++s) L[s] = lobe_of(o[0][h][s], o[1][h][s], o[2][h][s], o[3][h][s], o[4][h][s]);
+    const float mx = quad_max(fmaxf(L[0].logit, L[1].logit));
+    w[0] = expf(L[0].logit - mx);
+    w[1] = expf(L[1].logit - mx);
+    const float den = quad_sum(w[0] + w[1]);
+    w[0] /= den;
+    w[1] /= den;
+}
+
+// Loss of row h, -wt log q(d) (returned by every lane of the quad), and its
+// gradient with respect to this lane's raw outputs g[f][s] (lobes 2q + s) of
+// -wt log q(d) + wt kGuideNormPenalty sum_i (|o_i| - 1)^2; the second term
+// holds the length of each lobe's direction output near 1 (the direction
+// o / |o| does not depend on it, and the gradient of the first term shrinks
+// as 1 / |o|).  All 32 lanes must call it.
+__device__ __forceinline__ float loss_grad_quad(const float o[kOutTiles][2][2], int h, float dx, float dy, float dz,
+                                                float wt, float g[kOutTiles][2]) {
+    LobeOut L[2];
+    float pi[2];
+    mixture_quad(o, h, L, pi);
+    float f[2];
+    for (int s = 0; s < 2; ++s) f[s] = vmf_pdf(L[s].kappa, L[s].mx * dx + L[s].my * dy + L[s].mz * dz);
+    const float q = fmaxf(quad_sum(pi[0] * f[0] + pi[1] * f[1]), 1.0e-30f);
+    for (int s = 0; s < 2; ++s) {
+        const float r = pi[s] * f[s] / q;  // responsibility of the lobe
+        // weight logit: d(-log q)/d l = -(r - pi), through l = B tanh(o / B)
+        g[4][s] = -wt * (r - pi[s]) * (1.0f - L[s].th * L[s].th);
+        // concentration: d log f / d kappa = 1/kappa - 2 e^{-2k} / (1 - e^{-2k}) + (mu.d - 1)
+        const float k = L[s].kappa;
+        const float md = L[s].mx * dx + L[s].my * dy + L[s].mz * dz;
+        const float dlogf = 1.0f / k - 2.0f * expf(-2.0f * k) / -expm1f(-2.0f * k) + (md - 1.0f);
+        const float raw_k = o[3][h][s];
+        const float dk = (softplus(raw_k) + 0.01f < kGuideKappaMax) ? sigmoid(raw_k) : 0.0f;
+        g[3][s] = -wt * r * dlogf * dk;
+        // mean: d log f / d mu = kappa d, through mu = o / |o|: (I - mu mu^T) / |o|;
+        // plus the length penalty 2 wt c (|o| - 1) mu
+        const float gx = -wt * r * k * dx, gy = -wt * r * k * dy, gz = -wt * r * k * dz;
+        const float gm = gx * L[s].mx + gy * L[s].my + gz * L[s].mz;
+        const float pen = 2.0f * wt * kGuideNormPenalty * (L[s].norm - 1.0f);
+        g[0][s] = (gx - gm * L[s].mx) / L[s].norm + pen * L[s].mx;
+        g[1][s] = (gy - gm * L[s].my) / L[s].norm + pen * L[s].my;
+        g[2][s] = (gz - gm * L[s].mz) / L[s].norm + pen * L[s].mz;
+    }
+    return -wt * logf(q);
 }
 
 // ---------------------------------------------------------------- inference
+struct SmemFwd {
+    __nv_bfloat16 W[kLayers][kH][kStride];  // W[l][in][out]
+    float b[kLayers][kH];
+};
+
 // rows: 16 floats each (x, n, wo in the first 9); out: 40 raw floats per row
-__global__ void __launch_bounds__(128) k_guide_infer(GuideView g, const float* __restrict__ rows, uint32_t n,
-                                                     float* __restrict__ out) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    SmemFwd& S = *reinterpret_cast<SmemFwd*>(smem_raw);
-    load_weights(S.W, S.b, g);
+__global__ void __launch_bounds__(32 * kInferWarps, 4) k_guide_infer(GuideView gv, const float* __restrict__ rows,
+                                                                      uint32_t n, float* __restrict__ out) {
+    __shared__ SmemFwd S;
+    load_weights(S.W, S.b, gv);
     __syncthreads();
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    for (uint32_t base = (blockIdx.x * kWarps + warp) * 16u; base < n; base += gridDim.x * kWarps * 16u) {
-        if (lane < 16) {
-            const uint32_t r = base + lane;
-            float f[kGuideInputs];
-            if (r < n) {
-                float x9[9];
-                for (int c = 0; c < 9; ++c) x9[c] = rows[16 * (size_t)r + c];
-                encode(x9, g.params, f);
-            } else {
-                for (int c = 0; c < kGuideInputs; ++c) f[c] = 0.0f;
-            }
-            store_inputs(S.x[warp][lane], f);
-        }
-        __syncwarp();
-        forward_tile(S, warp, lane);
-        __syncwarp();
-        for (int e = lane; e < 16 * kGuideOutputs; e += 32) {
-            const uint32_t r = base + e / kGuideOutputs;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, q = lane & 3;
+    for (uint32_t base = (blockIdx.x * kInferWarps + warp) * 16u; base < n; base += gridDim.x * kInferWarps * 16u) {
+        float v[2][9];
+        for (int h = 0; h < 2; ++h) {
+            const uint32_t r = base + g + 8 * h;
+            float x9[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
             if (r < n)
-                out[kGuideOutputs * (size_t)r + e % kGuideOutputs] = S.out[warp][e / kGuideOutputs][e % kGuideOutputs];
+                for (int c = 0; c < 9; ++c) x9[c] = rows[16 * (size_t)r + c];
+            coords(x9, gv.params, v[h]);
         }
-        __syncwarp();
+        uint32_t a[4][4];
+        encode_frag(v[0], v[1], q, a);
+        float o[kOutTiles][2][2];
+        forward_frag(a, S.W, S.b, lane, o, nullptr);
+        for (int h = 0; h < 2; ++h) {
+            const uint32_t r = base + g + 8 * h;
+            if (r >= n) continue;
+            for (int f = 0; f < kOutTiles; ++f)
+                *reinterpret_cast<float2*>(out + kGuideOutputs * (size_t)r + 8 * f + 2 * q) =
+                    make_float2(o[f][h][0], o[f][h][1]);
+        }
     }
 }
 
@@ -313,40 +344,37 @@ __device__ __forceinline__ void vertex_of(const PathsView& P, uint32_t slot, flo
     x9[8] = -rd.z;
 }
 
-__global__ void __launch_bounds__(128) k_guide_infer_paths(GuideView g, PathsView P, QueueView Q, GuideRenderD gd) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    SmemFwd& S = *reinterpret_cast<SmemFwd*>(smem_raw);
+__global__ void __launch_bounds__(32 * kInferWarps, 4) k_guide_infer_paths(GuideView gv, PathsView P, QueueView Q,
+                                                                            GuideRenderD gd) {
+    __shared__ SmemFwd S;
     const uint32_t n = guided_count(Q, gd);
-    if (blockIdx.x * kRows >= n) return;
-    load_weights(S.W, S.b, g);
+    if (blockIdx.x * kInferWarps * 16u >= n) return;
+    load_weights(S.W, S.b, gv);
     __syncthreads();
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    for (uint32_t base = (blockIdx.x * kWarps + warp) * 16u; base < n; base += gridDim.x * kWarps * 16u) {
-        if (lane < 16) {
-            const uint32_t r = base + lane;
-            float f[kGuideInputs];
-            if (r < n) {
-                float x9[9];
-                vertex_of(P, guided_slot(Q, r), x9);
-                encode(x9, g.params, f);
-            } else {
-                for (int c = 0; c < kGuideInputs; ++c) f[c] = 0.0f;
-            }
-            store_inputs(S.x[warp][lane], f);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, q = lane & 3;
+    for (uint32_t base = (blockIdx.x * kInferWarps + warp) * 16u; base < n; base += gridDim.x * kInferWarps * 16u) {
+        float v[2][9];
+        for (int h = 0; h < 2; ++h) {
+            const uint32_t r = base + g + 8 * h;
+            float x9[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+            if (r < n) vertex_of(P, guided_slot(Q, r), x9);
+            coords(x9, gv.params, v[h]);
         }
-        __syncwarp();
-        forward_tile(S, warp, lane);
-        __syncwarp();
-        if (lane < 16 && base + lane < n) {
-            GuideMixture M;
-            float norms[kGuideLobes], th[kGuideLobes];
-            mixture_from_raw(S.out[warp][lane], M, norms, th);
-            float4* dst = gd.lobes + (size_t)kGuideLobeVecs * (base + lane);
-            for (int i = 0; i < kGuideLobes; ++i) dst[i] = M.lobe[i];
-            dst[8] = make_float4(M.w[0], M.w[1], M.w[2], M.w[3]);
-            dst[9] = make_float4(M.w[4], M.w[5], M.w[6], M.w[7]);
+        uint32_t a[4][4];
+        encode_frag(v[0], v[1], q, a);
+        float o[kOutTiles][2][2];
+        forward_frag(a, S.W, S.b, lane, o, nullptr);
+        for (int h = 0; h < 2; ++h) {
+            LobeOut L[2];
+            float w[2];
+            mixture_quad(o, h, L, w);
+            const uint32_t r = base + g + 8 * h;
+            if (r >= n) continue;
+            float4* dst = gd.lobes + (size_t)kGuideLobeVecs * r;
+            dst[2 * q] = make_float4(L[0].mx, L[0].my, L[0].mz, L[0].kappa);
+            dst[2 * q + 1] = make_float4(L[1].mx, L[1].my, L[1].mz, L[1].kappa);
+            reinterpret_cast<float2*>(dst + 8)[q] = make_float2(w[0], w[1]);
         }
-        __syncwarp();
     }
 }
 
@@ -356,84 +384,67 @@ struct SmemTrain {
     float b[kLayers][kH];
     __nv_bfloat16 act[kLayers][kRows][kStride];  // input of layer l for the chunk's rows
     __nv_bfloat16 dy[kRows][kStride];            // gradient at the output of the current layer
-    float out[kWarps][16][kH + 4];
     float gW[kLayers][kH][kH];                   // this CTA's dW; warp w owns input rows 16w..16w+15
     float gb[kLayers][kH];
-    float loss[kWarps];
+    float loss[kTrainWarps];
 };
 
 // samples: 16 floats each (x, n, wo, wi, weight); loss weight = weight * scale / wsum
-__global__ void __launch_bounds__(128) k_guide_train(GuideView g, const float* __restrict__ samples,
-                                                     const uint32_t* __restrict__ count, uint32_t cap,
-                                                     const float* __restrict__ wsum, float weight_scale) {
+__global__ void __launch_bounds__(32 * kTrainWarps) k_guide_train(GuideView gv, const float* __restrict__ samples,
+                                                                  const uint32_t* __restrict__ count, uint32_t cap,
+                                                                  const float* __restrict__ wsum, float weight_scale) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     SmemTrain& S = *reinterpret_cast<SmemTrain*>(smem_raw);
     const uint32_t n = min(*count, cap);
-    if (blockIdx.x * kRows >= n) return;
+    if (blockIdx.x * kRows >= n) return;  // (no samples are recorded once the iteration budget is used up)
     float scale = weight_scale;
     if (wsum) {
         const float s = *wsum;
         scale = s > 0.0f ? weight_scale / s : 0.0f;
     }
-    load_weights(S.W, S.b, g);
+    load_weights(S.W, S.b, gv);
     for (int i = threadIdx.x; i < kLayers * kH * kH; i += blockDim.x) (&S.gW[0][0][0])[i] = 0.0f;
     for (int i = threadIdx.x; i < kLayers * kH; i += blockDim.x) (&S.gb[0][0])[i] = 0.0f;
-    if (threadIdx.x < kWarps) S.loss[threadIdx.x] = 0.0f;
+    if (threadIdx.x < kTrainWarps) S.loss[threadIdx.x] = 0.0f;
     __syncthreads();
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int gq = lane >> 2, q = lane & 3;
     const int r0 = 16 * warp;  // this warp's rows within the chunk
     for (uint32_t chunk = blockIdx.x * (uint32_t)kRows; chunk < n; chunk += gridDim.x * (uint32_t)kRows) {
         // ---- forward, keeping each layer's input
-        float dirw[4] = {0.0f, 0.0f, 0.0f, 0.0f};
-        if (lane < 16) {
-            const uint32_t r = chunk + r0 + lane;
-            float f[kGuideInputs];
+        float v[2][9], dir[2][3], wt[2];
+        for (int h = 0; h < 2; ++h) {
+            const uint32_t r = chunk + r0 + gq + 8 * h;
+            float x9[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+            dir[h][0] = dir[h][1] = dir[h][2] = 0.0f;
+            wt[h] = 0.0f;
             if (r < n) {
                 const float* s = samples + 16 * (size_t)r;
-                float x9[9];
                 for (int c = 0; c < 9; ++c) x9[c] = s[c];
-                encode(x9, g.params, f);
-                dirw[0] = s[9];
-                dirw[1] = s[10];
-                dirw[2] = s[11];
-                dirw[3] = s[12] * scale;
-            } else {
-                for (int c = 0; c < kGuideInputs; ++c) f[c] = 0.0f;
+                dir[h][0] = s[9];
+                dir[h][1] = s[10];
+                dir[h][2] = s[11];
+                wt[h] = s[12] * scale;
             }
-            store_inputs(S.act[0][r0 + lane], f);
+            coords(x9, gv.params, v[h]);
         }
-        __syncwarp();
         uint32_t a[4][4];
-        float acc[8][4];
-        load_a(a, &S.act[0][r0], lane);
-        for (int l = 0; l < kLayers; ++l) {
-            layer_fwd(acc, a, S.W[l], lane);
-            activate(a, acc, S.b[l], l + 1 < kLayers, lane);
-            if (l + 1 < kLayers) {
-                // keep the next layer's input (the bf16 fragments just packed)
-                for (int kt = 0; kt < 4; ++kt) {
-                    *reinterpret_cast<uint32_t*>(&S.act[l + 1][r0 + gq][16 * kt + 2 * q]) = a[kt][0];
-                    *reinterpret_cast<uint32_t*>(&S.act[l + 1][r0 + gq + 8][16 * kt + 2 * q]) = a[kt][1];
-                    *reinterpret_cast<uint32_t*>(&S.act[l + 1][r0 + gq][16 * kt + 8 + 2 * q]) = a[kt][2];
-                    *reinterpret_cast<uint32_t*>(&S.act[l + 1][r0 + gq + 8][16 * kt + 8 + 2 * q]) = a[kt][3];
-                }
-            }
-        }
-        store_acc(S.out[warp], acc, lane);
-        __syncwarp();
-        // ---- loss gradient at the output, one lane per row
+        encode_frag(v[0], v[1], q, a);
+        store_a(&S.act[0][r0], a, lane);
+        float o[kOutTiles][2][2];
+        forward_frag(a, S.W, S.b, lane, o, reinterpret_cast<__nv_bfloat16(*)[kRows][kStride]>(&S.act[0][r0]));
+        // ---- loss gradient at the output, in the fragment layout
         float lossv = 0.0f;
-        if (lane < 16) {
-            float gr[kGuideOutputs];
-            if (dirw[3] > 0.0f) {
-                lossv = vmf_loss_grad(S.out[warp][lane], dirw[0], dirw[1], dirw[2], dirw[3], gr);
-            } else {
-                for (int c = 0; c < kGuideOutputs; ++c) gr[c] = 0.0f;
-            }
-            for (int c = 0; c < kH; c += 2)
-                *reinterpret_cast<uint32_t*>(&S.dy[r0 + lane][c]) =
-                    pack_bf16(c < kGuideOutputs ? gr[c] : 0.0f, c + 1 < kGuideOutputs ? gr[c + 1] : 0.0f);
+        for (int h = 0; h < 2; ++h) {
+            float gr[kOutTiles][2];
+            const float lh = loss_grad_quad(o, h, dir[h][0], dir[h][1], dir[h][2], wt[h], gr);
+            const bool live = wt[h] > 0.0f;
+            if (live && q == 0) lossv += lh;
+            for (int f = 0; f < kOutTiles; ++f)
+                *reinterpret_cast<uint32_t*>(&S.dy[r0 + gq + 8 * h][8 * f + 2 * q]) =
+                    live ? pack_bf16(gr[f][0], gr[f][1]) : 0u;
+            for (int f = kOutTiles; f < 8; ++f)
+                *reinterpret_cast<uint32_t*>(&S.dy[r0 + gq + 8 * h][8 * f + 2 * q]) = 0u;
         }
         for (int off = 16; off > 0; off >>= 1) lossv += __shfl_xor_sync(0xffffffffu, lossv, off);
         if (lane == 0) S.loss[warp] += lossv;
@@ -504,16 +515,16 @@ __global__ void __launch_bounds__(128) k_guide_train(GuideView g, const float* _
     // flush this CTA's gradient
     for (int i = threadIdx.x; i < kLayers * kH * kH; i += blockDim.x) {
         const float v = (&S.gW[0][0][0])[i];
-        if (v != 0.0f) atomicAdd(g.gW + i, v);
+        if (v != 0.0f) atomicAdd(gv.gW + i, v);
     }
     for (int i = threadIdx.x; i < kLayers * kH; i += blockDim.x) {
         const float v = (&S.gb[0][0])[i];
-        if (v != 0.0f) atomicAdd(g.gb + i, v);
+        if (v != 0.0f) atomicAdd(gv.gb + i, v);
     }
     if (threadIdx.x == 0) {
         float s = 0.0f;
-        for (int w = 0; w < kWarps; ++w) s += S.loss[w];
-        atomicAdd(g.loss, s);
+        for (int w = 0; w < kTrainWarps; ++w) s += S.loss[w];
+        atomicAdd(gv.loss, s);
     }
 }
 
@@ -563,26 +574,25 @@ size_t guide_infer_smem() { return sizeof(SmemFwd); }
 size_t guide_train_smem() { return sizeof(SmemTrain); }
 
 int guide_kernel_attributes() {
-    const int a = (int)cudaFuncAttributeMaxDynamicSharedMemorySize;
-    cudaError_t e = cudaFuncSetAttribute(k_guide_infer, (cudaFuncAttribute)a, (int)sizeof(SmemFwd));
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_guide_infer_paths, (cudaFuncAttribute)a, (int)sizeof(SmemFwd));
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_guide_train, (cudaFuncAttribute)a, (int)sizeof(SmemTrain));
-    return (int)e;
+    return (int)cudaFuncSetAttribute(k_guide_train, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)sizeof(SmemTrain));
 }
+
+int guide_infer_grid(int num_sms) { return num_sms * 4; }
 
 void launch_guide_infer(const GuideView& g, const float* rows, uint32_t n, float* out, int grid, cudaStream_t st) {
     if (n == 0) return;
-    k_guide_infer<<<grid, 128, sizeof(SmemFwd), st>>>(g, rows, n, out);
+    k_guide_infer<<<grid, 32 * kInferWarps, 0, st>>>(g, rows, n, out);
 }
 
 void launch_guide_infer_paths(const GuideView& g, const PathsView& p, const QueueView& q, const GuideRenderD& gd,
                               int grid, cudaStream_t st) {
-    k_guide_infer_paths<<<grid, 128, sizeof(SmemFwd), st>>>(g, p, q, gd);
+    k_guide_infer_paths<<<grid, 32 * kInferWarps, 0, st>>>(g, p, q, gd);
 }
 
 void launch_guide_train(const GuideView& g, const float* samples, const uint32_t* count, uint32_t cap,
                         const float* wsum, float weight_scale, int grid, cudaStream_t st) {
-    k_guide_train<<<grid, 128, sizeof(SmemTrain), st>>>(g, samples, count, cap, wsum, weight_scale);
+    k_guide_train<<<grid, 32 * kTrainWarps, sizeof(SmemTrain), st>>>(g, samples, count, cap, wsum, weight_scale);
 }
 
 void launch_guide_adam(const GuideView& g, const uint32_t* count, const uint32_t* iter, float lr, float beta1,

@@ -516,7 +516,7 @@ RGR_DEV void shade_slot(const RequestD& rq, const PathsView& P, int k, uint32_t 
     // logic.cl:31-33, applied here: the stage that made the shading result consumes it
     L = L + T * shLe;
     T = T * shT;
-    if (kGuided && is.sel2 != 0.0f && gd.record) {
+    if (kGuided && is.sel2 != 0.0f && gd.record && guide_training_open(gd.train)) {
         // training record: the vertex, the sampled direction, the path's (L, T) just
         // after this vertex, so that the logic can recover the radiance L_i that
         // arrived along wi when the path ends, and cos / pdf of the sample
@@ -828,7 +828,7 @@ __global__ void __launch_bounds__(128) k_trace_logic(PathsView P, QueueView Q, R
     }
     if (kGuided) {
         uint32_t offered = 0;
-        if (newPath && rp.gd.record) {
+        if (newPath && rp.gd.record && guide_training_open(rp.gd.train)) {
             const float cl = rq.radiance_clamp;
             if (is_finite(L.x) && is_finite(L.y) && is_finite(L.z) && L.x < cl && L.y < cl && L.z < cl)
                 offered = guide_emit_samples(rp.gd, slot, L);

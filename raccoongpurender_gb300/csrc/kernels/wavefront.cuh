@@ -93,12 +93,18 @@ struct GuideTrainD {
     unsigned long long* candidates; // finished records offered this iteration
     float* accept;                  // acceptance probability of a finished record
     uint32_t* iter;                 // completed training iterations (Adam step)
+    uint32_t max_iter;              // no recording or training once *iter reaches it (0: no limit)
     uint32_t* last;                 // samples the last iteration trained on
     float* loss_hist;               // loss of every iteration, ring of kLossHist
 };
 constexpr uint32_t kLossHist = 4096;
 constexpr int kGuideRecords = 3;   // training records kept per path (its first guided vertices)
 constexpr int kGuideLobeVecs = 10;  // float4 per inferred mixture: 8 x (mean, kappa) + 2 x 4 weights
+
+// training still wanted (iteration budget not used up)
+__device__ __forceinline__ bool guide_training_open(const GuideTrainD& t) {
+    return t.max_iter == 0u || *t.iter < t.max_iter;
+}
 
 // per-render guiding state the wavefront kernels read
 struct GuideRenderD {

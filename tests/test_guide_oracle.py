@@ -24,7 +24,7 @@ def test_loss_gradient_finite_differences():
     rng = np.random.default_rng(1)
     n = 16
     raw = rng.normal(size=(n, go.OUTPUTS))
-    raw.reshape(n, go.LOBES, 5)[:, :, 3] = rng.uniform(-2.0, 3.0, (n, go.LOBES))
+    raw[:, 3 * go.LOBES:4 * go.LOBES] = rng.uniform(-2.0, 3.0, (n, go.LOBES))  # concentrations
     d = rng.normal(size=(n, 3))
     d /= np.linalg.norm(d, axis=1, keepdims=True)
     w = rng.uniform(0.1, 2.0, n)
@@ -83,7 +83,7 @@ def test_network_gradient_finite_differences():
 def test_mixture_is_normalised():
     rng = np.random.default_rng(6)
     raw = rng.normal(size=(3, go.OUTPUTS))
-    raw.reshape(3, go.LOBES, 5)[:, :, 3] = rng.uniform(-1.0, 3.0, (3, go.LOBES))  # kappa up to ~3
+    raw[:, 3 * go.LOBES:4 * go.LOBES] = rng.uniform(-1.0, 3.0, (3, go.LOBES))  # kappa up to ~3
     # quasi-uniform directions on the sphere (Fibonacci lattice)
     m = 200_000
     k = np.arange(m) + 0.5
