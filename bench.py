@@ -375,6 +375,12 @@ def main() -> None:
         for soa, prim, t, n in sets:
             lane.trace_closest_device([a.data_ptr() for a in soa], n, prim.data_ptr(), t.data_ptr(), 0, sptr)
 
+    # launch shape and BVH staging depth from the autotuner (results do not depend on them)
+    from raccoongpurender_gb300 import autotune
+    trace_tuned, trace_trials = autotune.tune_trace(
+        lane, [([a.data_ptr() for a in soa], n, prim.data_ptr(), t.data_ptr()) for soa, prim, t, n in sets], sptr,
+        device=local, log=lambda *_: None)
+
     # algorithmic traffic: exact node visits and primitive tests per ray
     counts = []
     for soa, prim, t, n in sets:
@@ -481,6 +487,9 @@ def main() -> None:
                            "bvh": {"max_leaf": 4, "inner_nodes": int(info.num_inner_nodes),
                                    "depth": int(info.depth), "build_s": round(build_s, 2)},
                            "l2": "inputs larger than L2 (224 MB of rays per step)",
+                           "autotuned": trace_tuned,
+                           "autotune_trials": [dict(t["params"], ms=round(t["seconds"] * 1e3, 3))
+                                               for t in trace_trials],
                            "parallelism": f"replicas{world}"},
                 "e2e": {"value": round(e2e_value, 1), "unit": "Mrays/s", "h2d_bytes_per_step": rays_per_step * 28,
                         "d2h_bytes_per_step": rays_per_step * 8},

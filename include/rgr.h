@@ -252,6 +252,22 @@ int rgr_set_render_tuning(rgr_context* c, int32_t shade_blocks_per_sm, int32_t g
    256-thread blocks per SM (0 = as many as fit).  Chosen by the autotuner. */
 int rgr_set_trace_tuning(rgr_context* c, int32_t refill, int32_t blocks_per_sm);
 
+/* How a bounce casts its extension rays: persistent = 1 runs a persistent
+   closest-hit kernel over the slots just shaded whose warps take new slots
+   when at least `refill` (1..32, default 24) lanes are idle, then the logic
+   kernel; persistent = 0 traces and runs the logic in one kernel, one thread
+   per slot; persistent = -1 (default) picks 1 for scenes of at least 4096
+   inner BVH nodes.  Results are identical.  Takes effect at the next
+   rgr_render_begin. */
+int rgr_set_render_trace(rgr_context* c, int32_t persistent, int32_t refill);
+
+/* Shared-memory staging of the closest-hit kernel: each CTA copies the first
+   staged_nodes (0..1024) inner nodes — the top levels of the tree, which the
+   builder stores first in breadth-first order — into shared memory and reads
+   them from there (64 bytes each; more staging means fewer resident CTAs).
+   0 = off.  Chosen by the autotuner. */
+int rgr_set_trace_staging(rgr_context* c, uint32_t staged_nodes);
+
 /* ---- learned path guiding (no counterpart in the reference) --------------
    A small MLP maps a shading vertex (frequency-encoded position, normal and
    outgoing direction: 36 inputs) through 4 hidden layers of 64 (ReLU) to an

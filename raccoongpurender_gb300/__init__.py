@@ -140,6 +140,8 @@ _SIGS = {
     "rgr_trace_closest_counts_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p, C.c_void_p,
                                                   C.c_void_p, C.c_void_p, C.c_void_p]),
     "rgr_set_trace_tuning": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32]),
+    "rgr_set_trace_staging": (C.c_int, [C.c_void_p, C.c_uint32]),
+    "rgr_set_render_trace": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32]),
     "rgr_set_render_tuning": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32]),
     "rgr_batch_create": (C.c_int, [C.c_void_p, C.c_int32, C.c_uint32]),
     "rgr_batch_destroy": (None, [C.c_void_p]),
@@ -465,6 +467,16 @@ class WavefrontLane:
 
     def set_trace_tuning(self, refill: int = 16, blocks_per_sm: int = 0) -> None:
         _check(self._lib.rgr_set_trace_tuning(self._h, refill, blocks_per_sm), "rgr_set_trace_tuning")
+
+    def set_render_trace(self, persistent=-1, refill: int = 24) -> None:
+        """Extension rays of a bounce: persistent refilling kernel + logic (True),
+        fused (False), or by scene size (-1, the default)."""
+        mode = persistent if isinstance(persistent, int) and not isinstance(persistent, bool) else int(bool(persistent))
+        _check(self._lib.rgr_set_render_trace(self._h, mode, refill), "rgr_set_render_trace")
+
+    def set_trace_staging(self, staged_nodes: int) -> None:
+        """Top BVH nodes each traversal CTA keeps in shared memory (0 = off)."""
+        _check(self._lib.rgr_set_trace_staging(self._h, staged_nodes), "rgr_set_trace_staging")
 
     def trace_closest_counts_device(self, soa_ptrs, n: int, prim_ptr: int, t_ptr: int, nodes_ptr: int,
                                     prims_ptr: int, stream: int = 0) -> None:

@@ -4,7 +4,10 @@ Knobs (all results are bit-identical across knob values; only speed changes):
   * path_count     — resident paths in the pool (queue capacities follow it);
   * graph_steps    — bounces per replayed CUDA graph;
   * shade_blocks   — resident 256-thread blocks per SM of the shade kernel;
-  * trace_refill / trace_blocks — closest-hit kernel launch shape.
+  * trace_refill   — refill a closest-hit warp with new rays when this many
+                     lanes are idle;
+  * trace_stage    — top BVH nodes each closest-hit CTA stages in shared
+                     memory (the "BVH staging depth": 64 nodes = 6 levels).
 Coordinate descent from a default point: each knob in turn is swept over its
 candidates with the others fixed, keeping the fastest.  Each trial runs a
 proxy of the real workload (the same scenes and cameras with the samples per
@@ -22,6 +25,8 @@ from pathlib import Path
 
 DEFAULTS = dict(path_count=1 << 22, graph_steps=8, shade_blocks=8)
 CANDIDATES = dict(path_count=[1 << 20, 1 << 21, 1 << 22], graph_steps=[4, 8, 16], shade_blocks=[4, 8, 16])
+TRACE_DEFAULTS = dict(trace_refill=24, trace_stage=0)
+TRACE_CANDIDATES = dict(trace_refill=[8, 16, 24, 32], trace_stage=[0, 64, 256, 1024])
 
 
 def _gpu_name(device: int) -> str:
@@ -54,16 +59,19 @@ class Autotuner:
         tmp.write_text(json.dumps(d, indent=1, sort_keys=True))
         os.replace(tmp, self.cache_path)
 
-    def tune(self, signature: str, run_trial, use_cache: bool = True) -> dict:
+    def tune(self, signature: str, run_trial, use_cache: bool = True, defaults: dict | None = None,
+             candidates: dict | None = None) -> dict:
         """run_trial(params) -> seconds.  Returns the best params."""
+        defaults = DEFAULTS if defaults is None else defaults
+        candidates = CANDIDATES if candidates is None else candidates
         key = hashlib.sha1((_gpu_name(self.device) + "|" + signature).encode()).hexdigest()[:16]
         if use_cache:
             cached = self._load().get(key)
             if cached:
                 return dict(cached["params"])
-        best = dict(DEFAULTS)
+        best = dict(defaults)
         best_t = self._time(run_trial, best)
-        for knob, values in CANDIDATES.items():
+        for knob, values in candidates.items():
             for v in values:
                 if v == best[knob]:
                     continue
@@ -104,3 +112,35 @@ def tune_batch(scenes_and_requests, device: int = 0, spp_cap: int = 4, use_cache
         return time.perf_counter() - t0
 
     return Autotuner(device, log=log).tune(sig, trial, use_cache=use_cache)
+
+
+def tune_trace(lane, ray_sets, stream: int, device: int = 0, reps: int = 3, use_cache: bool = False,
+               log=print) -> tuple[dict, list]:
+    """Tune the closest-hit kernel (refill threshold, BVH staging depth) on
+    `ray_sets`, a list of (7 device pointers, n, prim pointer, t pointer), by
+    timing `reps` passes over all sets with CUDA events on `stream`.  Applies
+    the best to `lane`; returns (params, trials)."""
+    import torch
+
+    sig = "trace|" + "|".join(str(n) for _, n, _, _ in ray_sets)
+    st = torch.cuda.ExternalStream(stream)
+
+    def run(p):
+        lane.set_trace_staging(p["trace_stage"])
+        lane.set_trace_tuning(p["trace_refill"], 0)
+        for ptrs, n, pp, tp in ray_sets:  # warm
+            lane.trace_closest_device(ptrs, n, pp, tp, 0, stream)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        for _ in range(reps):
+            for ptrs, n, pp, tp in ray_sets:
+                lane.trace_closest_device(ptrs, n, pp, tp, 0, stream)
+        e1.record(st)
+        e1.synchronize()
+        return e0.elapsed_time(e1) * 1e-3 / reps
+
+    tuner = Autotuner(device, log=log)
+    best = tuner.tune(sig, run, use_cache=use_cache, defaults=TRACE_DEFAULTS, candidates=TRACE_CANDIDATES)
+    lane.set_trace_staging(best["trace_stage"])
+    lane.set_trace_tuning(best["trace_refill"], 0)
+    return best, tuner.trials

@@ -277,6 +277,47 @@ struct Flattener {
 
 }  // namespace
 
+// Device-layout order for shared-memory staging: the first `k` inner nodes a
+// breadth-first walk from the root meets (the levels every ray passes
+// through) move to the front of the node array in that order, the others keep
+// their depth-first order; links are renumbered.  The traversal kernel copies
+// a prefix of the array into shared memory and reads those nodes from there.
+// Results do not depend on the order: links are explicit.
+void stage_top_levels(Bvh& b, size_t k) {
+    const size_t n = b.nodes.size();
+    if (n == 0 || (b.root_link & kLeafFlag)) return;
+    k = std::min(k, n);
+    std::vector<uint32_t> bfs;
+    bfs.reserve(k);
+    std::vector<uint8_t> taken(n, 0);
+    bfs.push_back(b.root_link);
+    taken[b.root_link] = 1;
+    for (size_t head = 0; head < bfs.size() && bfs.size() < k; ++head) {
+        const NodeD& d = b.nodes[bfs[head]];
+        for (int c = 0; c < 2 && bfs.size() < k; ++c) {
+            const uint32_t l = d.link[c];
+            if (!(l & kLeafFlag) && !taken[l]) {
+                taken[l] = 1;
+                bfs.push_back(l);
+            }
+        }
+    }
+    std::vector<uint32_t> to_new(n);
+    uint32_t next = 0;
+    for (uint32_t old : bfs) to_new[old] = next++;
+    for (uint32_t i = 0; i < n; ++i)
+        if (!taken[i]) to_new[i] = next++;
+    std::vector<NodeD> out(n);
+    for (uint32_t i = 0; i < n; ++i) {
+        NodeD d = b.nodes[i];
+        for (int c = 0; c < 2; ++c)
+            if (!(d.link[c] & kLeafFlag)) d.link[c] = to_new[d.link[c]];
+        out[to_new[i]] = d;
+    }
+    b.nodes.swap(out);
+    b.root_link = to_new[b.root_link];
+}
+
 int build_bvh(rgr_scene* s, const rgr_bvh_params& params) {
     rgr_bvh_params p = params;
     if (p.max_leaf_size < 1 || p.max_leaf_size > 8) {
@@ -364,6 +405,7 @@ int build_bvh(rgr_scene* s, const rgr_bvh_params& params) {
     uint32_t next_ref = 0;
     uint32_t root_link = f.emit(root.get(), 0, &next_ref, 0);
     out.root_link = root_link;  // 0 for an inner root, a leaf link otherwise
+    stage_top_levels(out, kStagedNodes);
     out.depth = f.max_depth_seen;
     float ra = Builder::area(root->lo, root->hi);
     out.sah_cost = ra > 0.0f ? f.sah / ra : 0.0;

@@ -184,13 +184,16 @@ extern "C" int rgr_render_noalloc(rgr_context* c, const rgr_camera* cam, const r
     launch_init(p, q, k.seed_offset, st);
     int sms = 152;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+    const TraceShape ts{true, 24, sms * (trace_paths_max_blocks_per_sm() > 0 ? trace_paths_max_blocks_per_sm() : 1),
+                        scal + 3};
     for (int32_t i = 0; i < steps; ++i) {
         launch_compact_new(p, q, st);
         launch_shade(p, q, rp, sms * 8, st);
+        launch_trace_paths(p, q, rp, ts, st);
         if (!ok(cudaMemsetAsync(q.counts + 1, 0, sizeof(uint32_t) * (kNumQueues - 1), st), "cudaMemsetAsync") ||
             !ok(cudaMemsetAsync(q.tile_new, 0, sizeof(uint32_t) * ntiles, st), "cudaMemsetAsync"))
             return RGR_E_CUDA;
-        launch_trace_logic(p, q, rp, st);
+        launch_trace_logic(p, q, rp, ts, st);
     }
     if (!ok(cudaGetLastError(), "kernel launch")) return RGR_E_CUDA;
     uint32_t err = 0;

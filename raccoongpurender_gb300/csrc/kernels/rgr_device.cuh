@@ -90,6 +90,7 @@ struct SceneView {
     int32_t env_w, env_h;
     int32_t has_env;
     int32_t small_coords;       // every scene coordinate within +-1e30 (no NaN in slab products)
+    uint32_t num_nodes;         // inner nodes
 };
 
 constexpr uint32_t kLeafFlag = 0x80000000u;

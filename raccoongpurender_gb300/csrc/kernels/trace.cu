@@ -33,14 +33,22 @@ struct RayBatch {
     uint32_t* err;
     unsigned long long* next;    // work counter, zero at launch
     int refill;                  // refill when at least this many lanes are idle
+    uint32_t stage;              // inner nodes copied to shared memory (kStaged)
 };
 
-template <bool kCount>
+template <bool kCount, bool kStaged>
 __global__ void __launch_bounds__(256, RGR_TRACE_MIN_BLOCKS) k_trace_rays(SceneView sc, RayBatch b) {
     const unsigned full = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     const unsigned lt = (1u << lane) - 1u;
     const uint64_t pol = l2_evict_last_policy();
+    extern __shared__ float4 s_nodes[];
+    StagedNodes stn{s_nodes, 0u};
+    if (kStaged) {
+        stn.n = min(b.stage, sc.num_nodes);
+        for (uint32_t i = threadIdx.x; i < 4u * stn.n; i += blockDim.x) s_nodes[i] = __ldg(sc.nodes + i);
+        __syncthreads();
+    }
     TraceState s;
     TraceCounters cnt;
     uint64_t ray = ~0ull;  // ~0: idle
@@ -69,7 +77,7 @@ __global__ void __launch_bounds__(256, RGR_TRACE_MIN_BLOCKS) k_trace_rays(SceneV
             continue;
         }
         if (ray != ~0ull) {
-            if (s.link != kDone) trace_round<kCount>(sc, s, &cnt, err, pol);
+            if (s.link != kDone) trace_round<kCount, kStaged>(sc, s, &cnt, err, pol, stn);
             if (s.link == kDone) {
                 __stcs(b.prim + ray, s.prim);
                 __stcs(b.t + ray, s.tmin);
@@ -94,11 +102,15 @@ __global__ void __launch_bounds__(256, RGR_TRACE_MIN_BLOCKS) k_trace_rays(SceneV
 
 void launch_trace_rays(const SceneView& sc, const float* ox, const float* oy, const float* oz, const float* dx,
                        const float* dy, const float* dz, const float* tmax, uint64_t n, int32_t* prim, float* t,
-                       float* ng, uint32_t* err, unsigned long long* counter, int refill, int grid, cudaStream_t st) {
+                       float* ng, uint32_t* err, unsigned long long* counter, int refill, int grid, uint32_t stage,
+                       cudaStream_t st) {
     if (n == 0) return;
-    RayBatch b{ox, oy, oz, dx, dy, dz, tmax, n, prim, t, ng, nullptr, nullptr, err, counter, refill};
+    RayBatch b{ox, oy, oz, dx, dy, dz, tmax, n, prim, t, ng, nullptr, nullptr, err, counter, refill, stage};
     cudaMemsetAsync(counter, 0, sizeof(unsigned long long), st);
-    k_trace_rays<false><<<grid, 256, 0, st>>>(sc, b);
+    if (stage > 0)
+        k_trace_rays<false, true><<<grid, 256, 64 * (size_t)stage, st>>>(sc, b);
+    else
+        k_trace_rays<false, false><<<grid, 256, 0, st>>>(sc, b);
 }
 
 void launch_trace_rays_counts(const SceneView& sc, const float* ox, const float* oy, const float* oz, const float* dx,
@@ -106,14 +118,20 @@ void launch_trace_rays_counts(const SceneView& sc, const float* ox, const float*
                               float* t, uint32_t* nodes, uint32_t* prims, uint32_t* err, unsigned long long* counter,
                               int grid, cudaStream_t st) {
     if (n == 0) return;
-    RayBatch b{ox, oy, oz, dx, dy, dz, tmax, n, prim, t, nullptr, nodes, prims, err, counter, 16};
+    RayBatch b{ox, oy, oz, dx, dy, dz, tmax, n, prim, t, nullptr, nodes, prims, err, counter, 16, 0u};
     cudaMemsetAsync(counter, 0, sizeof(unsigned long long), st);
-    k_trace_rays<true><<<grid, 256, 0, st>>>(sc, b);
+    k_trace_rays<true, false><<<grid, 256, 0, st>>>(sc, b);
 }
 
-int trace_rays_max_blocks_per_sm() {
+int trace_rays_max_blocks_per_sm(uint32_t stage) {
     int nb = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_trace_rays<false>, 256, 0);
+    if (stage > 0) {
+        cudaFuncSetAttribute(k_trace_rays<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)(64 * kMaxStagedNodes));
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_trace_rays<false, true>, 256, 64 * (size_t)stage);
+    } else {
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_trace_rays<false, false>, 256, 0);
+    }
     return nb;
 }
 

@@ -160,18 +160,35 @@ RGR_DEV uint32_t pop(TraceState& s) {
     return link;
 }
 
+// Shared-memory copy of the first inner nodes (the builder puts the top levels
+// there, breadth-first); links below `n` are read from it.
+struct StagedNodes {
+    const float4* smem;
+    uint32_t n;
+};
+
 // One round: inner nodes down to the next leaf, then that leaf.  On return
 // s.link is the next link to visit, or kDone.
-template <bool kNanCheck, bool kCount>
-RGR_DEV void trace_round_t(const SceneView& sc, TraceState& s, TraceCounters* cnt, uint32_t& err, uint64_t pol) {
+template <bool kNanCheck, bool kCount, bool kStaged>
+RGR_DEV void trace_round_t(const SceneView& sc, TraceState& s, TraceCounters* cnt, uint32_t& err, uint64_t pol,
+                           StagedNodes st) {
     const float4* __restrict__ nodes = sc.nodes;
     uint32_t link = s.link;
     while (!(link & kLeafFlag)) {
-        const float4* np = nodes + 4 * (size_t)link;
-        const float4 q0 = ld_keep(np + 0, pol);
-        const float4 q1 = ld_keep(np + 1, pol);
-        const float4 q2 = ld_keep(np + 2, pol);
-        const float4 q3 = ld_keep(np + 3, pol);
+        float4 q0, q1, q2, q3;
+        if (kStaged && link < st.n) {
+            const float4* np = st.smem + 4 * link;
+            q0 = np[0];
+            q1 = np[1];
+            q2 = np[2];
+            q3 = np[3];
+        } else {
+            const float4* np = nodes + 4 * (size_t)link;
+            q0 = ld_keep(np + 0, pol);
+            q1 = ld_keep(np + 1, pol);
+            q2 = ld_keep(np + 2, pol);
+            q3 = ld_keep(np + 3, pol);
+        }
         if (kCount) cnt->nodes++;
         float L0, L1, R0, R1;
         bool L = slab<kNanCheck>(q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, s.ro, s.inv, s.tmin, L0, L1);
@@ -217,12 +234,13 @@ RGR_DEV void trace_round_t(const SceneView& sc, TraceState& s, TraceCounters* cn
     s.link = link;
 }
 
-template <bool kCount>
-RGR_DEV void trace_round(const SceneView& sc, TraceState& s, TraceCounters* cnt, uint32_t& err, uint64_t pol) {
+template <bool kCount, bool kStaged = false>
+RGR_DEV void trace_round(const SceneView& sc, TraceState& s, TraceCounters* cnt, uint32_t& err, uint64_t pol,
+                         StagedNodes st = StagedNodes{nullptr, 0u}) {
     if (s.nan_free) {
-        trace_round_t<false, kCount>(sc, s, cnt, err, pol);
+        trace_round_t<false, kCount, kStaged>(sc, s, cnt, err, pol, st);
     } else {
-        trace_round_t<true, kCount>(sc, s, cnt, err, pol);
+        trace_round_t<true, kCount, kStaged>(sc, s, cnt, err, pol, st);
     }
 }
 

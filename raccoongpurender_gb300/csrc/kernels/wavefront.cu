@@ -761,7 +761,78 @@ RGR_DEV uint32_t guide_emit_samples(const GuideRenderD& gd, uint32_t slot, f3 L)
     return offered;
 }
 
-template <bool kGuided>
+// extension_ray_cast (extension_ray_cast_stackless.cl:202-246) of the slots
+// this bounce shaded — the items of the seven queues, concatenated as the
+// shading kernel reads them, less the new-path slots it retired — by
+// persistent warps that hand finished lanes the next items (one atomic per
+// refill per warp), as the closest-hit service kernel does with rays.  Runs
+// between the shading kernel and the queue resets.  A hit writes Ng and the
+// primitive into P.ng, t into P.ro.w and clears the volume hit in P.rd.w; a
+// miss leaves P.ng.w at the -1 the shading stage wrote.  Each slot may belong
+// to another request (scene).
+__global__ void __launch_bounds__(256, 5) k_trace_paths(PathsView P, QueueView Q, RenderParams rp,
+                                                         unsigned long long* next, int refill) {
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const unsigned lt = (1u << lane) - 1u;
+    const uint64_t pol = l2_evict_last_policy();
+    uint32_t off[kNumQueues + 1];
+    off[0] = 0;
+#pragma unroll
+    for (int k = 0; k < kNumQueues; ++k) off[k + 1] = off[k] + Q.counts[k];
+    const uint32_t total = off[kNumQueues];
+    TraceState s;
+    const SceneView* scp = nullptr;
+    uint32_t slot = ~0u;  // ~0: idle
+    bool exhausted = false;
+    uint32_t err = 0;
+    for (;;) {
+        const unsigned idle = __ballot_sync(full, slot == ~0u);
+        if (!exhausted && (int)__popc(idle) >= refill) {
+            const uint32_t need = __popc(idle);
+            unsigned long long base = 0;
+            if (lane == 0) base = atomicAdd(next, (unsigned long long)need);
+            base = __shfl_sync(full, base, 0);
+            if (base + need >= total) exhausted = true;
+            if (slot == ~0u) {
+                const unsigned long long i = base + __popc(idle & lt);
+                if (i < total) {
+                    int k = 0;
+#pragma unroll
+                    for (int j = 1; j < kNumQueues; ++j) k += ((uint32_t)i >= off[j]) ? 1 : 0;
+                    const uint32_t r = Q.items[k][(uint32_t)i - off[k]];
+                    if (P.qid[r] != kQueueIdle) {
+                        slot = r;
+                        scp = &rp.reqs[P.req[r]].sc;
+                        const float4 ro4 = P.ro[r], rd4 = P.rd[r];
+                        trace_begin(*scp, s, xyz(ro4), xyz(rd4), ro4.w);
+                    }
+                }
+            }
+        }
+        if (__ballot_sync(full, slot != ~0u) == 0u) {
+            if (exhausted) break;
+            continue;
+        }
+        if (slot != ~0u) {
+            if (s.link != kDone) trace_round<false>(*scp, s, nullptr, err, pol);
+            if (s.link == kDone) {
+                if (s.prim >= 0) {
+                    const f3 ng = hit_normal(*scp, s.prim, s.ro, s.rd, s.tmin);
+                    P.ng[slot] = f4(ng, __int_as_float(s.prim));
+                    P.ro[slot] = f4(s.ro, s.tmin);
+                    P.rd[slot] = f4(s.rd, __int_as_float(-1));
+                }
+                slot = ~0u;
+            }
+        }
+    }
+    if (err) atomicOr(rp.err, err);
+}
+
+// kPreTraced: k_trace_paths has cast the extension rays of this bounce; the
+// kernel only runs the logic.  Otherwise each thread traces its slot first.
+template <bool kGuided, bool kPreTraced>
 __global__ void __launch_bounds__(128) k_trace_logic(PathsView P, QueueView Q, RenderParams rp) {
     const uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x;
     const bool live = slot < P.n && P.qid[slot] != kQueueIdle;
@@ -770,19 +841,26 @@ __global__ void __launch_bounds__(128) k_trace_logic(PathsView P, QueueView Q, R
     const int req = P.req[slot];
     const RequestD& rq = rp.reqs[req];
     const SceneView& sc = rq.sc;
-    float4 ro4 = P.ro[slot], rd4 = P.rd[slot];
-    f3 ro = xyz(ro4), rd = xyz(rd4);
-    float tmin = ro4.w;
+    const float4 rd4 = P.rd[slot];
+    f3 rd = xyz(rd4);
     int32_t hv = __float_as_int(rd4.w);
     uint32_t err = 0;
-    // extension_ray_cast (extension_ray_cast_stackless.cl:202-246)
-    int32_t hs = trace_closest<false>(sc, ro, rd, tmin, nullptr, err);
-    if (hs >= 0) {
-        f3 ng = hit_normal(sc, hs, ro, rd, tmin);
-        P.ng[slot] = f4(ng, __int_as_float(hs));
-        P.ro[slot] = f4(ro, tmin);
-        hv = -1;
-        P.rd[slot] = f4(rd, __int_as_float(-1));
+    int32_t hs;
+    if (kPreTraced) {
+        hs = __float_as_int(P.ng[slot].w);
+    } else {
+        // extension_ray_cast (extension_ray_cast_stackless.cl:202-246)
+        const float4 ro4 = P.ro[slot];
+        f3 ro = xyz(ro4);
+        float tmin = ro4.w;
+        hs = trace_closest<false>(sc, ro, rd, tmin, nullptr, err);
+        if (hs >= 0) {
+            f3 ng = hit_normal(sc, hs, ro, rd, tmin);
+            P.ng[slot] = f4(ng, __int_as_float(hs));
+            P.ro[slot] = f4(ro, tmin);
+            hv = -1;
+            P.rd[slot] = f4(rd, __int_as_float(-1));
+        }
     }
     // logic (logic.cl:27-190)
     float4 T4 = P.T[slot], L4 = P.L[slot];
@@ -996,11 +1074,32 @@ void launch_shade(const PathsView& p, const QueueView& q, const RenderParams& rp
     else
         k_shade<false><<<grid, 256, 0, st>>>(p, q, rp);
 }
-void launch_trace_logic(const PathsView& p, const QueueView& q, const RenderParams& rp, cudaStream_t st) {
-    if (rp.gd.lobes)
-        k_trace_logic<true><<<(p.n + 127) / 128, 128, 0, st>>>(p, q, rp);
-    else
-        k_trace_logic<false><<<(p.n + 127) / 128, 128, 0, st>>>(p, q, rp);
+void launch_trace_paths(const PathsView& p, const QueueView& q, const RenderParams& rp, const TraceShape& ts,
+                        cudaStream_t st) {
+    if (!ts.persistent) return;
+    cudaMemsetAsync(ts.counter, 0, sizeof(unsigned long long), st);
+    k_trace_paths<<<ts.grid, 256, 0, st>>>(p, q, rp, ts.counter, ts.refill);
+}
+
+void launch_trace_logic(const PathsView& p, const QueueView& q, const RenderParams& rp, const TraceShape& ts,
+                        cudaStream_t st) {
+    const unsigned nb = (p.n + 127) / 128;
+    if (ts.persistent) {
+        if (rp.gd.lobes)
+            k_trace_logic<true, true><<<nb, 128, 0, st>>>(p, q, rp);
+        else
+            k_trace_logic<false, true><<<nb, 128, 0, st>>>(p, q, rp);
+    } else if (rp.gd.lobes) {
+        k_trace_logic<true, false><<<nb, 128, 0, st>>>(p, q, rp);
+    } else {
+        k_trace_logic<false, false><<<nb, 128, 0, st>>>(p, q, rp);
+    }
+}
+
+int trace_paths_max_blocks_per_sm() {
+    int nb = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_trace_paths, 256, 0);
+    return nb;
 }
 void launch_readback(int fmt, const double* accum, uint32_t npix, void* out, cudaStream_t st) {
     k_readback<<<(npix + 255) / 256, 256, 0, st>>>(fmt, accum, npix, out);

@@ -131,21 +131,41 @@ struct RenderParams {
 void launch_init(const PathsView& p, const QueueView& q, uint32_t seed_offset, cudaStream_t st);
 void launch_compact_new(const PathsView& p, const QueueView& q, cudaStream_t st);
 void launch_shade(const PathsView& p, const QueueView& q, const RenderParams& rp, int grid, cudaStream_t st);
-void launch_trace_logic(const PathsView& p, const QueueView& q, const RenderParams& rp, cudaStream_t st);
+// How a bounce casts its extension rays: persistent = a separate persistent
+// closest-hit kernel over the slots just shaded (refilling warps, `grid`
+// CTAs, `counter` a device word it may use; launch_trace_paths, between the
+// shading kernel and the queue resets), then the logic kernel; otherwise one
+// kernel traces and runs the logic per slot (launch_trace_paths does nothing).
+struct TraceShape {
+    bool persistent;
+    int refill;
+    int grid;
+    unsigned long long* counter;
+};
+void launch_trace_paths(const PathsView& p, const QueueView& q, const RenderParams& rp, const TraceShape& ts,
+                        cudaStream_t st);
+void launch_trace_logic(const PathsView& p, const QueueView& q, const RenderParams& rp, const TraceShape& ts,
+                        cudaStream_t st);
+int trace_paths_max_blocks_per_sm();
 void launch_readback(int fmt, const double* accum, uint32_t npix, void* dev_out, cudaStream_t st);
 void launch_sum_counts(const double* accum, uint32_t npix, unsigned long long* out, cudaStream_t st);
 void launch_debug_slots(const PathsView& p, uint32_t* out, cudaStream_t st);
 void launch_accum_add(double* dst, const double* src, uint32_t npix, cudaStream_t st);
 void launch_merge_intermediate(void* a, const void* b, uint32_t n, cudaStream_t st);
 // trace.cu
+// stage: inner nodes (the breadth-first top of the tree) each CTA copies to
+// shared memory, 0..kMaxStagedNodes
+constexpr uint32_t kMaxStagedNodes = 1024;
 void launch_trace_rays(const SceneView& sc, const float* ox, const float* oy, const float* oz, const float* dx,
                        const float* dy, const float* dz, const float* tmax, uint64_t n, int32_t* prim, float* t,
-                       float* ng, uint32_t* err, unsigned long long* counter, int refill, int grid, cudaStream_t st);
+                       float* ng, uint32_t* err, unsigned long long* counter, int refill, int grid, uint32_t stage,
+                       cudaStream_t st);
 void launch_trace_rays_counts(const SceneView& sc, const float* ox, const float* oy, const float* oz, const float* dx,
                               const float* dy, const float* dz, const float* tmax, uint64_t n, int32_t* prim,
                               float* t, uint32_t* nodes, uint32_t* prims, uint32_t* err, unsigned long long* counter,
                               int grid, cudaStream_t st);
-int trace_rays_max_blocks_per_sm();
+// resident 256-thread blocks per SM of the closest-hit kernel with `stage` staged nodes
+int trace_rays_max_blocks_per_sm(uint32_t stage = 0);
 
 }  // namespace dev
 }  // namespace rgr

@@ -46,6 +46,8 @@ struct alignas(16) NodeD {
 };
 static_assert(sizeof(NodeD) == 64, "NodeD must be 64 bytes");
 constexpr uint32_t kLeafFlag = 0x80000000u;
+// inner nodes placed first, in breadth-first order, for shared-memory staging
+constexpr size_t kStagedNodes = 1024;
 constexpr uint32_t kLeafFirstMask = 0x0fffffffu;
 inline uint32_t make_leaf_link(uint32_t first, uint32_t count) {
     return kLeafFlag | ((count - 1u) << 28) | first;

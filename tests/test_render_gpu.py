@@ -103,3 +103,23 @@ def test_backside_env_pdf_fix(rg, po):
     assert compare_slots(gs, os_) == {}
     assert (ga[:, 3] == oa[:, 3]).all()
     np.testing.assert_allclose(ga[:, :3], oa[:, :3], rtol=1e-12, atol=1e-300)
+
+
+def test_persistent_and_fused_trace_agree(rg, po):
+    """The persistent refilling trace kernel + logic and the fused per-slot
+    trace/logic kernel leave bit-identical slot state on the mixed scene."""
+    mesh, env, camd = scenes.mixed_scene(level=4, seed=3)
+    sm, _ = build(mesh, env=env)
+    cam = camera(camd, 96, 54)
+    out = []
+    for persistent in (True, False):
+        lane = rg.WavefrontLane(0, 1 << 14)
+        lane.set_render_trace(persistent, 24)
+        lane.setup(sm)
+        lane.initialize(cam, rg.render_config())
+        lane.step(20)
+        lane.synchronize()
+        out.append((lane.debug_slots(), lane.accumulation()))
+    for k in out[0][0]:
+        assert (np.asarray(out[0][0][k]).view(np.uint32) == np.asarray(out[1][0][k]).view(np.uint32)).all(), k
+    np.testing.assert_allclose(out[0][1], out[1][1], rtol=1e-12, atol=1e-300)

@@ -78,3 +78,16 @@ def test_empty_scene(rg):
     prim, t = lane.trace_closest(rays)
     assert (prim == -1).all()
     assert (bits(t) == bits(rays.tmax)).all()
+
+
+@pytest.mark.parametrize("stage", [1, 100, 1024])
+def test_staged_top_levels(rg, po, stage):
+    """Top BVH levels read from shared memory give the same hits."""
+    mesh = scenes.displaced_icosphere(6, seed=7)
+    sm, osc = build(mesh)
+    lane = rg.WavefrontLane(0, 1024)
+    lane.setup(sm)
+    lane.set_trace_staging(stage)
+    prim_rays, rnd = scenes.closest_hit_rays(mesh, res=128, n_random=32768, seed=4)
+    _check(lane, osc, prim_rays)
+    _check(lane, osc, rnd)
