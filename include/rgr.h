@@ -293,6 +293,11 @@ typedef struct rgr_guide_config {
                                 envmap sampling stay; guiding it doubles the largest per-vertex weight) */
     uint32_t train_interval; /* bounces per training iteration (1): samples of all of them feed it */
     uint32_t max_iterations; /* stop training (and recording samples) after this many iterations (0: never) */
+    int32_t inference_kernel; /* RGR_GUIDE_MMA_SYNC (default): warp-level mma.sync with the whole
+                                 network in register fragments; RGR_GUIDE_TCGEN05: tcgen05.mma with
+                                 TMEM accumulators, one thread per row (1.9x slower for this
+                                 64-wide network: the per-row scalar work, not the MMA, bounds it) */
+    uint32_t reserved;
     uint64_t seed;           /* weight initialisation (1) */
 } rgr_guide_config;
 typedef struct rgr_guide_stats {
@@ -300,6 +305,8 @@ typedef struct rgr_guide_stats {
     float last_loss;         /* loss of the last iteration (sum over its samples of -w log q, w normalised) */
     float accept;            /* probability with which a finished record is offered as a sample */
 } rgr_guide_stats;
+#define RGR_GUIDE_TCGEN05 0
+#define RGR_GUIDE_MMA_SYNC 1
 #define RGR_GUIDE_LAYERS 5
 #define RGR_GUIDE_WIDTH 64   /* every layer is stored as a zero-padded 64 x 64 W[in][out] */
 
@@ -329,6 +336,8 @@ int rgr_guide_infer_device(rgr_guide* g, const float* rows, uint32_t n, float* o
 int rgr_guide_train_device(rgr_guide* g, const float* samples, uint32_t n, float weight_scale, int32_t apply_adam,
                            float* grads, float* loss, void* stream);
 int rgr_guide_stats_get(rgr_guide* g, rgr_guide_stats* st);
+/* RGR_OK, or RGR_E_CUDA when a tensor-core wait of the guide's kernels timed out */
+int rgr_guide_check(rgr_guide* g);
 /* losses of the last min(max, iterations) iterations, oldest first; *count receives how many */
 int rgr_guide_loss_history(rgr_guide* g, float* out, uint32_t max, uint32_t* count);
 /* the training samples of the last iteration of a guided render (16 floats each, as

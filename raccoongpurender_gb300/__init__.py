@@ -78,7 +78,10 @@ class rgr_guide_config(C.Structure):
     _fields_ = [("learning_rate", C.c_float), ("beta1", C.c_float), ("beta2", C.c_float), ("epsilon", C.c_float),
                 ("batch_samples", C.c_uint32), ("guide_fraction", C.c_float), ("train", C.c_int32),
                 ("guide_volumes", C.c_int32), ("train_interval", C.c_uint32), ("max_iterations", C.c_uint32),
-                ("seed", C.c_uint64)]
+                ("inference_kernel", C.c_int32), ("reserved", C.c_uint32), ("seed", C.c_uint64)]
+
+
+GUIDE_TCGEN05, GUIDE_MMA_SYNC = 0, 1  # rgr_guide_config.inference_kernel
 
 
 class rgr_guide_stats(C.Structure):
@@ -167,6 +170,7 @@ _SIGS = {
     "rgr_guide_stats_get": (C.c_int, [C.c_void_p, C.c_void_p]),
     "rgr_guide_loss_history": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p]),
     "rgr_guide_last_batch": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p]),
+    "rgr_guide_check": (C.c_int, [C.c_void_p]),
 }
 
 _lib = None
@@ -562,6 +566,10 @@ class Guide:
                                                 grads_ptr or None, C.byref(loss), stream or None),
                "rgr_guide_train_device")
         return loss.value
+
+    def check(self) -> None:
+        """Raise if a tensor-core wait of the guide's kernels timed out."""
+        _check(self._lib.rgr_guide_check(self._h), "rgr_guide_check")
 
     def stats(self) -> dict:
         st = rgr_guide_stats()

@@ -25,8 +25,8 @@ BUILD = ROOT / "_build" / "rgr"
 LIB_DIR = PKG / "_lib"
 LIB = LIB_DIR / "librgr.so"
 
-CUDA_SOURCES = ["kernels/trace.cu", "kernels/wavefront.cu", "kernels/guide_mlp.cu", "host/context.cu", "host/noalloc.cu",
-                "host/guide.cu"]
+CUDA_SOURCES = ["kernels/trace.cu", "kernels/wavefront.cu", "kernels/guide_mlp.cu", "kernels/guide_tc.cu",
+                "host/context.cu", "host/noalloc.cu", "host/guide.cu"]
 CXX_SOURCES = ["host/scene.cpp", "host/bvh_build.cpp", "host/envmap_tables.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

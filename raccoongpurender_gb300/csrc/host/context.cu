@@ -271,7 +271,7 @@ struct rgr_context {
     // train_now: a guided render ends a training interval with this bounce
     int step_launches(cudaStream_t st, bool train_now = true) {
         launch_compact_new(pv, qv, st);
-        if (guided) launch_guide_infer_paths(guide->view, pv, qv, rp.gd, guide_infer_grid(num_sms), st);
+        if (guided) guide->infer_paths(pv, qv, rp.gd, st);
         launch_shade(pv, qv, rp, shade_grid, st);
         launch_trace_paths(pv, qv, rp, render_trace, st);
         RGR_CUDA(cudaMemsetAsync(qv.counts + 1, 0, sizeof(uint32_t) * (kNumQueues - 1), st));

@@ -6,6 +6,7 @@
 #include <cmath>
 #include <cstring>
 #include <new>
+#include <string>
 #include <vector>
 
 #include "guide_host.h"
@@ -18,6 +19,7 @@ namespace {
 // counters buffer layout (bytes)
 constexpr size_t kCtrCount = 0, kCtrWsum = 4, kCtrCand = 8, kCtrAccept = 16, kCtrIter = 20, kCtrLast = 24;
 constexpr size_t kCtrTest = 32;  // the test stream's count/wsum/cand/accept at the same offsets from here
+constexpr size_t kCtrErr = 60;   // error bits of the tensor-core kernels
 constexpr size_t kCtrBytes = 64;
 
 uint64_t splitmix64(uint64_t& x) {
@@ -73,6 +75,7 @@ int rgr_guide::init(const rgr_guide_config& c) {
     AL(samples, 64 * (size_t)cfg.batch_samples);
     AL(counters, kCtrBytes);
     AL(loss_hist, 4 * kLossHist);
+    AL(wtsw, kGuideWtBytes);
 #undef AL
     GuideView& g = view;
     g.w = w.as<float>();
@@ -83,6 +86,7 @@ int rgr_guide::init(const rgr_guide_config& c) {
     g.m = m.as<float>();
     g.v = v.as<float>();
     g.loss = loss.as<float>();
+    g.wt_sw = wtsw.as<unsigned char>();
     for (int k = 0; k < 3; ++k) {
         g.params.lo[k] = -1.0f;
         g.params.inv_ext[k] = 0.5f;
@@ -128,6 +132,15 @@ int rgr_guide::set_bounds(const float lo[3], const float hi[3]) {
     return RGR_OK;
 }
 
+uint32_t* rgr_guide::error_word() const { return reinterpret_cast<uint32_t*>(counters.as<unsigned char>() + kCtrErr); }
+
+void rgr_guide::infer_paths(const PathsView& p, const QueueView& q, const GuideRenderD& gd, cudaStream_t st) {
+    if (cfg.inference_kernel == RGR_GUIDE_TCGEN05)
+        launch_guide_infer_paths_tc(view, p, q, gd, guide_tc_grid(num_sms), error_word(), st);
+    else
+        launch_guide_infer_paths(view, p, q, gd, guide_infer_grid(num_sms), st);
+}
+
 int rgr_guide::train_launches(cudaStream_t st) {
     if (cfg.train) {
         launch_guide_train(view, train.samples, train.count, train.cap, train.wsum, 1.0f, num_sms, st);
@@ -152,6 +165,8 @@ void rgr_guide_config_default(rgr_guide_config* c) {
     c->guide_volumes = 0;
     c->train_interval = 1;
     c->max_iterations = 0;
+    c->inference_kernel = RGR_GUIDE_MMA_SYNC;
+    c->reserved = 0;
     c->seed = 1;
 }
 
@@ -159,7 +174,8 @@ static bool valid_config(const rgr_guide_config& c) {
     return c.learning_rate >= 0.0f && std::isfinite(c.learning_rate) && c.beta1 >= 0.0f && c.beta1 < 1.0f &&
            c.beta2 >= 0.0f && c.beta2 < 1.0f && c.epsilon > 0.0f && c.batch_samples >= 64 &&
            c.batch_samples <= (1u << 24) && c.guide_fraction >= 0.0f && c.guide_fraction <= 1.0f &&
-           c.train_interval >= 1 && c.train_interval <= 64;
+           c.train_interval >= 1 && c.train_interval <= 64 &&
+           (c.inference_kernel == RGR_GUIDE_TCGEN05 || c.inference_kernel == RGR_GUIDE_MMA_SYNC);
 }
 
 int rgr_guide_create(rgr_guide** out, int32_t device, const rgr_guide_config* cfg) {
@@ -178,6 +194,7 @@ int rgr_guide_create(rgr_guide** out, int32_t device, const rgr_guide_config* cf
     if (device < 0 || device >= ndev) return RGR_E_INVALID;
     RGR_CUDA(cudaSetDevice(device));
     RGR_CUDA((cudaError_t)guide_kernel_attributes());
+    RGR_CUDA((cudaError_t)guide_tc_attributes());
     rgr_guide* g = new (std::nothrow) rgr_guide();
     if (!g) return RGR_E_OOM;
     g->device = device;
@@ -235,11 +252,17 @@ int rgr_guide_set_weights(rgr_guide* g, const float* w, const float* b) {
     }
     std::vector<uint16_t> hbf(kGuideWeights);
     for (int i = 0; i < kGuideWeights; ++i) hbf[i] = to_bf16(w[i]);
+    std::vector<unsigned char> hsw(kGuideWtBytes);
+    for (uint32_t l = 0; l < (uint32_t)kGuideLayers; ++l)
+        for (uint32_t in = 0; in < 64; ++in)
+            for (uint32_t out = 0; out < 64; ++out)
+                memcpy(&hsw[wt_sw_offset(l, in, out)], &hbf[(l * 64 + in) * 64 + out], 2);
     RGR_CUDA(cudaSetDevice(g->device));
     RGR_CUDA(cudaDeviceSynchronize());
     RGR_CUDA(cudaMemcpy(g->w.p, w, 4 * kGuideWeights, cudaMemcpyHostToDevice));
     RGR_CUDA(cudaMemcpy(g->b.p, b, 4 * kGuideBiases, cudaMemcpyHostToDevice));
     RGR_CUDA(cudaMemcpy(g->wbf.p, hbf.data(), 2 * kGuideWeights, cudaMemcpyHostToDevice));
+    RGR_CUDA(cudaMemcpy(g->wtsw.p, hsw.data(), kGuideWtBytes, cudaMemcpyHostToDevice));
     RGR_CUDA(cudaMemset(g->gW.p, 0, 4 * kGuideWeights));
     RGR_CUDA(cudaMemset(g->gb.p, 0, 4 * kGuideBiases));
     RGR_CUDA(cudaMemset(g->m.p, 0, 4 * kGuideParams));
@@ -256,8 +279,13 @@ int rgr_guide_infer_device(rgr_guide* g, const float* rows, uint32_t n, float* o
     if (!g || (n && (!rows || !out))) return RGR_E_INVALID;
     if (n == 0) return RGR_OK;
     RGR_CUDA(cudaSetDevice(g->device));
-    const int grid = (int)std::min<uint32_t>((n + 127) / 128, (uint32_t)guide_infer_grid(g->num_sms));
-    launch_guide_infer(g->view, rows, n, out, grid, (cudaStream_t)stream);
+    if (g->cfg.inference_kernel == RGR_GUIDE_TCGEN05) {
+        const int grid = (int)std::min<uint32_t>((n + 127) / 128, (uint32_t)guide_tc_grid(g->num_sms));
+        launch_guide_infer_tc(g->view, rows, n, out, grid, g->error_word(), (cudaStream_t)stream);
+    } else {
+        const int grid = (int)std::min<uint32_t>((n + 127) / 128, (uint32_t)guide_infer_grid(g->num_sms));
+        launch_guide_infer(g->view, rows, n, out, grid, (cudaStream_t)stream);
+    }
     RGR_CUDA(cudaGetLastError());
     return RGR_OK;
 }
@@ -290,6 +318,19 @@ int rgr_guide_train_device(rgr_guide* g, const float* samples, uint32_t n, float
     }
     RGR_CUDA(cudaStreamSynchronize(st));
     if (loss) *loss = hl;
+    return RGR_OK;
+}
+
+int rgr_guide_check(rgr_guide* g) {
+    if (!g) return RGR_E_INVALID;
+    RGR_CUDA(cudaSetDevice(g->device));
+    RGR_CUDA(cudaDeviceSynchronize());
+    uint32_t e = 0;
+    RGR_CUDA(cudaMemcpy(&e, g->error_word(), 4, cudaMemcpyDeviceToHost));
+    if (e) {
+        set_error("guide: a tensor-core wait timed out (error bits " + std::to_string(e) + ")");
+        return RGR_E_CUDA;
+    }
     return RGR_OK;
 }
 

@@ -12,7 +12,7 @@ struct rgr_guide {
     // network: FP32 master weights and biases, BF16 weights, gradients, Adam moments, loss
     rgr::DevBuf w, b, wbf, gW, gb, m, v, loss;
     // training stream: samples, counters, loss history
-    rgr::DevBuf samples, counters, loss_hist;
+    rgr::DevBuf samples, counters, loss_hist, wtsw;
     rgr::dev::GuideView view{};
     rgr::dev::GuideTrainD train{};  // the render's stream (counter bytes 0..27)
     rgr::dev::GuideTrainD test{};   // rgr_guide_train_device's (bytes 32..59; shares iter)
@@ -20,6 +20,10 @@ struct rgr_guide {
 
     int init(const rgr_guide_config& c);
     int set_bounds(const float lo[3], const float hi[3]);
+    // the bounce's inference launch (tcgen05 or mma.sync kernel, per cfg)
+    void infer_paths(const rgr::dev::PathsView& p, const rgr::dev::QueueView& q, const rgr::dev::GuideRenderD& gd,
+                     cudaStream_t st);
+    uint32_t* error_word() const;
     // the launches that follow the trace/logic kernel of a guided render on the
     // bounces that end a training interval: train, Adam, reset the stream
     int train_launches(cudaStream_t st);

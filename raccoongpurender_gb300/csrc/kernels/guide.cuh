@@ -40,6 +40,8 @@ struct GuideView {
     float* w;              // FP32 master weights, kGuideWeights
     float* b;              // FP32 biases, kGuideBiases
     __nv_bfloat16* wbf;    // BF16 copy of w that the tensor cores read
+    unsigned char* wt_sw;  // the BF16 weights as the tcgen05 kernel stages them: per layer W^T
+                           // (64 output rows x 64 inputs, K-major, 128-byte swizzle), 8 KB each
     float* gW;             // gradient accumulators (zeroed by Adam)
     float* gb;
     float* m;              // Adam moments, kGuideParams each (weights then biases)
@@ -47,6 +49,19 @@ struct GuideView {
     float* loss;           // sum of sample losses of the last batch
     GuideParams params;
 };
+
+constexpr uint32_t kGuideWtBytes = kGuideLayers * 64 * 128;
+
+// byte offset of 16-byte chunk c of row r in a K-major 128-byte-swizzled tile
+// (the chunk sits at position c ^ (r % 8) of its 128-byte line; 8-line groups
+// are 1024 bytes apart)
+__host__ __device__ __forceinline__ uint32_t sw128_offset(uint32_t r, uint32_t c) {
+    return (r >> 3) * 1024u + (r & 7u) * 128u + ((c ^ (r & 7u)) << 4);
+}
+// where weight W[l][in][out] lives in wt_sw
+__host__ __device__ __forceinline__ uint32_t wt_sw_offset(uint32_t l, uint32_t in, uint32_t out) {
+    return l * 8192u + sw128_offset(out, in >> 3) + (in & 7u) * 2u;
+}
 
 // ------------------------------------------------------------ vMF mixture
 // vMF density on the sphere, kappa / (2 pi (1 - e^{-2 kappa})) e^{kappa (c - 1)}
@@ -134,6 +149,16 @@ void launch_guide_adam(const GuideView& g, const uint32_t* count, const uint32_t
                        float beta2, float eps, cudaStream_t st);
 // after an iteration: advance *iter, log the loss, retune the acceptance, reset counters
 void launch_guide_finish(const GuideView& g, const GuideTrainD& t, cudaStream_t st);
+
+// tcgen05 / TMEM inference (guide_tc.cu): same results as the mma.sync kernels up
+// to FP32 accumulation order; a timed-out tensor-core wait sets bit 0 of *err
+size_t guide_tc_smem();
+int guide_tc_attributes();  // cudaError_t of opting the kernels into their shared memory
+int guide_tc_grid(int num_sms);
+void launch_guide_infer_tc(const GuideView& g, const float* rows, uint32_t n, float* out, int grid, uint32_t* err,
+                           cudaStream_t st);
+void launch_guide_infer_paths_tc(const GuideView& g, const PathsView& p, const QueueView& q, const GuideRenderD& gd,
+                                 int grid, uint32_t* err, cudaStream_t st);
 
 }  // namespace dev
 }  // namespace rgr

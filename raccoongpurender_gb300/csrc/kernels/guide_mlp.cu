@@ -385,9 +385,24 @@ struct SmemTrain {
     __nv_bfloat16 act[kLayers][kRows][kStride];  // input of layer l for the chunk's rows
     __nv_bfloat16 dy[kRows][kStride];            // gradient at the output of the current layer
     float gW[kLayers][kH][kH];                   // this CTA's dW; warp w owns input rows 16w..16w+15
-    float gb[kLayers][kH];
+    float gb[kTrainWarps][kLayers][kH];          // db per warp (its rows), summed at the flush
     float loss[kTrainWarps];
 };
+
+// Column sums over a warp's 16 rows of a gradient in the fragment layout (lane
+// (g, q) holds columns 2q, 2q + 1 of an 8-column tile for rows g (p0) and
+// g + 8 (p1), as packed bf16): added to gb[col] by lanes 0..3.
+__device__ __forceinline__ void add_colsums(float* gb, int col, uint32_t p0, uint32_t p1, int lane) {
+    float s0 = bf16_lo(p0) + bf16_lo(p1), s1 = bf16_hi(p0) + bf16_hi(p1);
+    for (int o = 4; o < 32; o <<= 1) {
+        s0 += __shfl_xor_sync(0xffffffffu, s0, o);
+        s1 += __shfl_xor_sync(0xffffffffu, s1, o);
+    }
+    if (lane < 4) {
+        gb[col] += s0;
+        gb[col + 1] += s1;
+    }
+}
 
 // samples: 16 floats each (x, n, wo, wi, weight); loss weight = weight * scale / wsum
 __global__ void __launch_bounds__(32 * kTrainWarps) k_guide_train(GuideView gv, const float* __restrict__ samples,
@@ -404,7 +419,7 @@ __global__ void __launch_bounds__(32 * kTrainWarps) k_guide_train(GuideView gv, 
     }
     load_weights(S.W, S.b, gv);
     for (int i = threadIdx.x; i < kLayers * kH * kH; i += blockDim.x) (&S.gW[0][0][0])[i] = 0.0f;
-    for (int i = threadIdx.x; i < kLayers * kH; i += blockDim.x) (&S.gb[0][0])[i] = 0.0f;
+    for (int i = threadIdx.x; i < kTrainWarps * kLayers * kH; i += blockDim.x) (&S.gb[0][0][0])[i] = 0.0f;
     if (threadIdx.x < kTrainWarps) S.loss[threadIdx.x] = 0.0f;
     __syncthreads();
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -435,17 +450,20 @@ __global__ void __launch_bounds__(32 * kTrainWarps) k_guide_train(GuideView gv, 
         forward_frag(a, S.W, S.b, lane, o, reinterpret_cast<__nv_bfloat16(*)[kRows][kStride]>(&S.act[0][r0]));
         // ---- loss gradient at the output, in the fragment layout
         float lossv = 0.0f;
+        uint32_t gp[2][kOutTiles];  // the output gradient, packed bf16, per row half
         for (int h = 0; h < 2; ++h) {
             float gr[kOutTiles][2];
             const float lh = loss_grad_quad(o, h, dir[h][0], dir[h][1], dir[h][2], wt[h], gr);
             const bool live = wt[h] > 0.0f;
             if (live && q == 0) lossv += lh;
-            for (int f = 0; f < kOutTiles; ++f)
-                *reinterpret_cast<uint32_t*>(&S.dy[r0 + gq + 8 * h][8 * f + 2 * q]) =
-                    live ? pack_bf16(gr[f][0], gr[f][1]) : 0u;
+            for (int f = 0; f < kOutTiles; ++f) {
+                gp[h][f] = live ? pack_bf16(gr[f][0], gr[f][1]) : 0u;
+                *reinterpret_cast<uint32_t*>(&S.dy[r0 + gq + 8 * h][8 * f + 2 * q]) = gp[h][f];
+            }
             for (int f = kOutTiles; f < 8; ++f)
                 *reinterpret_cast<uint32_t*>(&S.dy[r0 + gq + 8 * h][8 * f + 2 * q]) = 0u;
         }
+        for (int f = 0; f < kOutTiles; ++f) add_colsums(S.gb[warp][kLayers - 1], 8 * f + 2 * q, gp[0][f], gp[1][f], lane);
         for (int off = 16; off > 0; off >>= 1) lossv += __shfl_xor_sync(0xffffffffu, lossv, off);
         if (lane == 0) S.loss[warp] += lossv;
         __syncthreads();
@@ -475,12 +493,7 @@ __global__ void __launch_bounds__(32 * kTrainWarps) k_guide_train(GuideView gv, 
                     S.gW[l][16 * warp + gq + 8][8 * j + 2 * q + 1] += dw[j][3];
                 }
             }
-            // db[l] += column sums of dy
-            if (threadIdx.x < kH) {
-                float s = 0.0f;
-                for (int r = 0; r < kRows; ++r) s += __bfloat162float(S.dy[r][threadIdx.x]);
-                S.gb[l][threadIdx.x] += s;
-            }
+            // (db[l], the column sums of this dy, was added when dy was formed)
             if (l == 0) break;
             // dx = dy W^T (B operand (k = out, n = in) read from W[in][out]), masked by ReLU'
             float dx[8][4];
@@ -505,8 +518,10 @@ __global__ void __launch_bounds__(32 * kTrainWarps) k_guide_train(GuideView gv, 
                 const float v1 = bf16_hi(m0) > 0.0f ? dx[j][1] : 0.0f;
                 const float v2 = bf16_lo(m1) > 0.0f ? dx[j][2] : 0.0f;
                 const float v3 = bf16_hi(m1) > 0.0f ? dx[j][3] : 0.0f;
-                *reinterpret_cast<uint32_t*>(&S.dy[r0 + gq][c]) = pack_bf16(v0, v1);
-                *reinterpret_cast<uint32_t*>(&S.dy[r0 + gq + 8][c]) = pack_bf16(v2, v3);
+                const uint32_t p0 = pack_bf16(v0, v1), p1 = pack_bf16(v2, v3);
+                *reinterpret_cast<uint32_t*>(&S.dy[r0 + gq][c]) = p0;
+                *reinterpret_cast<uint32_t*>(&S.dy[r0 + gq + 8][c]) = p1;
+                add_colsums(S.gb[warp][l - 1], c, p0, p1, lane);
             }
             __syncthreads();
         }
@@ -518,7 +533,8 @@ __global__ void __launch_bounds__(32 * kTrainWarps) k_guide_train(GuideView gv, 
         if (v != 0.0f) atomicAdd(gv.gW + i, v);
     }
     for (int i = threadIdx.x; i < kLayers * kH; i += blockDim.x) {
-        const float v = (&S.gb[0][0])[i];
+        float v = 0.0f;
+        for (int w = 0; w < kTrainWarps; ++w) v += (&S.gb[w][0][0])[i];
         if (v != 0.0f) atomicAdd(gv.gb + i, v);
     }
     if (threadIdx.x == 0) {
@@ -548,7 +564,12 @@ __global__ void k_guide_adam(GuideView g, const uint32_t* count, const uint32_t*
     const float nv = *p - lr * (mm / bc1) / (sqrtf(vv / bc2) + eps);
     *p = nv;
     *grad = 0.0f;
-    if (is_w) g.wbf[i] = __float2bfloat16_rn(nv);
+    if (is_w) {
+        const __nv_bfloat16 h = __float2bfloat16_rn(nv);
+        g.wbf[i] = h;
+        const uint32_t l = (uint32_t)i / 4096u, in = ((uint32_t)i / 64u) % 64u, out = (uint32_t)i % 64u;
+        *reinterpret_cast<__nv_bfloat16*>(g.wt_sw + wt_sw_offset(l, in, out)) = h;
+    }
 }
 
 __global__ void k_guide_finish(GuideView g, GuideTrainD t) {

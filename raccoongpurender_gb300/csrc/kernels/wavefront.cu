@@ -730,35 +730,68 @@ RGR_DEV uint32_t mix32(uint32_t h) {  // murmur3 finaliser
 // combines with the BSDF (the network does not see the material).
 // Records are offered with the acceptance probability the last iteration set
 // (a hash of slot, record and iteration, not the path's RNG, so rendering is
-// unchanged) until `cap` samples are in.  Returns the records offered.
-RGR_DEV uint32_t guide_emit_samples(const GuideRenderD& gd, uint32_t slot, f3 L) {
+// unchanged) until `cap` samples are in.  Every lane of `active` calls it
+// (ending = its path ended and it records); the warp takes one atomic for the
+// sample count, one for the weight sum and one for the offered count.
+RGR_DEV void guide_emit_samples(const GuideRenderD& gd, uint32_t slot, f3 L, bool ending, unsigned active) {
     const GuideTrainD& tr = gd.train;
-    const uint32_t nr = min((uint32_t)gd.nrec[slot], (uint32_t)kGuideRecords);
-    if (nr == 0u) return 0u;
-    const float accept = *tr.accept;
-    const uint32_t it = *tr.iter;
-    uint32_t offered = 0;
-    for (uint32_t r = 0; r < nr; ++r) {
-        const float4* rec = gd.records + ((size_t)slot * kGuideRecords + r) * 5;
-        const float4 d = rec[3], e = rec[4];
-        const float lx = d.w > 0.0f ? (L.x - d.x) / d.w : 0.0f;
-        const float ly = e.x > 0.0f ? (L.y - d.y) / e.x : 0.0f;
-        const float lz = e.y > 0.0f ? (L.z - d.z) / e.y : 0.0f;
-        const float w = (0.2126f * lx + 0.7152f * ly + 0.0722f * lz) * e.z;
-        if (!(w > 0.0f) || !is_finite(w)) continue;
-        ++offered;
-        const uint32_t h = mix32(slot * 0x9e3779b1u ^ (r + 1u) * 0x85ebca77u ^ (it + 1u) * 0xc2b2ae3du);
-        if ((float)(h >> 8) * (1.0f / 16777216.0f) >= accept) continue;
-        const uint32_t idx = atomicAdd(tr.count, 1u);
-        if (idx >= tr.cap) continue;
-        float4* dst = reinterpret_cast<float4*>(tr.samples + 16 * (size_t)idx);
-        dst[0] = rec[0];  // x, n.x
-        dst[1] = rec[1];  // n.yz, wo.xy
-        dst[2] = rec[2];  // wo.z, wi
-        dst[3] = make_float4(w, 0.0f, 0.0f, 0.0f);
-        atomicAdd(tr.wsum, w);
+    const int lane = threadIdx.x & 31;
+    const uint32_t nr = ending ? min((uint32_t)gd.nrec[slot], (uint32_t)kGuideRecords) : 0u;
+    float w[kGuideRecords];
+    uint32_t take = 0, offered = 0;  // take: bit r = record r is accepted
+    if (nr) {
+        const float accept = *tr.accept;
+        const uint32_t it = *tr.iter;
+        for (uint32_t r = 0; r < (uint32_t)kGuideRecords; ++r) {
+            w[r] = 0.0f;
+            if (r >= nr) continue;
+            const float4* rec = gd.records + ((size_t)slot * kGuideRecords + r) * 5;
+            const float4 d = rec[3], e = rec[4];
+            const float lx = d.w > 0.0f ? (L.x - d.x) / d.w : 0.0f;
+            const float ly = e.x > 0.0f ? (L.y - d.y) / e.x : 0.0f;
+            const float lz = e.y > 0.0f ? (L.z - d.z) / e.y : 0.0f;
+            const float wr = (0.2126f * lx + 0.7152f * ly + 0.0722f * lz) * e.z;
+            if (!(wr > 0.0f) || !is_finite(wr)) continue;
+            ++offered;
+            const uint32_t h = mix32(slot * 0x9e3779b1u ^ (r + 1u) * 0x85ebca77u ^ (it + 1u) * 0xc2b2ae3du);
+            if ((float)(h >> 8) * (1.0f / 16777216.0f) >= accept) continue;
+            w[r] = wr;
+            take |= 1u << r;
+        }
     }
-    return offered;
+    // exclusive prefix of the accepted counts (0..3: two ballots) over the
+    // active lanes, which need not be contiguous
+    const uint32_t mine = __popc(take);
+    const unsigned b0 = __ballot_sync(active, mine & 1u), b1 = __ballot_sync(active, (mine >> 1) & 1u);
+    const unsigned lt = (1u << lane) - 1u;
+    const uint32_t total = __popc(b0) + 2u * __popc(b1);
+    const int leader = __ffs(active) - 1;
+    uint32_t base = 0;
+    if (lane == leader && total) base = atomicAdd(tr.count, total);
+    base = __shfl_sync(active, base, leader);
+    uint32_t idx = base + __popc(b0 & lt) + 2u * __popc(b1 & lt);
+    float wsum = 0.0f;
+    for (uint32_t r = 0; r < (uint32_t)kGuideRecords; ++r) {
+        if (!((take >> r) & 1u)) continue;
+        if (idx < tr.cap) {
+            const float4* rec = gd.records + ((size_t)slot * kGuideRecords + r) * 5;
+            float4* dst = reinterpret_cast<float4*>(tr.samples + 16 * (size_t)idx);
+            dst[0] = rec[0];  // x, n.x
+            dst[1] = rec[1];  // n.yz, wo.xy
+            dst[2] = rec[2];  // wo.z, wi
+            dst[3] = make_float4(w[r], 0.0f, 0.0f, 0.0f);
+            wsum += w[r];
+        }
+        ++idx;
+    }
+    // the weight sum, gathered lane by lane (the active lanes are not contiguous)
+    float wtot = 0.0f;
+    for (unsigned m = active; m; m &= m - 1u) wtot += __shfl_sync(active, wsum, __ffs(m) - 1);
+    offered = __reduce_add_sync(active, offered);
+    if (lane == leader) {
+        if (wtot > 0.0f) atomicAdd(tr.wsum, wtot);
+        if (offered) atomicAdd(tr.candidates, (unsigned long long)offered);
+    }
 }
 
 // extension_ray_cast (extension_ray_cast_stackless.cl:202-246) of the slots
@@ -904,16 +937,10 @@ __global__ void __launch_bounds__(128) k_trace_logic(PathsView P, QueueView Q, R
             atomicAdd(a + 3, 1.0);
         }
     }
-    if (kGuided) {
-        uint32_t offered = 0;
-        if (newPath && rp.gd.record && guide_training_open(rp.gd.train)) {
-            const float cl = rq.radiance_clamp;
-            if (is_finite(L.x) && is_finite(L.y) && is_finite(L.z) && L.x < cl && L.y < cl && L.z < cl)
-                offered = guide_emit_samples(rp.gd, slot, L);
-        }
-        offered = __reduce_add_sync(active, offered);
-        if ((int)(threadIdx.x & 31) == __ffs(active) - 1 && offered)
-            atomicAdd(rp.gd.train.candidates, (unsigned long long)offered);
+    if (kGuided && rp.gd.record && guide_training_open(rp.gd.train)) {
+        const float cl = rq.radiance_clamp;
+        const bool kept = is_finite(L.x) && is_finite(L.y) && is_finite(L.z) && L.x < cl && L.y < cl && L.z < cl;
+        guide_emit_samples(rp.gd, slot, L, newPath && kept, active);
     }
     P.T[slot] = f4(T, T4.w);
     P.L[slot] = f4(L, __uint_as_float(logic_i + 1));

@@ -34,14 +34,16 @@ def _rel(a, b):
     return float(np.linalg.norm(np.asarray(a, np.float64) - b) / max(np.linalg.norm(b), 1e-30))
 
 
-def test_forward_matches_oracle(rg):
+@pytest.mark.parametrize("kernel", ["tcgen05", "mma_sync"])
+def test_forward_matches_oracle(rg, kernel):
     torch = _torch()
-    g, W, b = _guide(rg)
+    g, W, b = _guide(rg, inference_kernel=rg.GUIDE_TCGEN05 if kernel == "tcgen05" else rg.GUIDE_MMA_SYNC)
     s = go.random_samples(3000, seed=11)
     rows = torch.from_numpy(s).cuda()
     out = torch.zeros((len(s), go.OUTPUTS), dtype=torch.float32, device="cuda")
     g.infer_device(rows.data_ptr(), len(s), out.data_ptr())
     torch.cuda.synchronize()
+    g.check()
     got = out.cpu().numpy()
     ref, _ = go.forward(W, b, go.encode(s[:, 0:9], LO, IE), bf16_round=True)
     exact, _ = go.forward(W, b, go.encode(s[:, 0:9], LO, IE), bf16_round=False)
@@ -146,3 +148,24 @@ def test_training_learns_a_direction_field(rg):
     assert last < 0.8, (first, last)
     hist = g.loss_history()
     assert len(hist) == 400 and hist[-20:].mean() < hist[:20].mean() - 1.0
+
+
+def test_tcgen05_and_mma_sync_agree(rg):
+    """The two inference kernels compute the same BF16 network; only the FP32
+    accumulation order differs.  Several tiles per CTA, a ragged last tile."""
+    torch = _torch()
+    W, b = go.init_weights(5)
+    s = go.random_samples(200_000 + 77, seed=14)
+    rows = torch.from_numpy(s).cuda()
+    outs = []
+    for k in (rg.GUIDE_TCGEN05, rg.GUIDE_MMA_SYNC):
+        g = rg.Guide(0, inference_kernel=k)
+        g.set_weights(W, b)
+        g.set_bounds(LO, HI)
+        out = torch.full((len(s), go.OUTPUTS), float("nan"), dtype=torch.float32, device="cuda")
+        g.infer_device(rows.data_ptr(), len(s), out.data_ptr())
+        torch.cuda.synchronize()
+        g.check()
+        outs.append(out.cpu().numpy())
+    assert np.isfinite(outs[0]).all() and np.isfinite(outs[1]).all()
+    assert _rel(outs[0], outs[1]) < 2e-3
