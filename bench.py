@@ -255,9 +255,9 @@ def guiding_bench(dev_index: int, w: int = 960, h: int = 540, spp: int = 256, re
     """Equal-time relMSE, guided vs plain, against a ref_spp FP64-accumulated
     plain render, at w x h: plain rendering at `spp` against guided rendering
     given the same wall time: "cold" (the guide starts untrained and trains
-    online on the render's own samples, inference and training inside the
-    time) and "warm" (the guide a cold run trained, frozen).  Medians over 3
-    seeds.  Scenes: the full-render glossy/volume scene (the 1.31M-triangle
+    online on the render's own samples for its first 120 iterations, then is
+    frozen; inference and training inside the time) and "warm" (the guide a
+    cold run trained, frozen).  Medians over 3 seeds.  Scenes: the full-render glossy/volume scene (the 1.31M-triangle
     sphere, ground, volume box, sky + sun) and the sky-lit room."""
     import raccoongpurender_gb300 as rg
     from raccoongpurender_gb300 import guiding, scenes
@@ -275,7 +275,7 @@ def guiding_bench(dev_index: int, w: int = 960, h: int = 540, spp: int = 256, re
         t0 = time.perf_counter()
         ref = guiding.render_mean(rg, sm, cam, spp=ref_spp, seed_offset=1 << 30, path_count=1 << 22)
         ref_s = time.perf_counter() - t0
-        r = guiding.equal_time(rg, sm, cam, ref, spp, path_count=1 << 22)
+        r = guiding.equal_time(rg, sm, cam, ref, spp, path_count=1 << 22, guide_kw=dict(max_iterations=120))
         r.update({"resolution": f"{w}x{h}", "reference_spp": ref_spp, "reference_s": round(ref_s, 2),
                   "triangles": int(mesh.ntris)})
         out[name] = r
