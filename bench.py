@@ -204,6 +204,45 @@ def batch_bench(dev_index: int, n: int = 32) -> dict:
             "setup_s": round(setup_s, 1)}
 
 
+def bvh_bench(dev_index: int, mesh, sets, stream: int, sah_build_s: float) -> dict:
+    """BVH construction of the closest-hit scene: the host binned-SAH builder
+    (all host threads) against the linear BVH built on the GPU (Morton codes,
+    radix tree, refit; host flattening into the renderer's layout), and the
+    closest-hit rate on each tree (same rays, same kernel)."""
+    import torch
+    import raccoongpurender_gb300 as rg
+    t0 = time.perf_counter()
+    sm = rg.SceneManager()
+    sm.addMesh(mesh)
+    t1 = time.perf_counter()
+    sm.buildBVH(max_leaf_size=4, builder=rg.BVH_LBVH_GPU, device=dev_index)
+    t2 = time.perf_counter()
+    sm2 = rg.SceneManager()
+    sm2.addMesh(mesh)
+    t3 = time.perf_counter()
+    sm2.buildBVH(max_leaf_size=4, builder=rg.BVH_LBVH_GPU, device=dev_index)  # warm (CUDA context, allocator)
+    t4 = time.perf_counter()
+    lane = rg.WavefrontLane(dev_index, 1024)
+    lane.setup(sm2)
+    st = torch.cuda.ExternalStream(stream)
+    for ptrs, n, pp, tp in sets:
+        lane.trace_closest_device(ptrs, n, pp, tp, 0, stream)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    reps = 5
+    for _ in range(reps):
+        for ptrs, n, pp, tp in sets:
+            lane.trace_closest_device(ptrs, n, pp, tp, 0, stream)
+    e1.record(st)
+    e1.synchronize()
+    rays = sum(n for _, n, _, _ in sets) * reps
+    info = sm2.info()
+    return {"sah_host_s": round(sah_build_s, 3), "lbvh_gpu_s": round(t4 - t3, 3),
+            "lbvh_gpu_first_call_s": round(t2 - t1, 3), "lbvh_mrays_s": round(rays / (e0.elapsed_time(e1) * 1e3), 1),
+            "lbvh_depth": int(info.depth), "lbvh_sah_cost": round(float(info.sah_cost), 2),
+            "lbvh_inner_nodes": int(info.num_inner_nodes)}
+
+
 def guide_kernels_bench(dev_index: int) -> dict:
     """The guiding network's kernels on 2^18 random samples: one training
     iteration (forward + loss + backward on the tensor cores, gradient flush,
@@ -472,6 +511,8 @@ def main() -> None:
         render = {"cornell_256_4spp": render_bench(local, "cornell"),
                   "mixed_1080p_64spp": render_bench(local, "mixed"),
                   "batch_32_requests": batch_bench(local)}
+    bvh = bvh_bench(local, mesh, [([a.data_ptr() for a in soa], n, prim.data_ptr(), t.data_ptr())
+                                  for soa, prim, t, n in sets], sptr, build_s) if not args.no_render else None
     guide = None
     if not args.no_guiding:
         guide = {"kernels": guide_kernels_bench(local), "equal_time": guiding_bench(local)}
@@ -494,7 +535,7 @@ def main() -> None:
                 "e2e": {"value": round(e2e_value, 1), "unit": "Mrays/s", "h2d_bytes_per_step": rays_per_step * 28,
                         "d2h_bytes_per_step": rays_per_step * 8},
                 "gpu_launches": 2 * args.steps, "roofline": roof, "cpu_baseline": cpu, "clocks": clocks,
-                "render": render, "guiding": guide}
+                "render": render, "bvh_build": bvh, "guiding": guide}
         print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()

@@ -56,7 +56,13 @@ typedef struct rgr_bvh_params {
     float intersect_cost;    /* SAH cost of one primitive test */
     int32_t max_depth;       /* <= 63: the reference traversal's 64-bit bit stack */
     int32_t num_threads;     /* host threads for the build (0 = all) */
+    int32_t builder;         /* RGR_BVH_SAH (default): binned SAH on the host threads;
+                                RGR_BVH_LBVH_GPU: linear BVH (Morton order, radix tree) on `device`,
+                                subtrees of at most max_leaf_size primitives collapsed into leaves */
+    int32_t device;          /* the GPU of RGR_BVH_LBVH_GPU */
 } rgr_bvh_params;
+#define RGR_BVH_SAH 0
+#define RGR_BVH_LBVH_GPU 1
 
 typedef struct rgr_scene_info {
     uint64_t num_triangles, num_spheres, num_vertices;
@@ -91,6 +97,13 @@ int rgr_scene_add_spheres(rgr_scene* s, const float* xyzr, uint64_t n, const rgr
    (common/share/envmap.hpp:160-242, alias_method.hpp:47-114).  Without an envmap the
    renderer selects BSDF sampling only (the reference requires one). */
 int rgr_scene_set_envmap(rgr_scene* s, const float* rgba, int32_t w, int32_t h, float clamp_max, float scale);
+/* Rebuild the scene's envmap tables with the selection weights and their FP64
+   normalisation computed on `device` (fixed-order reduction); the alias
+   pairing stays the reference's sequential one, on the host.  The tables
+   rgr_scene_set_envmap builds on the host follow the reference bit for bit;
+   these agree with them to FP64 rounding (a pdf may differ in its last bit,
+   and an alias pairing where a height lands on 1.0 exactly). */
+int rgr_scene_envmap_tables_gpu(rgr_scene* s, int32_t device);
 /* SceneManager::buildBVH (scene_manager.hpp:517-577): binned-SAH build, deterministic. */
 int rgr_scene_build_bvh(rgr_scene* s, const rgr_bvh_params* p);
 int rgr_scene_get_info(const rgr_scene* s, rgr_scene_info* info);

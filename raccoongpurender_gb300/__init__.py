@@ -48,7 +48,11 @@ class rgr_material(C.Structure):
 
 class rgr_bvh_params(C.Structure):
     _fields_ = [("max_leaf_size", C.c_int32), ("sah_bins", C.c_int32), ("traversal_cost", C.c_float),
-                ("intersect_cost", C.c_float), ("max_depth", C.c_int32), ("num_threads", C.c_int32)]
+                ("intersect_cost", C.c_float), ("max_depth", C.c_int32), ("num_threads", C.c_int32),
+                ("builder", C.c_int32), ("device", C.c_int32)]
+
+
+BVH_SAH, BVH_LBVH_GPU = 0, 1  # rgr_bvh_params.builder
 
 
 class rgr_scene_info(C.Structure):
@@ -118,6 +122,7 @@ _SIGS = {
     "rgr_scene_add_mesh": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p, C.c_uint64, C.c_void_p]),
     "rgr_scene_add_spheres": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p]),
     "rgr_scene_set_envmap": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_float, C.c_float]),
+    "rgr_scene_envmap_tables_gpu": (C.c_int, [C.c_void_p, C.c_int32]),
     "rgr_scene_build_bvh": (C.c_int, [C.c_void_p, C.c_void_p]),
     "rgr_scene_get_info": (C.c_int, [C.c_void_p, C.c_void_p]),
     "rgr_bvh_export_stackless": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p, C.c_uint64]),
@@ -289,9 +294,15 @@ class SceneManager:
             proc[..., :3] *= np.float32(scale)
         self.envmap = proc
 
+    def envmapTablesOnGPU(self, device: int = 0) -> None:
+        """Rebuild the envmap tables with FP64 weights and normalisation on the GPU."""
+        _check(self._lib.rgr_scene_envmap_tables_gpu(self._h, device), "rgr_scene_envmap_tables_gpu")
+
     def buildBVH(self, max_leaf_size: int = 4, sah_bins: int = 32, num_threads: int = 0,
-                 traversal_cost: float = 1.0, intersect_cost: float = 1.0) -> None:
-        """SceneManager::buildBVH (scene_manager.hpp:517-577)."""
+                 traversal_cost: float = 1.0, intersect_cost: float = 1.0, builder: int = 0,
+                 device: int = 0) -> None:
+        """SceneManager::buildBVH (scene_manager.hpp:517-577); builder BVH_LBVH_GPU
+        builds a linear BVH on the GPU instead of the host SAH tree."""
         p = rgr_bvh_params()
         self._lib.rgr_bvh_params_default(C.byref(p))
         p.max_leaf_size = max_leaf_size
@@ -299,6 +310,8 @@ class SceneManager:
         p.num_threads = num_threads
         p.traversal_cost = traversal_cost
         p.intersect_cost = intersect_cost
+        p.builder = builder
+        p.device = device
         _check(self._lib.rgr_scene_build_bvh(self._h, C.byref(p)), "rgr_scene_build_bvh")
 
     def info(self) -> rgr_scene_info:

@@ -275,6 +275,32 @@ struct Flattener {
     }
 };
 
+// The builder's tree from a GPU radix tree: child c >= 0 is internal node c,
+// c < 0 the single sorted primitive ~c; nodes covering at most `leaf`
+// primitives become leaves over their (contiguous) sorted range.
+BNode* lbvh_node(const LbvhTree& t, const PrimBox* boxes, int32_t c, int leaf) {
+    BNode* n = new BNode();
+    if (c < 0) {
+        const uint32_t k = (uint32_t)~c;
+        const PrimBox& pb = boxes[t.order[k]];
+        memcpy(n->lo, pb.lo, 12);
+        memcpy(n->hi, pb.hi, 12);
+        n->first = k;
+        n->count = 1;
+        return n;
+    }
+    memcpy(n->lo, &t.box[6 * (size_t)c], 12);
+    memcpy(n->hi, &t.box[6 * (size_t)c + 3], 12);
+    if (t.count[c] <= leaf) {
+        n->first = (uint32_t)t.first[c];
+        n->count = (uint32_t)t.count[c];
+        return n;
+    }
+    n->kid[0] = lbvh_node(t, boxes, t.left[c], leaf);
+    n->kid[1] = lbvh_node(t, boxes, t.right[c], leaf);
+    return n;
+}
+
 }  // namespace
 
 // Device-layout order for shared-memory staging: the first `k` inner nodes a
@@ -384,13 +410,33 @@ int build_bvh(rgr_scene* s, const rgr_bvh_params& params) {
     }
     std::vector<uint32_t> order(nprim);
     for (uint64_t i = 0; i < nprim; ++i) order[i] = (uint32_t)i;
-    Builder b;
-    b.prims = boxes.data();
-    b.order = order.data();
-    b.p = p;
-    int nth = p.num_threads > 0 ? p.num_threads : (int)std::max(1u, std::thread::hardware_concurrency());
-    b.spare_threads = nth - 1;
-    std::unique_ptr<BNode> root(b.build(0, (uint32_t)nprim, 0));
+    std::unique_ptr<BNode> root;
+    if (p.builder == RGR_BVH_LBVH_GPU && nprim >= 2) {
+        // Morton-order radix tree on the GPU; subtrees of <= max_leaf_size primitives become leaves
+        std::vector<float> b6(6 * nprim);
+        float clo[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, chi[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+        for (uint64_t i = 0; i < nprim; ++i) {
+            for (int k = 0; k < 3; ++k) {
+                b6[6 * i + k] = boxes[i].lo[k];
+                b6[6 * i + 3 + k] = boxes[i].hi[k];
+                clo[k] = std::min(clo[k], boxes[i].c[k]);
+                chi[k] = std::max(chi[k], boxes[i].c[k]);
+            }
+        }
+        LbvhTree t;
+        int r = lbvh_build_gpu(p.device, b6.data(), (uint32_t)nprim, clo, chi, t);
+        if (r != RGR_OK) return r;
+        order = t.order;
+        root.reset(lbvh_node(t, boxes.data(), 0, p.max_leaf_size));
+    } else {
+        Builder b;
+        b.prims = boxes.data();
+        b.order = order.data();
+        b.p = p;
+        int nth = p.num_threads > 0 ? p.num_threads : (int)std::max(1u, std::thread::hardware_concurrency());
+        b.spare_threads = nth - 1;
+        root.reset(b.build(0, (uint32_t)nprim, 0));
+    }
 
     Flattener f;
     f.order = order.data();

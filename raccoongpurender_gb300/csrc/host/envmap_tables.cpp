@@ -59,13 +59,24 @@ void build_table(const EnvTables& env, int kind, const std::vector<double>& frag
     for (double v : weight) total.add(v);
     double inv = 1.0 / total.get();
     std::vector<double> prob(n);
+    for (int i = 0; i < n; ++i) prob[i] = weight[i] * inv;
+    alias_from_probabilities(w, h, prob.data(), sr, pdf, height, alias);
+}
+
+}  // namespace
+
+// AliasMethod::prepare (alias_method.hpp:47-114) from normalised probabilities:
+// heights prob * n with Kahan compensation, the reference's two stacks, and the
+// pdf per solid angle.
+void alias_from_probabilities(int w, int h, const double* prob, const std::vector<double>& sr, float* pdf,
+                              float* height, int32_t* alias) {
+    const int n = w * h;
     std::vector<KahanD> hk(n);
     std::vector<int32_t> al(n, -1);
     std::vector<int> lower, upper;
     lower.reserve(n);
     upper.reserve(n);
     for (int i = 0; i < n; ++i) {
-        prob[i] = weight[i] * inv;
         hk[i].sum = prob[i] * n;
         hk[i].c = 0.0;
         if (hk[i].get() < 1.0) lower.push_back(i);
@@ -93,14 +104,12 @@ void build_table(const EnvTables& env, int kind, const std::vector<double>& frag
     }
 }
 
-}  // namespace
-
-int build_envmap_tables(EnvTables& env) {
-    const int w = env.w, h = env.h;
+namespace {
+// fragments and per-row solid angles (EnvmapCoordinateSystem, envmap.hpp:34-78)
+void envmap_geometry(int w, int h, std::vector<double>& frag, std::vector<double>& sr) {
     const size_t n = (size_t)w * h;
-    // fragments and per-row solid angles (EnvmapCoordinateSystem, envmap.hpp:34-78)
-    std::vector<double> frag(4 * n);
-    std::vector<double> sr(h);
+    frag.resize(4 * n);
+    sr.resize(h);
     const double phi_step = kTwoPi / w, theta_step = kPi / h;
     for (int y = 0; y < h; ++y) {
         double t0 = theta_step * y, t1 = theta_step * (y + 1);
@@ -114,6 +123,14 @@ int build_envmap_tables(EnvTables& env) {
         }
         sr[y] = ((std::cos(t0) - std::cos(t1)) * kTwoPi) / w;
     }
+}
+}  // namespace
+
+int build_envmap_tables(EnvTables& env) {
+    const int w = env.w, h = env.h;
+    const size_t n = (size_t)w * h;
+    std::vector<double> frag, sr;
+    envmap_geometry(w, h, frag, sr);
     env.frag.resize(4 * n);
     for (size_t i = 0; i < 4 * n; ++i) env.frag[i] = (float)frag[i];
     env.pdf.assign(7 * n, 0.0f);
@@ -122,6 +139,30 @@ int build_envmap_tables(EnvTables& env) {
     std::vector<std::thread> th;
     for (int k = 0; k < 7; ++k)
         th.emplace_back(build_table, std::cref(env), k, std::cref(frag), std::cref(sr), env.pdf.data() + k * n,
+                        env.height.data() + k * n, env.alias.data() + k * n);
+    for (auto& t : th) t.join();
+    return RGR_OK;
+}
+
+// The same tables with the selection weights and their FP64 normalisation
+// computed on the GPU (envmap_gpu.cu); the alias pairing, which is sequential,
+// stays on the host.
+int build_envmap_tables_gpu(EnvTables& env, int device) {
+    const int w = env.w, h = env.h;
+    const size_t n = (size_t)w * h;
+    std::vector<double> frag, sr;
+    envmap_geometry(w, h, frag, sr);
+    env.frag.resize(4 * n);
+    for (size_t i = 0; i < 4 * n; ++i) env.frag[i] = (float)frag[i];
+    std::vector<double> prob(7 * n);
+    int r = envmap_probabilities_gpu(device, env.rgba.data(), w, h, prob.data());
+    if (r != RGR_OK) return r;
+    env.pdf.assign(7 * n, 0.0f);
+    env.height.assign(7 * n, 0.0f);
+    env.alias.assign(7 * n, -1);
+    std::vector<std::thread> th;
+    for (int k = 0; k < 7; ++k)
+        th.emplace_back(alias_from_probabilities, w, h, prob.data() + k * n, std::cref(sr), env.pdf.data() + k * n,
                         env.height.data() + k * n, env.alias.data() + k * n);
     for (auto& t : th) t.join();
     return RGR_OK;

@@ -92,6 +92,8 @@ void rgr_bvh_params_default(rgr_bvh_params* p) {
     p->intersect_cost = 1.0f;
     p->max_depth = 63;
     p->num_threads = 0;
+    p->builder = RGR_BVH_SAH;
+    p->device = 0;
 }
 
 int rgr_scene_create(rgr_scene** out) {
@@ -196,6 +198,16 @@ int rgr_scene_set_envmap(rgr_scene* s, const float* rgba, int32_t w, int32_t h, 
         }
     }
     int st = build_envmap_tables(env);
+    if (st != RGR_OK) return st;
+    s->env = std::move(env);
+    return RGR_OK;
+}
+
+int rgr_scene_envmap_tables_gpu(rgr_scene* s, int32_t device) {
+    if (!s || device < 0) return RGR_E_INVALID;
+    if (!s->env.present) return RGR_E_STATE;
+    EnvTables env = s->env;
+    int st = build_envmap_tables_gpu(env, device);
     if (st != RGR_OK) return st;
     s->env = std::move(env);
     return RGR_OK;

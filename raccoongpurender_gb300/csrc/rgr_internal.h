@@ -75,6 +75,19 @@ struct Bvh {
     float bounds[6] = {0, 0, 0, 0, 0, 0};
 };
 
+// A linear BVH built on the GPU (bvh_gpu.cu): internal node i has children
+// left[i], right[i] (>= 0 internal node, < 0 leaf ~k = sorted primitive k),
+// covers sorted primitives [first[i], first[i] + count[i]) and has the box
+// box[6i .. 6i+5] (lo xyz, hi xyz); order[k] = primitive id; the root is 0.
+struct LbvhTree {
+    std::vector<uint32_t> order;
+    std::vector<int32_t> left, right, first, count;
+    std::vector<float> box;
+};
+// boxes: 6 floats per primitive (lo xyz, hi xyz); n >= 2
+int lbvh_build_gpu(int device, const float* boxes, uint32_t n, const float centroid_lo[3],
+                   const float centroid_hi[3], LbvhTree& out);
+
 // ---------------------------------------------------------------- envmap
 struct EnvTables {
     bool present = false;
@@ -86,6 +99,12 @@ struct EnvTables {
     std::vector<float> frag;      // 4*w*h
 };
 int build_envmap_tables(EnvTables& env);
+// the same tables, selection weights and FP64 normalisation on `device`
+int build_envmap_tables_gpu(EnvTables& env, int device);
+void alias_from_probabilities(int w, int h, const double* prob, const std::vector<double>& sr, float* pdf,
+                              float* height, int32_t* alias);
+// 7 x w x h normalised selection probabilities (FP64) of the envmap tables, on the GPU
+int envmap_probabilities_gpu(int device, const float* rgba, int w, int h, double* prob_out);
 
 }  // namespace rgr
 
