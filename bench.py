@@ -339,6 +339,57 @@ def cpu_baseline(mesh, sm, coherent, incoherent, sample: int = 1048576) -> dict:
             "sample": f"{sample} coherent + {sample} incoherent rays of the same workload, {dt:.2f} s"}
 
 
+def render_gpu_for_oracle(dev_index: int, which: str) -> dict:
+    """The GPU render the CPU leg compares with: Cornell 256^2, 4 spp, depth 5
+    (configuration 1, complete) and the mixed 1080p scene at 1 spp, depth 8
+    (configuration 3 at reduced spp); FP64 sums per pixel."""
+    import raccoongpurender_gb300 as rg
+    from raccoongpurender_gb300 import scenes
+    if which == "cornell":
+        mesh, env, camd = scenes.cornell_box(), None, scenes.cornell_camera(256, 256)
+        cfg = rg.render_config(spp=4, max_depth=5, dof=0.0)
+        pool = 1 << 18  # one slot per sample: the oracle, too, walks every slot each bounce
+    else:
+        mesh, env, camd = scenes.mixed_scene(level=8, seed=3)
+        cfg = rg.render_config(spp=1, max_depth=8, dof=0.0045)
+        pool = 1 << 21
+    sm = rg.SceneManager()
+    sm.addMesh(mesh)
+    if env is not None:
+        sm.setEnvmap(env)
+    sm.buildBVH(max_leaf_size=4)
+    cam = rg.camera_look_at(camd["eye"], camd["target"], camd["up"], camd["vfov"], camd["w"], camd["h"])
+    lane = rg.WavefrontLane(dev_index, pool)
+    lane.setup(sm)
+    lane.initialize(cam, cfg)
+    steps = lane.render_until_done(100000)
+    return dict(scene=sm, mesh=mesh, cam=cam, cfg=cfg, acc=lane.accumulation().reshape(-1, 4), steps=steps,
+                pool=pool)
+
+
+def cpu_render_baseline(gpu: dict, name: str) -> dict:
+    """The oracle's restatement of the reference render on all host threads,
+    timed, and the GPU image's largest per-pixel relative error against it."""
+    import numpy as np
+    from oracle import pyoracle as po
+    sm, mesh, cam, cfg = gpu["scene"], gpu["mesh"], gpu["cam"], gpu["cfg"]
+    osc = po.OracleScene.from_scene(sm, mesh.points, mesh.indices)
+    npix = cam.image_w * cam.image_h
+    threads = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    acc, _, _ = osc.render(po.camera_from_rgr(cam), po.config_from_rgr(cfg, npix), gpu["pool"], gpu["steps"] + 4,
+                           threads=threads, want_slots=False)
+    dt = time.perf_counter() - t0
+    g = gpu["acc"]
+    rel = np.abs(g[:, :3] - acc[:, :3]) / np.maximum(np.abs(acc[:, :3]), 1e-300)
+    rel[(acc[:, :3] == 0) & (g[:, :3] == 0)] = 0.0
+    paths = int(acc[:, 3].sum())
+    return {"value": round(paths / dt / 1e6, 3), "unit": "Mpaths/s", "cores": threads, "kind": "port",
+            "sample": f"{name}: {cam.image_w}x{cam.image_h}, {int(cfg.spp)} spp, {dt:.2f} s",
+            "gpu_image_vs_oracle": {"max_rel_err": float(rel.max()), "counts_equal": bool((g[:, 3] == acc[:, 3]).all()),
+                                    "pixels": npix}}
+
+
 def run_reference(args) -> None:
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -519,6 +570,8 @@ def main() -> None:
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cpu = cpu_baseline(mesh, sm, coherent, incoherent)
+        if not args.no_render:
+            cpu["render"] = {w: cpu_render_baseline(render_gpu_for_oracle(local, w), w) for w in ("cornell", "mixed")}
     info = sm.info()
     if rank == 0:
         line = {"metric": METRIC, "value": round(value, 1), "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
