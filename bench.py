@@ -39,6 +39,20 @@ WORKLOAD = "closest-hit: 1.31M-tri displaced icosphere, 4M coherent + 4M incoher
 METRIC = "closest-hit Mrays/s (1 GB300)"
 
 
+def measured_traffic() -> int | None:
+    """DRAM bytes per step of the closest-hit kernel from the committed ncu
+    summary (profiles/k_trace_rays_closest_hit_1.31M.md), or None."""
+    p = os.path.join(ROOT, "profiles", "k_trace_rays_closest_hit_1.31M.md")
+    try:
+        with open(p) as f:
+            for line in f:
+                if line.startswith("traffic_bytes_per_step = "):
+                    return int(line.split("=")[1])
+    except OSError:
+        pass
+    return None
+
+
 def measured_peaks() -> dict:
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -546,8 +560,11 @@ def main() -> None:
     coh_bytes = bytes_per_ray[0] * n_each
     inc_bytes = bytes_per_ray[1] * n_each
     achieved = (coh_bytes + inc_bytes) / ((coh_ms + inc_ms) * 1e-3) / 1e9
+    traffic = measured_traffic()
     roof = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peaks["hbm_gbs"], "unit": "GB/s",
-            "frac": round(achieved / peaks["hbm_gbs"], 4), "traffic": None,
+            "frac": round(achieved / peaks["hbm_gbs"], 4), "traffic": traffic,
+            "traffic_note": "DRAM bytes per step (both launches) from ncu, profiles/k_trace_rays_closest_hit_1.31M.md;"
+                            f" algorithmic bytes per step {int(coh_bytes + inc_bytes)}: the tree is L2-resident",
             "peak_source": peaks["source"] + " hbm_gbs",
             "per_set": {"coherent": {"ms": round(coh_ms, 3), "mrays_s": round(n_each / coh_ms / 1e3, 1),
                                      "nodes_per_ray": round(counts[0][0], 2), "prims_per_ray": round(counts[0][1], 2),
