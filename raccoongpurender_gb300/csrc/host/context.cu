@@ -173,6 +173,11 @@ struct rgr_context {
     std::string graph_exec_key;  // graph_key() when graph_exec was captured
     // ray-cast service buffers
     DevBuf trays[7], tprim, tt, tread, tcounter;
+    // rgr_trace_closest pipeline: two stream slots, each with its chunk's buffers
+    struct TraceSlot {
+        DevBuf rays[7], prim, t, counter, err;
+    } tslot[2];
+    cudaStream_t stream2 = nullptr;
     int trace_grid = 0;      // persistent traversal grid (SMs x resident blocks)
     int trace_refill = 24;   // refill a warp when this many lanes are idle (measured best of 1..32)
     int trace_blocks = 0;    // resident blocks per SM asked for (0: as many as fit)
@@ -188,6 +193,7 @@ struct rgr_context {
 
     ~rgr_context() {
         if (graph_exec) cudaGraphExecDestroy(graph_exec);
+        if (stream2) cudaStreamDestroy(stream2);
         if (stream) cudaStreamDestroy(stream);
     }
     // the resident path pool: state, queues, counters (WavefrontLane::setup, :451-522)
@@ -679,32 +685,54 @@ int rgr_trace_closest_counts_device(rgr_context* c, const rgr_ray_soa* rays, uin
     return RGR_OK;
 }
 
+// Host arrays in and out: the rays go in chunks of up to 2^20 alternating
+// over two streams, so that a chunk's copies overlap the traversal of the
+// previous one (with page-locked host memory; pageable memory still works,
+// its copies just do not overlap).
 int rgr_trace_closest(rgr_context* c, const rgr_ray_soa* rays, uint64_t n, int32_t* prim, float* t) {
     if (!c || !rays || !prim || !t) return RGR_E_INVALID;
     if (!c->scene.valid) return RGR_E_STATE;
     if (n == 0) return RGR_OK;
-    RGR_CUDA(cudaSetDevice(c->device));
-    cudaStream_t st = c->stream;
     const float* src[7] = {rays->ox, rays->oy, rays->oz, rays->dx, rays->dy, rays->dz, rays->tmax};
-    int r;
-    for (int k = 0; k < 7; ++k) {
+    for (int k = 0; k < 7; ++k)
         if (!src[k]) return RGR_E_INVALID;
-        if ((r = c->trays[k].upload(src[k], 4 * n, st)) != RGR_OK) return r;
+    RGR_CUDA(cudaSetDevice(c->device));
+    if (!c->stream2) RGR_CUDA(cudaStreamCreateWithFlags(&c->stream2, cudaStreamNonBlocking));
+    const uint64_t kChunk = 1ull << 20;
+    const uint64_t chunk = std::min(n, kChunk);
+    cudaStream_t streams[2] = {c->stream, c->stream2};
+    int r;
+    for (int s = 0; s < 2; ++s) {
+        rgr_context::TraceSlot& ts = c->tslot[s];
+        for (int k = 0; k < 7; ++k)
+            if ((r = ts.rays[k].alloc(4 * chunk)) != RGR_OK) return r;
+        if ((r = ts.prim.alloc(4 * chunk)) != RGR_OK || (r = ts.t.alloc(4 * chunk)) != RGR_OK ||
+            (r = ts.counter.alloc(8)) != RGR_OK || (r = ts.err.alloc(16)) != RGR_OK)
+            return r;
+        RGR_CUDA(cudaMemsetAsync(ts.err.p, 0, 4, streams[s]));
     }
-    if ((r = c->tprim.alloc(4 * n)) != RGR_OK) return r;
-    if ((r = c->tt.alloc(4 * n)) != RGR_OK) return r;
-    rgr_ray_soa d{c->trays[0].as<float>(), c->trays[1].as<float>(), c->trays[2].as<float>(), c->trays[3].as<float>(),
-                  c->trays[4].as<float>(), c->trays[5].as<float>(), c->trays[6].as<float>()};
-    if ((r = c->err.alloc(16)) != RGR_OK) return r;
-    RGR_CUDA(cudaMemsetAsync(c->err.p, 0, 4, st));
-    r = rgr_trace_closest_device(c, &d, n, c->tprim.as<int32_t>(), c->tt.as<float>(), nullptr, st);
-    if (r != RGR_OK) return r;
-    uint32_t err = 0;
-    RGR_CUDA(cudaMemcpyAsync(prim, c->tprim.p, 4 * n, cudaMemcpyDeviceToHost, st));
-    RGR_CUDA(cudaMemcpyAsync(t, c->tt.p, 4 * n, cudaMemcpyDeviceToHost, st));
-    RGR_CUDA(cudaMemcpyAsync(&err, c->err.p, 4, cudaMemcpyDeviceToHost, st));
-    RGR_CUDA(cudaStreamSynchronize(st));
-    if (err) {
+    for (uint64_t off = 0, i = 0; off < n; off += chunk, ++i) {
+        const int s = (int)(i & 1u);
+        cudaStream_t st = streams[s];
+        rgr_context::TraceSlot& ts = c->tslot[s];
+        const uint64_t m = std::min(chunk, n - off);
+        for (int k = 0; k < 7; ++k)
+            RGR_CUDA(cudaMemcpyAsync(ts.rays[k].p, src[k] + off, 4 * m, cudaMemcpyHostToDevice, st));
+        launch_trace_rays(c->scene.sv, ts.rays[0].as<float>(), ts.rays[1].as<float>(), ts.rays[2].as<float>(),
+                          ts.rays[3].as<float>(), ts.rays[4].as<float>(), ts.rays[5].as<float>(),
+                          ts.rays[6].as<float>(), m, ts.prim.as<int32_t>(), ts.t.as<float>(), nullptr,
+                          ts.err.as<uint32_t>(), ts.counter.as<unsigned long long>(), c->trace_refill, c->trace_grid,
+                          c->trace_stage, st);
+        RGR_CUDA(cudaGetLastError());
+        RGR_CUDA(cudaMemcpyAsync(prim + off, ts.prim.p, 4 * m, cudaMemcpyDeviceToHost, st));
+        RGR_CUDA(cudaMemcpyAsync(t + off, ts.t.p, 4 * m, cudaMemcpyDeviceToHost, st));
+    }
+    uint32_t err[2] = {0, 0};
+    for (int s = 0; s < 2; ++s) {
+        RGR_CUDA(cudaMemcpyAsync(&err[s], c->tslot[s].err.p, 4, cudaMemcpyDeviceToHost, streams[s]));
+        RGR_CUDA(cudaStreamSynchronize(streams[s]));
+    }
+    if (err[0] | err[1]) {
         set_error("traversal stack overflow");
         return RGR_E_OVERFLOW;
     }
