@@ -75,3 +75,14 @@ def test_trained_guide_lowers_error_in_the_sky_room(rg):
                               ref)
     print(f"room 64 spp relMSE plain {e_plain:.5f} trained guide {e_guided:.5f} ratio {e_plain / e_guided:.2f}")
     assert e_guided < 0.75 * e_plain
+
+
+def test_tcgen05_guided_render_is_unbiased(rg):
+    """The same guided render with the tcgen05/TMEM inference kernel."""
+    sm, cam = _scene(rg, "room")
+    plain = guiding.render_mean(rg, sm, cam, spp=512, seed_offset=1, path_count=1 << 18)
+    g = rg.Guide(0, inference_kernel=rg.GUIDE_TCGEN05)
+    guided = guiding.render_mean(rg, sm, cam, spp=512, seed_offset=1, path_count=1 << 18, guide=g)
+    g.check()
+    assert g.stats()["iterations"] > 50
+    assert abs(guided.mean() / plain.mean() - 1.0) < 0.02

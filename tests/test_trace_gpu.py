@@ -117,3 +117,24 @@ def test_lbvh_built_on_gpu(rg, po):
         _, t1 = lane.trace_closest(rays)
         assert (bits(t) == bits(t1)).all()
         assert (q == p).mean() > 0.999
+
+
+def test_host_api_chunks(rg, po):
+    """rgr_trace_closest pipelines its rays in chunks of 2^20 over two streams:
+    a ragged count spanning several chunks gives the same hits as the
+    device-array entry point."""
+    torch = pytest.importorskip("torch")
+    mesh = scenes.displaced_icosphere(5, seed=7)
+    sm, _ = build(mesh)
+    lane = rg.WavefrontLane(0, 1024)
+    lane.setup(sm)
+    rays = scenes.random_rays(2_500_017, (-1.3, -1.3, -1.3), (1.3, 1.3, 1.3), seed=9)
+    prim, t = lane.trace_closest(rays)
+    soa = [torch.from_numpy(np.ascontiguousarray(a)).cuda() for a in rays.soa()]
+    p2 = torch.empty(len(rays), dtype=torch.int32, device="cuda")
+    t2 = torch.empty(len(rays), dtype=torch.float32, device="cuda")
+    torch.cuda.synchronize()  # the context stream does not wait for torch's stream
+    lane.trace_closest_device([a.data_ptr() for a in soa], len(rays), p2.data_ptr(), t2.data_ptr())
+    lane.synchronize()
+    assert (prim == p2.cpu().numpy()).all()
+    assert (bits(t) == bits(t2.cpu().numpy())).all()
