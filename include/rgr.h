@@ -299,7 +299,8 @@ typedef struct rgr_guide_config {
     float learning_rate;     /* Adam (1e-3) */
     float beta1, beta2;      /* Adam (0.9, 0.999) */
     float epsilon;           /* Adam (1e-8) */
-    uint32_t batch_samples;  /* training samples per iteration (2^18) */
+    uint32_t batch_samples;  /* training samples per iteration (2^18); while rendering, an iteration
+                                waits (over several bounces if need be) for 1/16 of it */
     float guide_fraction;    /* share of the non-envmap selection probability given to the guide (0.5) */
     int32_t train;           /* train online while rendering (1), or keep the weights fixed (0) */
     int32_t guide_volumes;   /* guide in-volume scattering too (0: the isotropic phase function and

@@ -40,6 +40,8 @@ uint16_t to_bf16(float f) {
 // The network's real shape inside the zero-padded 64 x 64 layers.
 int fan_in(int l) { return l == 0 ? kGuideInputs : kGuideWidth; }
 int fan_out(int l) { return l == kGuideLayers - 1 ? kGuideOutputs : kGuideWidth; }
+// samples an online iteration waits for before it trains: 1/16 of the batch
+uint32_t min_batch(const rgr_guide_config& c) { return std::max<uint32_t>(1u, c.batch_samples / 16u); }
 
 bool check_padding(const float* w, const float* b) {
     for (int l = 0; l < kGuideLayers; ++l)
@@ -103,10 +105,12 @@ int rgr_guide::init(const rgr_guide_config& c) {
         t.last = reinterpret_cast<uint32_t*>(ctr + base + kCtrLast);
         t.loss_hist = loss_hist.as<float>();
         t.max_iter = 0;
+        t.min_count = 0;
     };
     stream_at(0, train);
     stream_at(kCtrTest, test);
     train.max_iter = cfg.max_iterations;
+    train.min_count = min_batch(cfg);
     // He-uniform initialisation of the real part of each layer (the output layer
     // scaled by 1/4 so that the first mixtures are broad), zero biases and padding
     std::vector<float> hw(kGuideWeights, 0.0f), hb(kGuideBiases, 0.0f);
@@ -143,8 +147,10 @@ void rgr_guide::infer_paths(const PathsView& p, const QueueView& q, const GuideR
 
 int rgr_guide::train_launches(cudaStream_t st) {
     if (cfg.train) {
-        launch_guide_train(view, train.samples, train.count, train.cap, train.wsum, 1.0f, num_sms, st);
-        launch_guide_adam(view, train.count, train.iter, cfg.learning_rate, cfg.beta1, cfg.beta2, cfg.epsilon, st);
+        launch_guide_train(view, train.samples, train.count, train.cap, train.min_count, train.wsum, 1.0f, num_sms,
+                           st);
+        launch_guide_adam(view, train.count, train.min_count, train.iter, cfg.learning_rate, cfg.beta1, cfg.beta2,
+                          cfg.epsilon, st);
     }
     launch_guide_finish(view, train, st);
     RGR_CUDA(cudaGetLastError());
@@ -227,6 +233,7 @@ int rgr_guide_set_config(rgr_guide* g, const rgr_guide_config* cfg) {
     }
     g->cfg = *cfg;
     g->train.max_iter = cfg->max_iterations;
+    g->train.min_count = min_batch(*cfg);
     return RGR_OK;
 }
 
@@ -298,7 +305,7 @@ int rgr_guide_train_device(rgr_guide* g, const float* samples, uint32_t n, float
     RGR_CUDA(cudaMemcpyAsync(g->test.count, &n, 4, cudaMemcpyHostToDevice, st));
     RGR_CUDA(cudaMemsetAsync(g->loss.p, 0, 4, st));
     const int grid = (int)std::min<uint32_t>(std::max<uint32_t>((n + 63) / 64, 1u), (uint32_t)g->num_sms);
-    launch_guide_train(g->view, samples, g->test.count, n, nullptr, weight_scale, grid, st);
+    launch_guide_train(g->view, samples, g->test.count, n, 0u, nullptr, weight_scale, grid, st);
     RGR_CUDA(cudaGetLastError());
     if (grads) {
         RGR_CUDA(cudaMemcpyAsync(grads, g->gW.p, 4 * kGuideWeights, cudaMemcpyDeviceToDevice, st));
@@ -307,7 +314,7 @@ int rgr_guide_train_device(rgr_guide* g, const float* samples, uint32_t n, float
     float hl = 0.0f;
     RGR_CUDA(cudaMemcpyAsync(&hl, g->loss.p, 4, cudaMemcpyDeviceToHost, st));
     if (apply_adam) {
-        launch_guide_adam(g->view, g->test.count, g->test.iter, g->cfg.learning_rate, g->cfg.beta1, g->cfg.beta2,
+        launch_guide_adam(g->view, g->test.count, 0u, g->test.iter, g->cfg.learning_rate, g->cfg.beta1, g->cfg.beta2,
                           g->cfg.epsilon, st);
         launch_guide_finish(g->view, g->test, st);
         RGR_CUDA(cudaGetLastError());

@@ -108,7 +108,9 @@ __device__ __forceinline__ void mixture_sample(const GuideMixture& m, float u0, 
         acc += m.w[i];
         if (u0 < acc && k == kGuideLobes - 1) k = i;
     }
-    const float4 L = m.lobe[k];
+    float4 L = m.lobe[0];  // m.lobe[k] by selects: a run-time index would put the mixture in local memory
+#pragma unroll
+    for (int i = 1; i < kGuideLobes; ++i) L = (k == i) ? m.lobe[i] : L;
     const float kappa = L.w;
     float w = 1.0f + logf(u1 + (1.0f - u1) * expf(-2.0f * kappa)) / kappa;
     w = fminf(fmaxf(w, -1.0f), 1.0f);
@@ -141,12 +143,13 @@ void launch_guide_infer(const GuideView& g, const float* rows, uint32_t n, float
 // mixtures of this bounce's guided queue items (Lambertian, Ward, in-volume when enabled)
 void launch_guide_infer_paths(const GuideView& g, const PathsView& p, const QueueView& q, const GuideRenderD& gd,
                               int grid, cudaStream_t st);
-// one training iteration over min(*count, cap) samples: gradients into gW/gb, loss
+// one training iteration over min(*count, cap) samples: gradients into gW/gb,
+// loss; nothing while fewer than min_count samples are in
 void launch_guide_train(const GuideView& g, const float* samples, const uint32_t* count, uint32_t cap,
-                        const float* wsum, float weight_scale, int grid, cudaStream_t st);
-// Adam on the accumulated gradients when *count > 0; iteration number from *iter + 1
-void launch_guide_adam(const GuideView& g, const uint32_t* count, const uint32_t* iter, float lr, float beta1,
-                       float beta2, float eps, cudaStream_t st);
+                        uint32_t min_count, const float* wsum, float weight_scale, int grid, cudaStream_t st);
+// Adam on the accumulated gradients when *count > 0 and >= min_count; iteration number from *iter + 1
+void launch_guide_adam(const GuideView& g, const uint32_t* count, uint32_t min_count, const uint32_t* iter,
+                       float lr, float beta1, float beta2, float eps, cudaStream_t st);
 // after an iteration: advance *iter, log the loss, retune the acceptance, reset counters
 void launch_guide_finish(const GuideView& g, const GuideTrainD& t, cudaStream_t st);
 

@@ -407,10 +407,12 @@ __device__ __forceinline__ void add_colsums(float* gb, int col, uint32_t p0, uin
 // samples: 16 floats each (x, n, wo, wi, weight); loss weight = weight * scale / wsum
 __global__ void __launch_bounds__(32 * kTrainWarps) k_guide_train(GuideView gv, const float* __restrict__ samples,
                                                                   const uint32_t* __restrict__ count, uint32_t cap,
-                                                                  const float* __restrict__ wsum, float weight_scale) {
+                                                                  uint32_t min_count, const float* __restrict__ wsum,
+                                                                  float weight_scale) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     SmemTrain& S = *reinterpret_cast<SmemTrain*>(smem_raw);
     const uint32_t n = min(*count, cap);
+    if (n < min_count) return;            // too few yet: they carry over to the next bounce
     if (blockIdx.x * kRows >= n) return;  // (no samples are recorded once the iteration budget is used up)
     float scale = weight_scale;
     if (wsum) {
@@ -545,9 +547,9 @@ __global__ void __launch_bounds__(32 * kTrainWarps) k_guide_train(GuideView gv, 
 }
 
 // ---------------------------------------------------------------- Adam
-__global__ void k_guide_adam(GuideView g, const uint32_t* count, const uint32_t* iter, float lr, float beta1,
-                             float beta2, float eps) {
-    if (*count == 0u) return;
+__global__ void k_guide_adam(GuideView g, const uint32_t* count, uint32_t min_count, const uint32_t* iter, float lr,
+                             float beta1, float beta2, float eps) {
+    if (*count == 0u || *count < min_count) return;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= kGuideParams) return;
     const float t = (float)(*iter + 1u);
@@ -574,6 +576,14 @@ __global__ void k_guide_adam(GuideView g, const uint32_t* count, const uint32_t*
 
 __global__ void k_guide_finish(GuideView g, GuideTrainD t) {
     const uint32_t c = *t.count;
+    if (c < t.min_count) {
+        // no step this bounce: the samples stay for the next one.  Few paths
+        // end at the tail of a render, and Adam's normalised step would turn
+        // a handful of samples into a full-size, noisy update.
+        const unsigned long long cand = *t.candidates;
+        if (cand > 0ull) *t.accept = fminf(1.0f, (float)t.cap / (float)cand);
+        return;
+    }
     if (c > 0u) {
         const uint32_t it = *t.iter;
         t.loss_hist[it % kLossHist] = *g.loss;
@@ -612,13 +622,14 @@ void launch_guide_infer_paths(const GuideView& g, const PathsView& p, const Queu
 }
 
 void launch_guide_train(const GuideView& g, const float* samples, const uint32_t* count, uint32_t cap,
-                        const float* wsum, float weight_scale, int grid, cudaStream_t st) {
-    k_guide_train<<<grid, 32 * kTrainWarps, sizeof(SmemTrain), st>>>(g, samples, count, cap, wsum, weight_scale);
+                        uint32_t min_count, const float* wsum, float weight_scale, int grid, cudaStream_t st) {
+    k_guide_train<<<grid, 32 * kTrainWarps, sizeof(SmemTrain), st>>>(g, samples, count, cap, min_count, wsum,
+                                                                     weight_scale);
 }
 
-void launch_guide_adam(const GuideView& g, const uint32_t* count, const uint32_t* iter, float lr, float beta1,
-                       float beta2, float eps, cudaStream_t st) {
-    k_guide_adam<<<(kGuideParams + 255) / 256, 256, 0, st>>>(g, count, iter, lr, beta1, beta2, eps);
+void launch_guide_adam(const GuideView& g, const uint32_t* count, uint32_t min_count, const uint32_t* iter,
+                       float lr, float beta1, float beta2, float eps, cudaStream_t st) {
+    k_guide_adam<<<(kGuideParams + 255) / 256, 256, 0, st>>>(g, count, min_count, iter, lr, beta1, beta2, eps);
 }
 
 void launch_guide_finish(const GuideView& g, const GuideTrainD& t, cudaStream_t st) {

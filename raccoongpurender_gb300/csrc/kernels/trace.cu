@@ -49,7 +49,9 @@ __global__ void __launch_bounds__(256, RGR_TRACE_MIN_BLOCKS) k_trace_rays(SceneV
         for (uint32_t i = threadIdx.x; i < 4u * stn.n; i += blockDim.x) s_nodes[i] = __ldg(sc.nodes + i);
         __syncthreads();
     }
+    __shared__ uint32_t s_stack[kSmemStack > 0 ? kSmemStack * kStackThreads : 1];
     TraceState s;
+    s.sstk = s_stack + threadIdx.x;
     TraceCounters cnt;
     uint64_t ray = ~0ull;  // ~0: idle
     bool exhausted = false;
@@ -77,7 +79,7 @@ __global__ void __launch_bounds__(256, RGR_TRACE_MIN_BLOCKS) k_trace_rays(SceneV
             continue;
         }
         if (ray != ~0ull) {
-            if (s.link != kDone) trace_round<kCount, kStaged>(sc, s, &cnt, err, pol, stn);
+            if (s.link != kDone) trace_round<kCount, kStaged, kSmemStack>(sc, s, &cnt, err, pol, stn);
             if (s.link == kDone) {
                 __stcs(b.prim + ray, s.prim);
                 __stcs(b.t + ray, s.tmin);
@@ -108,9 +110,9 @@ void launch_trace_rays(const SceneView& sc, const float* ox, const float* oy, co
     RayBatch b{ox, oy, oz, dx, dy, dz, tmax, n, prim, t, ng, nullptr, nullptr, err, counter, refill, stage};
     cudaMemsetAsync(counter, 0, sizeof(unsigned long long), st);
     if (stage > 0)
-        k_trace_rays<false, true><<<grid, 256, 64 * (size_t)stage, st>>>(sc, b);
+        k_trace_rays<false, true><<<grid, kStackThreads, 64 * (size_t)stage, st>>>(sc, b);
     else
-        k_trace_rays<false, false><<<grid, 256, 0, st>>>(sc, b);
+        k_trace_rays<false, false><<<grid, kStackThreads, 0, st>>>(sc, b);
 }
 
 void launch_trace_rays_counts(const SceneView& sc, const float* ox, const float* oy, const float* oz, const float* dx,
@@ -120,7 +122,7 @@ void launch_trace_rays_counts(const SceneView& sc, const float* ox, const float*
     if (n == 0) return;
     RayBatch b{ox, oy, oz, dx, dy, dz, tmax, n, prim, t, nullptr, nodes, prims, err, counter, 16, 0u};
     cudaMemsetAsync(counter, 0, sizeof(unsigned long long), st);
-    k_trace_rays<true, false><<<grid, 256, 0, st>>>(sc, b);
+    k_trace_rays<true, false><<<grid, kStackThreads, 0, st>>>(sc, b);
 }
 
 int trace_rays_max_blocks_per_sm(uint32_t stage) {

@@ -28,6 +28,15 @@ namespace rgr {
 namespace dev {
 
 constexpr int kStackSize = 64;  // the builder limits tree depth to 63
+#ifndef RGR_SMEM_STACK
+#define RGR_SMEM_STACK 12
+#endif
+// The persistent kernels keep the first kSmemStack pending far links of each
+// thread in shared memory (entry i of thread t at i * kStackThreads + t: no
+// bank conflicts), the deeper ones in local memory.  A local-memory stack of
+// a full SM's threads does not fit in L1 and would be written back to L2.
+constexpr int kSmemStack = RGR_SMEM_STACK;
+constexpr int kStackThreads = 256;  // block size of the kernels that use it
 constexpr uint32_t kDone = 0xffffffffu;
 constexpr uint32_t kErrStackOverflow = 1u;
 
@@ -136,8 +145,21 @@ struct TraceState {
     int sp;           // pending far links; the newest is in `top`, older ones in stack[0..sp-2]
     uint32_t top;
     bool nan_free;
+    uint32_t* sstk;   // this thread's shared-memory entries (stride kStackThreads), with kSm > 0
     uint32_t stack[kStackSize];
 };
+
+template <int kSm>
+RGR_DEV void stack_put(TraceState& s, int i, uint32_t v) {
+    if (kSm > 0 && i < kSm)
+        s.sstk[i * kStackThreads] = v;
+    else
+        s.stack[i] = v;
+}
+template <int kSm>
+RGR_DEV uint32_t stack_get(const TraceState& s, int i) {
+    return (kSm > 0 && i < kSm) ? s.sstk[i * kStackThreads] : s.stack[i];
+}
 
 RGR_DEV void trace_begin(const SceneView& sc, TraceState& s, f3 ro, f3 rd, float tmax) {
     s.ro = ro;
@@ -150,13 +172,14 @@ RGR_DEV void trace_begin(const SceneView& sc, TraceState& s, f3 ro, f3 rd, float
     s.nan_free = ray_is_nan_free(ro, s.inv, sc.small_coords != 0);
 }
 
-// the newest pending far link, or kDone; the next one is fetched from local
-// memory now but needed only at the following pop
+// the newest pending far link, or kDone; the next one is fetched from the
+// stack now but needed only at the following pop
+template <int kSm>
 RGR_DEV uint32_t pop(TraceState& s) {
     if (s.sp == 0) return kDone;
     const uint32_t link = s.top;
     --s.sp;
-    if (s.sp > 0) s.top = s.stack[s.sp - 1];
+    if (s.sp > 0) s.top = stack_get<kSm>(s, s.sp - 1);
     return link;
 }
 
@@ -169,7 +192,7 @@ struct StagedNodes {
 
 // One round: inner nodes down to the next leaf, then that leaf.  On return
 // s.link is the next link to visit, or kDone.
-template <bool kNanCheck, bool kCount, bool kStaged>
+template <bool kNanCheck, bool kCount, bool kStaged, int kSm>
 RGR_DEV void trace_round_t(const SceneView& sc, TraceState& s, TraceCounters* cnt, uint32_t& err, uint64_t pol,
                            StagedNodes st) {
     const float4* __restrict__ nodes = sc.nodes;
@@ -197,7 +220,7 @@ RGR_DEV void trace_round_t(const SceneView& sc, TraceState& s, TraceCounters* cn
         if (L && R) {
             bool left_first = (L0 == R0) ? (L1 < R1) : (L0 < R0);
             if (s.sp < kStackSize) {  // push the far child
-                if (s.sp > 0) s.stack[s.sp - 1] = s.top;
+                if (s.sp > 0) stack_put<kSm>(s, s.sp - 1, s.top);
                 s.top = left_first ? cr : cl;
                 s.sp++;
             } else {
@@ -209,7 +232,7 @@ RGR_DEV void trace_round_t(const SceneView& sc, TraceState& s, TraceCounters* cn
         } else if (R) {
             link = cr;
         } else {
-            link = pop(s);
+            link = pop<kSm>(s);
         }
     }
     if (link != kDone) {
@@ -229,18 +252,19 @@ RGR_DEV void trace_round_t(const SceneView& sc, TraceState& s, TraceCounters* cn
                 if (sphere_test(s.ro, s.rd, xyz(a), b.x, s.tmin)) s.prim = (int32_t)__float_as_uint(a.w);
             }
         }
-        link = pop(s);
+        link = pop<kSm>(s);
     }
     s.link = link;
 }
 
-template <bool kCount, bool kStaged = false>
+// kSm: stack entries in shared memory (s.sstk set), 0 for a local-memory stack
+template <bool kCount, bool kStaged = false, int kSm = 0>
 RGR_DEV void trace_round(const SceneView& sc, TraceState& s, TraceCounters* cnt, uint32_t& err, uint64_t pol,
                          StagedNodes st = StagedNodes{nullptr, 0u}) {
     if (s.nan_free) {
-        trace_round_t<false, kCount, kStaged>(sc, s, cnt, err, pol, st);
+        trace_round_t<false, kCount, kStaged, kSm>(sc, s, cnt, err, pol, st);
     } else {
-        trace_round_t<true, kCount, kStaged>(sc, s, cnt, err, pol, st);
+        trace_round_t<true, kCount, kStaged, kSm>(sc, s, cnt, err, pol, st);
     }
 }
 

@@ -458,17 +458,22 @@ RGR_DEV void shade_slot(const RequestD& rq, const PathsView& P, int k, uint32_t 
         if (backside) {  // inVolumeList_Remove (types.cl:115-132)
             uint32_t hsh = volume_hash(__ldg(sc.volumes + mref.y));
             bool move = false;
-            for (int i = 0; i < vcount && i < 7; ++i) {
-                if (move) {
-                    vols[i - 1] = vols[i];
-                } else {
-                    int2 mi = __ldg(sc.materials + vols[i]);
-                    if (volume_hash(__ldg(sc.volumes + mi.y)) == hsh) move = true;
+#pragma unroll
+            for (int i = 0; i < 7; ++i) {  // constant indices keep the list in registers
+                if (i < vcount) {
+                    if (move) {
+                        if (i > 0) vols[i - 1] = vols[i];
+                    } else {
+                        int2 mi = __ldg(sc.materials + vols[i]);
+                        if (volume_hash(__ldg(sc.volumes + mi.y)) == hsh) move = true;
+                    }
                 }
             }
             if (move) vcount--;
         } else if (vcount < 7) {  // inVolumeList_Add (types.cl:108-114)
-            vols[vcount] = hs;
+#pragma unroll
+            for (int i = 0; i < 7; ++i)
+                if (i == vcount) vols[i] = hs;
             vcount++;
         }
         va = make_int4(vols[0], vols[1], vols[2], vols[3]);
@@ -540,8 +545,8 @@ RGR_DEV void shade_slot(const RequestD& rq, const PathsView& P, int k, uint32_t 
     if (0 < vcount) {
         uint64_t u = rng.uniform_integer();
         int sel = (int)(u % (uint64_t)vcount);
-        int vols[7] = {va.x, va.y, va.z, va.w, vb.x, vb.y, vb.z};
-        hv = vols[sel < 7 ? sel : 6];
+        const int vols[7] = {va.x, va.y, va.z, va.w, vb.x, vb.y, vb.z};
+        hv = pick(vols, sel < 7 ? sel : 6);
     }
     tmin = kFltMax;
     if (0 <= hv) {
@@ -673,7 +678,7 @@ __global__ void __launch_bounds__(256) k_shade(PathsView P, QueueView Q, RenderP
         int k = 0;
 #pragma unroll
         for (int j = 1; j < kNumQueues; ++j) k += (i >= off[j]) ? 1 : 0;
-        const uint32_t slot = Q.items[k][i - off[k]];
+        const uint32_t slot = queue_items(Q, k)[i - pick(off, k)];
         unsigned long long gpix = 0;
         int r;
         if (k == 0) {
@@ -709,7 +714,7 @@ RGR_DEV void enqueue(const QueueView& Q, int q, uint32_t slot, unsigned active) 
     if (lane == leader) base = atomicAdd(Q.counts + q, (uint32_t)__popc(peers));
     base = __shfl_sync(peers, base, leader);
     uint32_t rank = __popc(peers & ((1u << lane) - 1u));
-    Q.items[q][base + rank] = slot;
+    queue_items(Q, q)[base + rank] = slot;
 }
 
 RGR_DEV uint32_t mix32(uint32_t h) {  // murmur3 finaliser
@@ -814,7 +819,9 @@ __global__ void __launch_bounds__(256, 5) k_trace_paths(PathsView P, QueueView Q
 #pragma unroll
     for (int k = 0; k < kNumQueues; ++k) off[k + 1] = off[k] + Q.counts[k];
     const uint32_t total = off[kNumQueues];
+    __shared__ uint32_t s_stack[kSmemStack > 0 ? kSmemStack * kStackThreads : 1];
     TraceState s;
+    s.sstk = s_stack + threadIdx.x;
     const SceneView* scp = nullptr;
     uint32_t slot = ~0u;  // ~0: idle
     bool exhausted = false;
@@ -833,7 +840,7 @@ __global__ void __launch_bounds__(256, 5) k_trace_paths(PathsView P, QueueView Q
                     int k = 0;
 #pragma unroll
                     for (int j = 1; j < kNumQueues; ++j) k += ((uint32_t)i >= off[j]) ? 1 : 0;
-                    const uint32_t r = Q.items[k][(uint32_t)i - off[k]];
+                    const uint32_t r = queue_items(Q, k)[(uint32_t)i - pick(off, k)];
                     if (P.qid[r] != kQueueIdle) {
                         slot = r;
                         scp = &rp.reqs[P.req[r]].sc;
@@ -848,7 +855,7 @@ __global__ void __launch_bounds__(256, 5) k_trace_paths(PathsView P, QueueView Q
             continue;
         }
         if (slot != ~0u) {
-            if (s.link != kDone) trace_round<false>(*scp, s, nullptr, err, pol);
+            if (s.link != kDone) trace_round<false, false, kSmemStack>(*scp, s, nullptr, err, pol);
             if (s.link == kDone) {
                 if (s.prim >= 0) {
                     const f3 ng = hit_normal(*scp, s.prim, s.ro, s.rd, s.tmin);
@@ -1105,7 +1112,7 @@ void launch_trace_paths(const PathsView& p, const QueueView& q, const RenderPara
                         cudaStream_t st) {
     if (!ts.persistent) return;
     cudaMemsetAsync(ts.counter, 0, sizeof(unsigned long long), st);
-    k_trace_paths<<<ts.grid, 256, 0, st>>>(p, q, rp, ts.counter, ts.refill);
+    k_trace_paths<<<ts.grid, kStackThreads, 0, st>>>(p, q, rp, ts.counter, ts.refill);
 }
 
 void launch_trace_logic(const PathsView& p, const QueueView& q, const RenderParams& rp, const TraceShape& ts,

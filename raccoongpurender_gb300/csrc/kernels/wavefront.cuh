@@ -44,6 +44,24 @@ struct QueueView {
     unsigned long long* step_base;  // next_pixel_index at the start of this step
 };
 
+// Queue q's item array, chosen by selects: indexing the kernel-parameter
+// array with a run-time q would copy it to local memory in every thread.
+__device__ __forceinline__ uint32_t* queue_items(const QueueView& Q, int q) {
+    uint32_t* p = Q.items[0];
+#pragma unroll
+    for (int j = 1; j < kNumQueues; ++j) p = (q == j) ? Q.items[j] : p;
+    return p;
+}
+
+// a[k] of a small register array, by selects (no local-memory copy)
+template <int N, class T>
+__device__ __forceinline__ T pick(const T (&a)[N], int k) {
+    T v = a[0];
+#pragma unroll
+    for (int j = 1; j < N; ++j) v = (k == j) ? a[j] : v;
+    return v;
+}
+
 struct CameraD {
     float eye[3], up[3], right[3];
     float o[3], r[3], b[3];
@@ -95,6 +113,8 @@ struct GuideTrainD {
     uint32_t* iter;                 // completed training iterations (Adam step)
     uint32_t max_iter;              // no recording or training once *iter reaches it (0: no limit)
     uint32_t* last;                 // samples the last iteration trained on
+    uint32_t min_count;             // an iteration trains once this many samples are in; until then
+                                    // they carry over to the next bounce (0: always train)
     float* loss_hist;               // loss of every iteration, ring of kLossHist
 };
 constexpr uint32_t kLossHist = 4096;
