@@ -309,8 +309,8 @@ def guiding_bench(dev_index: int, w: int = 960, h: int = 540, spp: int = 256, re
     plain render, at w x h: plain rendering at `spp` against guided rendering
     given the same wall time: "cold" (the guide starts untrained and trains
     online on the render's own samples for its first 120 iterations, then is
-    frozen; inference and training inside the time) and "warm" (the guide a
-    cold run trained, frozen).  Medians over 3 seeds.  Scenes: the full-render glossy/volume scene (the 1.31M-triangle
+    frozen; inference and training inside the time) and "warm" (a guide
+    trained online by an earlier 1024-spp render of the same view, frozen).  Medians over 3 seeds.  Scenes: the full-render glossy/volume scene (the 1.31M-triangle
     sphere, ground, volume box, sky + sun) and the sky-lit room."""
     import raccoongpurender_gb300 as rg
     from raccoongpurender_gb300 import guiding, scenes
@@ -333,6 +333,29 @@ def guiding_bench(dev_index: int, w: int = 960, h: int = 540, spp: int = 256, re
                   "triangles": int(mesh.ntris)})
         out[name] = r
     return out
+
+
+def guided_render_cost(dev_index: int, spp: int = 64) -> dict:
+    """What a frozen guide costs per sample: the sky-lit room at 960x540
+    rendered once guided while the guide trains, then plain and with the
+    (now frozen) guide at the same spp; wall times of the last two."""
+    import raccoongpurender_gb300 as rg
+    from raccoongpurender_gb300 import guiding, scenes
+    mesh, env, camd = scenes.sky_room(level=6)
+    sm = rg.SceneManager()
+    sm.addMesh(mesh)
+    sm.setEnvmap(env)
+    sm.buildBVH(max_leaf_size=4)
+    cam = rg.camera_look_at(camd["eye"], camd["target"], camd["up"], camd["vfov"], 960, 540)
+    lane = rg.WavefrontLane(dev_index, 1 << 22)
+    lane.setup(sm)
+    g = rg.Guide(dev_index)
+    guiding.render(rg, sm, cam, spp, 77, guide=g, lane=lane)
+    g.set_config(train=0)
+    _, _, tp = guiding.render(rg, sm, cam, spp, 5, lane=lane)
+    _, _, tg = guiding.render(rg, sm, cam, spp, 5, guide=g, lane=lane)
+    return {"spp": spp, "plain_s": round(tp, 4), "frozen_guided_s": round(tg, 4),
+            "cost_per_sample": round(tg / tp - 1.0, 3), "training_iterations": g.stats()["iterations"]}
 
 
 def cpu_baseline(mesh, sm, coherent, incoherent, sample: int = 1048576) -> dict:
@@ -583,7 +606,8 @@ def main() -> None:
                                   for soa, prim, t, n in sets], sptr, build_s) if not args.no_render else None
     guide = None
     if not args.no_guiding:
-        guide = {"kernels": guide_kernels_bench(local), "equal_time": guiding_bench(local)}
+        guide = {"kernels": guide_kernels_bench(local), "cost": guided_render_cost(local),
+                 "equal_time": guiding_bench(local)}
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cpu = cpu_baseline(mesh, sm, coherent, incoherent)

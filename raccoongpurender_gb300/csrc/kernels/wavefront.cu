@@ -944,7 +944,11 @@ __global__ void __launch_bounds__(128) k_trace_logic(PathsView P, QueueView Q, R
             atomicAdd(a + 3, 1.0);
         }
     }
-    if (kGuided && rp.gd.record && guide_training_open(rp.gd.train)) {
+    // No samples once the sample budget is handed out: the paths still in
+    // flight are the long ones, and a few iterations on that subset alone
+    // undo much of what the guide learned (the same for every thread).
+    if (kGuided && rp.gd.record && guide_training_open(rp.gd.train) &&
+        !(rp.sample_limit != 0ull && *Q.next_pixel >= rp.sample_limit)) {
         const float cl = rq.radiance_clamp;
         const bool kept = is_finite(L.x) && is_finite(L.y) && is_finite(L.z) && L.x < cl && L.y < cl && L.z < cl;
         guide_emit_samples(rp.gd, slot, L, newPath && kept, active);
