@@ -113,6 +113,14 @@ int rgr_bvh_export_stackless(const rgr_scene* s, rgr_stackless_node* nodes, uint
 /* createEnvmapBuffer (scene_manager.hpp:604-650): tables as uploaded.  pdf/height/alias hold
    7*w*h entries (uniform, then +x,-x,+y,-y,+z,-z); frag holds 4*w*h (beg_y,end_y,beg_phi,end_phi). */
 int rgr_scene_export_envmap(const rgr_scene* s, float* pdf, float* height, int32_t* alias, float* frag);
+/* The scene as built (SceneManager's _points, _indices, _spheres and MaterialStorage): 3 floats
+   per vertex, 3 indices per triangle, xyzr per sphere, one material per primitive (triangles,
+   then spheres; back_emission reads 0: the material tables do not keep it).  Sizes from
+   rgr_scene_get_info; a null pointer skips that array. */
+int rgr_scene_export_geometry(const rgr_scene* s, float* points, uint32_t* indices, float* spheres,
+                              rgr_material* materials);
+/* The envmap image after clamp and scale (SceneManager::_envmapImage), RGBA float rows */
+int rgr_scene_export_envmap_image(const rgr_scene* s, int32_t* w, int32_t* h, float* rgba);
 
 /* ---- device context (replaces rt::WavefrontLane, wavefront_path_tracing.hpp:339-1153) */
 typedef struct rgr_context rgr_context;
@@ -167,6 +175,41 @@ typedef struct rgr_stats {
 void rgr_render_config_default(rgr_render_config* c);
 int rgr_camera_look_at(rgr_camera* c, const float eye[3], const float target[3], const float up[3], float vfov_deg,
                        uint32_t image_w, uint32_t image_h);
+
+/* ---- scene front-end: Alembic files (replaces houdini_alembic::AlembicStorage,
+   libs/houdini_alembic/houdini_alembic.hpp:417-432, and the scene loading of
+   WavefrontPathTracing's constructor, wavefront_path_tracing.hpp:1170-1216).
+   Reads Ogawa-container Alembic archives as a Houdini export writes them
+   (transform hierarchy, polygon meshes, point objects, cameras, geometry
+   parameters as attribute columns) without the Alembic SDK. */
+typedef struct rgr_alembic rgr_alembic;
+typedef struct rgr_alembic_info {
+    uint32_t frame_count;     /* AlembicStorage::frameCount (the "1.samples" property, else 1) */
+    uint32_t meshes;          /* visible triangle meshes added */
+    uint32_t meshes_skipped;  /* visible meshes with non-triangle faces (skipped, scene_manager.hpp:343-347) */
+    uint32_t triangles;
+    uint32_t spheres;         /* from visible point objects with pscale (addPointPrimitive) */
+    int32_t has_envmap;       /* an "ImageEnvmap" point set the envmap */
+    int32_t has_camera;       /* the first visible camera, as standardCamera builds it */
+    rgr_camera camera;
+    float lens_radius, focus_distance, fov_horizontal_degree, fov_vertical_degree;
+} rgr_alembic_info;
+/* AlembicStorage::open: RGR_E_INVALID (rgr_last_error() says why) if the file is not an
+   Ogawa Alembic archive */
+int rgr_alembic_open(rgr_alembic** out, const char* path);
+void rgr_alembic_close(rgr_alembic* a);
+uint32_t rgr_alembic_frame_count(const rgr_alembic* a);
+/* AlembicStorage::read(frame) as JSON text: every object the Houdini reader returns (type,
+   parent transform name, visibility, transforms, topology, P, attribute columns by scope,
+   camera parameters).  *needed = bytes including the terminating zero; cap 0 only asks. */
+int rgr_alembic_describe(rgr_alembic* a, uint32_t frame, char* buf, uint64_t cap, uint64_t* needed);
+/* The reference's scene load for `frame`: visible triangle meshes through their combined
+   transform with per-triangle materials from the "material" column and its property
+   columns (SceneManager::addPolymesh / add_materials, scene_manager.hpp:197-370), then
+   visible point objects (spheres, or the "ImageEnvmap" point's Radiance .hdr image relative
+   to the archive's directory: addPoint, :372-497), and the first visible camera.  Unknown
+   material names and malformed files return RGR_E_INVALID. */
+int rgr_alembic_load(rgr_alembic* a, uint32_t frame, rgr_scene* scene, rgr_alembic_info* info);
 
 /* OpenCLContext::lane_initialize + WavefrontLane ctor (raccoon_ocl.hpp:752-771, :341-349).
    path_count = resident paths (reference kWavefrontPathCountGPU = 2^22). */

@@ -7,6 +7,12 @@
   plus the step() driver ``oracle/ref/ref_step.cpp``.  Built only where the
   reference sources exist (``RGR_REFERENCE_DIR``, default ``/root/reference``);
   the GPU machines do not have them and use the committed golden fixtures.
+* ``oracle/_ref/abc_tool`` — the reference's vendored Alembic library
+  (``libs/abc``: Alembic, Imath, Iex, IlmThread, half) and its Houdini reader
+  (``libs/houdini_alembic/houdini_alembic.cpp``) compiled from their sources,
+  with ``oracle/abc/abc_tool.cpp``: writes the synthetic Alembic test scenes
+  and dumps what the reference reader returns for them
+  (``tests/golden/make_alembic_golden.py``).  Same condition as libref.so.
 
 Both are compiled with ``-ffp-contract=off`` (no fused multiply-add), the
 arithmetic convention shared with the CUDA kernels.
@@ -92,6 +98,45 @@ def build_ref(force: bool = False) -> Path | None:
     return REF_LIB
 
 
+ABC_TOOL = REF_OUT / "abc_tool"
+
+
+def build_abc_tool(force: bool = False) -> Path | None:
+    ref = reference_dir()
+    if ref is None or not (ref / "libs" / "abc" / "Alembic").exists():
+        return ABC_TOOL if ABC_TOOL.exists() else None
+    abc = ref / "libs" / "abc"
+    hou = ref / "libs" / "houdini_alembic"
+    # every Alembic / IlmBase translation unit but the Win32-only ones
+    srcs = sorted(p for p in abc.rglob("*.cpp") if "Win32" not in p.name) + [hou / "houdini_alembic.cpp"]
+    tool = HERE / "abc" / "abc_tool.cpp"
+    stamp = REF_OUT / "abc_stamp"
+    key = _digest([tool, HERE / "abc" / "windows.h"] + srcs)
+    if not force and ABC_TOOL.exists() and stamp.exists() and stamp.read_text() == key:
+        return ABC_TOOL
+    objdir = REF_OUT / "abc_obj"
+    objdir.mkdir(parents=True, exist_ok=True)
+    # the pre-generated IlmBase configuration declares Windows; abc/windows.h
+    # stands in for the one header that this pulls in.  houdini_alembic.hpp
+    # relies on <algorithm> and <cstring> arriving through other headers.
+    flags = ["g++", "-O2", "-std=c++14", "-fPIC", "-ffp-contract=off", "-w", "-include", "algorithm",
+             "-include", "cstring", "-I", str(abc),
+             "-I", str(abc / "Alembic"), "-I", str(hou), "-I", str(HERE / "abc")]
+    objs, jobs = [], []
+    for s in srcs + [tool]:
+        obj = objdir / (hashlib.sha1(str(s).encode()).hexdigest()[:16] + ".o")
+        objs.append(str(obj))
+        jobs.append(flags + ["-c", str(s), "-o", str(obj)])
+    with cf.ThreadPoolExecutor(max_workers=os.cpu_count() or 4) as ex:
+        list(ex.map(_run, jobs))
+    tmp = ABC_TOOL.with_suffix(".tmp")
+    _run(["g++", "-pthread", *objs, "-o", str(tmp)])
+    os.replace(tmp, ABC_TOOL)
+    stamp.write_text(key)
+    return ABC_TOOL
+
+
 if __name__ == "__main__":
     print(build_oracle(force="--force" in sys.argv))
     print(build_ref(force="--force" in sys.argv))
+    print(build_abc_tool(force="--force" in sys.argv))

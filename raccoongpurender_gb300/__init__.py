@@ -68,6 +68,14 @@ class rgr_camera(C.Structure):
                 ("image_w", C.c_uint32), ("image_h", C.c_uint32)]
 
 
+class rgr_alembic_info(C.Structure):
+    _fields_ = [("frame_count", C.c_uint32), ("meshes", C.c_uint32), ("meshes_skipped", C.c_uint32),
+                ("triangles", C.c_uint32), ("spheres", C.c_uint32), ("has_envmap", C.c_int32),
+                ("has_camera", C.c_int32), ("camera", rgr_camera), ("lens_radius", C.c_float),
+                ("focus_distance", C.c_float), ("fov_horizontal_degree", C.c_float),
+                ("fov_vertical_degree", C.c_float)]
+
+
 class rgr_render_config(C.Structure):
     _fields_ = [("dof", C.c_float), ("rr_depth", C.c_int32), ("radiance_clamp", C.c_float),
                 ("env_select_prob", C.c_float), ("max_depth", C.c_int32), ("seed_offset", C.c_uint32),
@@ -127,6 +135,13 @@ _SIGS = {
     "rgr_scene_get_info": (C.c_int, [C.c_void_p, C.c_void_p]),
     "rgr_bvh_export_stackless": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p, C.c_uint64]),
     "rgr_scene_export_envmap": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "rgr_scene_export_geometry": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "rgr_scene_export_envmap_image": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "rgr_alembic_open": (C.c_int, [C.c_void_p, C.c_char_p]),
+    "rgr_alembic_close": (None, [C.c_void_p]),
+    "rgr_alembic_frame_count": (C.c_uint32, [C.c_void_p]),
+    "rgr_alembic_describe": (C.c_int, [C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint64, C.c_void_p]),
+    "rgr_alembic_load": (C.c_int, [C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p]),
     "rgr_render_config_default": (None, [C.c_void_p]),
     "rgr_camera_look_at": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_float, C.c_uint32,
                                      C.c_uint32]),
@@ -294,6 +309,42 @@ class SceneManager:
             proc[..., :3] *= np.float32(scale)
         self.envmap = proc
 
+    def addAlembic(self, source, frame: int = 0) -> rgr_alembic_info:
+        """Load a frame of an Alembic archive the way WavefrontPathTracing's
+        constructor does (wavefront_path_tracing.hpp:1170-1216): visible
+        triangle meshes (addPolymesh), then visible point objects (spheres or
+        the ImageEnvmap point, addPoint); returns the load summary with the
+        first visible camera.  `source` is a path or an AlembicStorage."""
+        store = source if isinstance(source, AlembicStorage) else AlembicStorage(source)
+        before = self.info()
+        info = rgr_alembic_info()
+        _check(self._lib.rgr_alembic_load(store.handle, frame, self._h, C.byref(info)), "rgr_alembic_load")
+        # mirror what was added, as addPolymesh / addSpheres / setEnvmap keep it
+        pts, idx, sph, mats = self.geometry()
+        new_mats = mats[before.num_triangles + before.num_spheres:]
+        self._append_materials(new_mats)
+        self.num_triangles = int(self.info().num_triangles)
+        if info.has_envmap:
+            w, h = C.c_int32(), C.c_int32()
+            _check(self._lib.rgr_scene_export_envmap_image(self._h, C.byref(w), C.byref(h), None),
+                   "rgr_scene_export_envmap_image")
+            img = np.zeros((h.value, w.value, 4), np.float32)
+            _check(self._lib.rgr_scene_export_envmap_image(self._h, None, None, _ptr(img)),
+                   "rgr_scene_export_envmap_image")
+            self.envmap = img
+        return info
+
+    def geometry(self):
+        """(points (n, 3), indices (t, 3), spheres (s, 4), materials per primitive) as built."""
+        i = self.info()
+        pts = np.zeros((i.num_vertices, 3), np.float32)
+        idx = np.zeros((i.num_triangles, 3), np.uint32)
+        sph = np.zeros((i.num_spheres, 4), np.float32)
+        mats = np.zeros(i.num_triangles + i.num_spheres, materials.MATERIAL_DTYPE)
+        _check(self._lib.rgr_scene_export_geometry(self._h, _ptr(pts), _ptr(idx), _ptr(sph), _ptr(mats)),
+               "rgr_scene_export_geometry")
+        return pts, idx, sph, mats
+
     def envmapTablesOnGPU(self, device: int = 0) -> None:
         """Rebuild the envmap tables with FP64 weights and normalisation on the GPU."""
         _check(self._lib.rgr_scene_envmap_tables_gpu(self._h, device), "rgr_scene_envmap_tables_gpu")
@@ -340,6 +391,40 @@ class SceneManager:
         _check(self._lib.rgr_scene_export_envmap(self._h, _ptr(pdf), _ptr(height), _ptr(alias), _ptr(frag)),
                "rgr_scene_export_envmap")
         return dict(pdf=pdf, height=height, alias=alias, frag=frag, w=w, h=h)
+
+
+class AlembicStorage:
+    """houdini_alembic::AlembicStorage (libs/houdini_alembic/houdini_alembic.hpp:417-432):
+    an Alembic archive read by the library's own Ogawa reader."""
+
+    def __init__(self, path):
+        self._lib = load_library()
+        self._h = C.c_void_p()
+        _check(self._lib.rgr_alembic_open(C.byref(self._h), os.fsencode(str(path))), "rgr_alembic_open")
+        self.path = str(path)
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h and h.value:
+            self._lib.rgr_alembic_close(h)
+            self._h = C.c_void_p()
+
+    @property
+    def handle(self):
+        return self._h
+
+    def frameCount(self) -> int:
+        return int(self._lib.rgr_alembic_frame_count(self._h))
+
+    def read(self, frame: int = 0) -> dict:
+        """AlembicStorage::read(frame): the objects the Houdini reader returns,
+        as a dict ({"frame_count", "objects": [...]})."""
+        import json
+        need = C.c_uint64()
+        _check(self._lib.rgr_alembic_describe(self._h, frame, None, 0, C.byref(need)), "rgr_alembic_describe")
+        buf = C.create_string_buffer(need.value)
+        _check(self._lib.rgr_alembic_describe(self._h, frame, buf, need.value, C.byref(need)), "rgr_alembic_describe")
+        return json.loads(buf.value.decode())
 
 
 def render_config(**kw) -> rgr_render_config:

@@ -261,6 +261,55 @@ int rgr_scene_export_envmap(const rgr_scene* s, float* pdf, float* height, int32
     return RGR_OK;
 }
 
+namespace {
+rgr_material material_of(const rgr_scene* s, const MaterialRef& r) {
+    rgr_material m{};
+    m.type = r.type;
+    if (r.type == RGR_MAT_LAMBERTIAN) {
+        const LambertianD& d = s->lambertians[(size_t)r.index];
+        for (int k = 0; k < 3; ++k) {
+            m.le[k] = d.le[k];
+            m.r[k] = d.r[k];
+        }
+    } else if (r.type == RGR_MAT_WARD) {
+        const WardD& d = s->wards[(size_t)r.index];
+        m.alpha = d.alpha;
+        m.falloff = d.falloff;
+        for (int k = 0; k < 3; ++k) {
+            m.r[k] = d.reflectance[k];
+            m.edgetint[k] = d.edgetint[k];
+        }
+    } else if (r.type == RGR_MAT_HOMOGENEOUS_VOLUME) {
+        const VolumeD& d = s->volumes[(size_t)r.index];
+        for (int k = 0; k < 3; ++k) m.r[k] = d.r[k];
+        m.c = d.c;
+    }
+    return m;
+}
+}  // namespace
+
+int rgr_scene_export_geometry(const rgr_scene* s, float* points, uint32_t* indices, float* spheres,
+                              rgr_material* materials) {
+    if (!s) return RGR_E_INVALID;
+    if (points) memcpy(points, s->points.data(), 4 * s->points.size());
+    if (indices) memcpy(indices, s->indices.data(), 4 * s->indices.size());
+    if (spheres) memcpy(spheres, s->spheres.data(), 4 * s->spheres.size());
+    if (materials) {
+        size_t k = 0;
+        for (const MaterialRef& r : s->tri_materials) materials[k++] = material_of(s, r);
+        for (const MaterialRef& r : s->sphere_materials) materials[k++] = material_of(s, r);
+    }
+    return RGR_OK;
+}
+
+int rgr_scene_export_envmap_image(const rgr_scene* s, int32_t* w, int32_t* h, float* rgba) {
+    if (!s || !s->env.present) return RGR_E_STATE;
+    if (w) *w = s->env.w;
+    if (h) *h = s->env.h;
+    if (rgba) memcpy(rgba, s->env.rgba.data(), 4 * s->env.rgba.size());
+    return RGR_OK;
+}
+
 void rgr_render_config_default(rgr_render_config* c) {
     if (!c) return;
     c->dof = 0.0045f;
