@@ -335,6 +335,37 @@ def guiding_bench(dev_index: int, w: int = 960, h: int = 540, spp: int = 256, re
     return out
 
 
+def scene_load_bench(repeats: int = 3) -> dict:
+    """The scene front-end on the full-render scene: the 1.31M-triangle mixed
+    scene (sphere, ground, volume box, per-triangle materials) written as an
+    Alembic archive with a camera, then opened and built into a scene with
+    rgr_alembic_open + rgr_alembic_load (parse, transform, material binding);
+    best of `repeats`.  Host-side work (the reference reads its scenes on the
+    host too)."""
+    import tempfile
+    import raccoongpurender_gb300 as rg
+    from raccoongpurender_gb300 import alembic_io, materials, scenes
+    mesh, _, camd = scenes.mixed_scene(level=8, seed=3)
+    cols = alembic_io.columns_from_materials(materials.as_array(mesh.materials))
+    with tempfile.TemporaryDirectory() as d:
+        path = os.path.join(d, "mixed.abc")
+        t0 = time.perf_counter()
+        size = alembic_io.write_scene(path, meshes=[dict(name="mixed", P=mesh.points, indices=mesh.indices,
+                                                         prims=cols)],
+                                      camera=dict(ops=[("translate", camd["eye"])], resx=camd["w"], resy=camd["h"]))
+        write_s = time.perf_counter() - t0
+        best = None
+        for _ in range(repeats):
+            t0 = time.perf_counter()
+            sm = rg.SceneManager()
+            info = sm.addAlembic(path)
+            dt = time.perf_counter() - t0
+            best = dt if best is None else min(best, dt)
+    return {"triangles": int(info.triangles), "file_mb": round(size / 1e6, 1), "load_s": round(best, 4),
+            "mb_s": round(size / 1e6 / best, 1), "mtris_s": round(info.triangles / 1e6 / best, 2),
+            "write_s": round(write_s, 2), "threads": 1}
+
+
 def guided_render_cost(dev_index: int, spp: int = 64) -> dict:
     """What a frozen guide costs per sample: the sky-lit room at 960x540
     rendered once guided while the guide trains, then plain and with the
@@ -601,7 +632,8 @@ def main() -> None:
     if not args.no_render:
         render = {"cornell_256_4spp": render_bench(local, "cornell"),
                   "mixed_1080p_64spp": render_bench(local, "mixed"),
-                  "batch_32_requests": batch_bench(local)}
+                  "batch_32_requests": batch_bench(local),
+                  "scene_load_alembic": scene_load_bench()}
     bvh = bvh_bench(local, mesh, [([a.data_ptr() for a in soa], n, prim.data_ptr(), t.data_ptr())
                                   for soa, prim, t, n in sets], sptr, build_s) if not args.no_render else None
     guide = None

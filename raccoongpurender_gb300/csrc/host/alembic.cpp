@@ -615,7 +615,9 @@ struct Column {
     int dim = 1;
     std::vector<float> f;      // rows * dim (float and vector columns)
     std::vector<int32_t> i;    // int columns
-    std::vector<std::string> s;
+    std::vector<std::string> s;  // string columns: the distinct values ...
+    std::vector<uint32_t> si;     // ... and each row's index into them
+    const std::string& str(uint32_t r) const { return s[si[r]]; }
 };
 struct Sheet {
     std::vector<Column> cols;  // sorted by key
@@ -665,11 +667,10 @@ bool parse_column(const Compound& parent, const PropHeader& h, int64_t frame, Co
         const Sample vals = c.array(*vh, frame), idx = c.array(*ih, frame);
         col.type = kColString;
         col.rows = (uint32_t)idx.count;
-        for (uint64_t r = 0; r < idx.count; ++r) {
-            const uint32_t k = idx.as<uint32_t>()[r];
-            if (k >= vals.strings.size()) throw Error("indexed string out of range");
-            col.s.push_back(vals.strings[k]);
-        }
+        col.s = vals.strings;
+        col.si.assign(idx.as<uint32_t>(), idx.as<uint32_t>() + idx.count);
+        for (uint32_t k : col.si)
+            if (k >= col.s.size()) throw Error("indexed string out of range");
         return true;
     }
     if (h.type == kCompound && podName == "float32_t" && get(h.meta, "podExtent") == "2") {
@@ -727,6 +728,8 @@ bool parse_column(const Compound& parent, const PropHeader& h, int64_t frame, Co
         col.type = kColString;
         col.rows = (uint32_t)v.count;
         col.s.assign(v.strings.begin(), v.strings.begin() + (ptrdiff_t)v.count);
+        col.si.resize(v.count);
+        for (uint32_t r = 0; r < (uint32_t)v.count; ++r) col.si[r] = r;
         return true;
     }
     return false;
@@ -983,7 +986,7 @@ void json_sheet(Json& j, const Sheet& sh) {
             else if (col.type == kColFloat)
                 j.f(r < col.f.size() ? col.f[r] : 0.0f);
             else if (col.type == kColString)
-                j.str(r < col.s.size() ? col.s[r] : std::string());
+                j.str(col.str(r));
             else
                 j.vec(col.f.data() + (size_t)r * col.dim, col.dim);
         }
@@ -1202,20 +1205,30 @@ std::vector<rgr_material> bind_materials(const SceneObject& o, size_t ntris) {
     const Column* falloff = column(p, "falloff", kColFloat);
     const Column* C = column(p, "C", kColFloat);
     out.resize(rows);
+    if (mat->rows < rows) throw Error("material column shorter than the primitives");
+    // the class of each distinct name, once
+    std::vector<int> cls(mat->s.size());
+    for (size_t k = 0; k < mat->s.size(); ++k) {
+        const std::string& n = mat->s[k];
+        cls[k] = n == "Lambertian" ? RGR_MAT_LAMBERTIAN
+                 : n == "Specular" ? RGR_MAT_SPECULAR
+                 : n == "Dierectric" ? RGR_MAT_DIELECTRIC
+                 : n == "Ward" ? RGR_MAT_WARD
+                 : n == "HomogeneousVolume" ? RGR_MAT_HOMOGENEOUS_VOLUME : 0;
+    }
     for (uint32_t i = 0; i < rows; ++i) {
-        if (i >= mat->rows) throw Error("material column shorter than the primitives");
-        const std::string& name = mat->s[i];
+        const int c = cls[mat->si[i]];
         rgr_material m{};
-        if (name == "Lambertian") {
+        if (c == RGR_MAT_LAMBERTIAN) {
             m = lambertian(1.0f, 1.0f, 1.0f);
             set3(m.le, Le, i);
             set3(m.r, Cd, i);
             if (back && i < back->rows) m.back_emission = back->i[i];
-        } else if (name == "Specular") {
+        } else if (c == RGR_MAT_SPECULAR) {
             m.type = RGR_MAT_SPECULAR;
-        } else if (name == "Dierectric") {
+        } else if (c == RGR_MAT_DIELECTRIC) {
             m.type = RGR_MAT_DIELECTRIC;
-        } else if (name == "Ward") {
+        } else if (c == RGR_MAT_WARD) {
             m.type = RGR_MAT_WARD;
             m.alpha = 0.1f;
             m.r[0] = m.r[1] = m.r[2] = 1.0f;
@@ -1225,14 +1238,14 @@ std::vector<rgr_material> bind_materials(const SceneObject& o, size_t ntris) {
             set3(m.r, refl, i);
             set3(m.edgetint, tint, i);
             if (falloff && i < falloff->rows) m.falloff = falloff->f[i];
-        } else if (name == "HomogeneousVolume") {
+        } else if (c == RGR_MAT_HOMOGENEOUS_VOLUME) {
             m.type = RGR_MAT_HOMOGENEOUS_VOLUME;
             m.c = 1.0f;
             m.r[0] = m.r[1] = m.r[2] = 1.0f;
             if (C && i < C->rows) m.c = C->f[i];
             set3(m.r, Cd, i);
         } else {
-            throw Error("object " + o.name + ": unknown material \"" + name + "\"");
+            throw Error("object " + o.name + ": unknown material \"" + mat->str(i) + "\"");
         }
         out[i] = m;
     }
@@ -1312,8 +1325,8 @@ int add_points(rgr_scene* scene, const SceneObject& o, const std::string& dir, L
     const Column* clamp = column(o.points, "clamp", kColFloat);
     const Column* scale = column(o.points, "scale", kColFloat);
     for (uint32_t i = 0; i < ptype->rows; ++i) {
-        if (ptype->s[i] != "ImageEnvmap") continue;
-        std::string name = file && i < file->rows ? file->s[i] : std::string();
+        if (ptype->str(i) != "ImageEnvmap") continue;
+        std::string name = file && i < file->rows ? file->str(i) : std::string();
         const float cmax = clamp && i < clamp->rows ? clamp->f[i] : std::numeric_limits<float>::max();
         const float sc = scale && i < scale->rows ? scale->f[i] : 1.0f;
         if (name.empty()) continue;
