@@ -320,10 +320,12 @@ class SceneManager:
         info = rgr_alembic_info()
         _check(self._lib.rgr_alembic_load(store.handle, frame, self._h, C.byref(info)), "rgr_alembic_load")
         # mirror what was added, as addPolymesh / addSpheres / setEnvmap keep it
-        pts, idx, sph, mats = self.geometry()
-        new_mats = mats[before.num_triangles + before.num_spheres:]
-        self._append_materials(new_mats)
-        self.num_triangles = int(self.info().num_triangles)
+        after = self.info()
+        mats = np.zeros(after.num_triangles + after.num_spheres, materials.MATERIAL_DTYPE)
+        _check(self._lib.rgr_scene_export_geometry(self._h, None, None, None, _ptr(mats)),
+               "rgr_scene_export_geometry")
+        self._append_materials(mats[before.num_triangles + before.num_spheres:])
+        self.num_triangles = int(after.num_triangles)
         if info.has_envmap:
             w, h = C.c_int32(), C.c_int32()
             _check(self._lib.rgr_scene_export_envmap_image(self._h, C.byref(w), C.byref(h), None),
