@@ -354,7 +354,8 @@ typedef struct rgr_guide_config {
                                  network in register fragments; RGR_GUIDE_TCGEN05: tcgen05.mma with
                                  TMEM accumulators, one thread per row (1.9x slower for this
                                  64-wide network: the per-row scalar work, not the MMA, bounds it) */
-    uint32_t reserved;
+    uint32_t max_depth;      /* guide only the first max_depth vertices of a path (0: every vertex); the
+                                others use BSDF and envmap sampling alone and cost no inference */
     uint64_t seed;           /* weight initialisation (1) */
 } rgr_guide_config;
 typedef struct rgr_guide_stats {

@@ -90,7 +90,7 @@ class rgr_guide_config(C.Structure):
     _fields_ = [("learning_rate", C.c_float), ("beta1", C.c_float), ("beta2", C.c_float), ("epsilon", C.c_float),
                 ("batch_samples", C.c_uint32), ("guide_fraction", C.c_float), ("train", C.c_int32),
                 ("guide_volumes", C.c_int32), ("train_interval", C.c_uint32), ("max_iterations", C.c_uint32),
-                ("inference_kernel", C.c_int32), ("reserved", C.c_uint32), ("seed", C.c_uint64)]
+                ("inference_kernel", C.c_int32), ("max_depth", C.c_uint32), ("seed", C.c_uint64)]
 
 
 GUIDE_TCGEN05, GUIDE_MMA_SYNC = 0, 1  # rgr_guide_config.inference_kernel

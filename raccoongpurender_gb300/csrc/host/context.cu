@@ -188,7 +188,7 @@ struct rgr_context {
     // learned path guiding: the attached network and this render's per-slot buffers
     rgr_guide* guide = nullptr;
     bool guided = false;      // the current render uses `guide`
-    DevBuf globes, grecords, gnrec;
+    DevBuf globes, grecords, gnrec, gsel, gremap, gnsel;
     float scene_bounds[6] = {0, 0, 0, 0, 0, 0};
 
     ~rgr_context() {
@@ -277,6 +277,7 @@ struct rgr_context {
     // train_now: a guided render ends a training interval with this bounce
     int step_launches(cudaStream_t st, bool train_now = true) {
         launch_compact_new(pv, qv, st);
+        if (guided && rp.gd.max_depth) launch_guide_select(pv, qv, rp.gd, shade_grid, st);
         if (guided) guide->infer_paths(pv, qv, rp.gd, st);
         launch_shade(pv, qv, rp, shade_grid, st);
         launch_trace_paths(pv, qv, rp, render_trace, st);
@@ -303,6 +304,11 @@ struct rgr_context {
         if ((r = globes.alloc(16 * kGuideLobeVecs * n)) != RGR_OK) return r;
         if ((r = grecords.alloc(16 * 5 * kGuideRecords * n)) != RGR_OK) return r;
         if ((r = gnrec.alloc(n)) != RGR_OK) return r;
+        if (guide->cfg.max_depth) {
+            if ((r = gsel.alloc(4 * n)) != RGR_OK) return r;
+            if ((r = gremap.alloc(4 * n)) != RGR_OK) return r;
+            if ((r = gnsel.alloc(16)) != RGR_OK) return r;
+        }
         RGR_CUDA(cudaMemsetAsync(gnrec.p, 0, n, stream));
         if (!guide->bounds_set) {
             // the scene's bounds, widened by 1 % so that hit points stay inside
@@ -322,6 +328,12 @@ struct rgr_context {
         gd.guide_frac = guide->cfg.guide_fraction;
         gd.volumes = guide->cfg.guide_volumes ? 1 : 0;
         gd.record = guide->cfg.train ? 1 : 0;
+        gd.max_depth = guide->cfg.max_depth;
+        if (gd.max_depth) {
+            gd.sel = gsel.as<uint32_t>();
+            gd.remap = gremap.as<uint32_t>();
+            gd.nsel = gnsel.as<uint32_t>();
+        }
         guided = true;
         return RGR_OK;
     }

@@ -172,7 +172,7 @@ void rgr_guide_config_default(rgr_guide_config* c) {
     c->train_interval = 1;
     c->max_iterations = 0;
     c->inference_kernel = RGR_GUIDE_MMA_SYNC;
-    c->reserved = 0;
+    c->max_depth = 0;
     c->seed = 1;
 }
 

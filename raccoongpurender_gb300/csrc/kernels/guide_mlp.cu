@@ -307,19 +307,6 @@ __global__ void __launch_bounds__(32 * kInferWarps, 4) k_guide_infer(GuideView g
     }
 }
 
-// The guided items of this bounce, in the order the shading kernel numbers
-// them: queue 1 (Lambertian), queue 4 (Ward), then queue 6 (in-volume) when
-// volumes are guided.
-__device__ __forceinline__ uint32_t guided_count(const QueueView& Q, const GuideRenderD& gd) {
-    return Q.counts[kMatLambertian] + Q.counts[kMatWard] + (gd.volumes ? Q.counts[kMatVolumeInside] : 0u);
-}
-__device__ __forceinline__ uint32_t guided_slot(const QueueView& Q, uint32_t gi) {
-    const uint32_t c1 = Q.counts[kMatLambertian], c4 = Q.counts[kMatWard];
-    if (gi < c1) return Q.items[kMatLambertian][gi];
-    if (gi < c1 + c4) return Q.items[kMatWard][gi - c1];
-    return Q.items[kMatVolumeInside][gi - c1 - c4];
-}
-
 // Vertex of a slot as the network sees it: hit point, normal facing the
 // outgoing direction (zero inside a volume), outgoing direction.
 __device__ __forceinline__ void vertex_of(const PathsView& P, uint32_t slot, float* x9) {
@@ -347,7 +334,7 @@ __device__ __forceinline__ void vertex_of(const PathsView& P, uint32_t slot, flo
 __global__ void __launch_bounds__(32 * kInferWarps, 4) k_guide_infer_paths(GuideView gv, PathsView P, QueueView Q,
                                                                             GuideRenderD gd) {
     __shared__ SmemFwd S;
-    const uint32_t n = guided_count(Q, gd);
+    const uint32_t n = guide_rows(Q, gd);
     if (blockIdx.x * kInferWarps * 16u >= n) return;
     load_weights(S.W, S.b, gv);
     __syncthreads();
@@ -357,7 +344,7 @@ __global__ void __launch_bounds__(32 * kInferWarps, 4) k_guide_infer_paths(Guide
         for (int h = 0; h < 2; ++h) {
             const uint32_t r = base + g + 8 * h;
             float x9[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
-            if (r < n) vertex_of(P, guided_slot(Q, r), x9);
+            if (r < n) vertex_of(P, guide_row_slot(Q, gd, r), x9);
             coords(x9, gv.params, v[h]);
         }
         uint32_t a[4][4];

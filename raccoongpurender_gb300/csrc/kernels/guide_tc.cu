@@ -179,15 +179,6 @@ __device__ __forceinline__ void row_mixture(const float* o, float4* dst) {
     dst[9] = make_float4(w[4] / den, w[5] / den, w[6] / den, w[7] / den);
 }
 
-__device__ __forceinline__ uint32_t guided_count_tc(const QueueView& Q, const GuideRenderD& gd) {
-    return Q.counts[kMatLambertian] + Q.counts[kMatWard] + (gd.volumes ? Q.counts[kMatVolumeInside] : 0u);
-}
-__device__ __forceinline__ uint32_t guided_slot_tc(const QueueView& Q, uint32_t gi) {
-    const uint32_t c1 = Q.counts[kMatLambertian], c4 = Q.counts[kMatWard];
-    if (gi < c1) return Q.items[kMatLambertian][gi];
-    if (gi < c1 + c4) return Q.items[kMatWard][gi - c1];
-    return Q.items[kMatVolumeInside][gi - c1 - c4];
-}
 __device__ __forceinline__ void vertex_of_tc(const PathsView& P, uint32_t slot, float* x9) {
     const float4 ro = P.ro[slot], rd = P.rd[slot], ng = P.ng[slot];
     x9[0] = ro.x + rd.x * ro.w;
@@ -217,7 +208,7 @@ __global__ void __launch_bounds__(kTcThreads) k_guide_infer_tc(GuideView gv, con
                                                                QueueView Q, GuideRenderD gd, uint32_t* err) {
     extern __shared__ unsigned char smem_raw[];
     SmemTc& S = *reinterpret_cast<SmemTc*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-    const uint32_t n = kPaths ? guided_count_tc(Q, gd) : nrows;
+    const uint32_t n = kPaths ? guide_rows(Q, gd) : nrows;
     if (blockIdx.x * kTcThreads >= n) return;
     const uint32_t t = threadIdx.x, warp = t >> 5;
     // the weights, already in the staged layout (wt_sw), by one bulk copy
@@ -261,7 +252,7 @@ __global__ void __launch_bounds__(kTcThreads) k_guide_infer_tc(GuideView gv, con
             float x9[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
             if (r < n) {
                 if (kPaths) {
-                    vertex_of_tc(P, guided_slot_tc(Q, r), x9);
+                    vertex_of_tc(P, guide_row_slot(Q, gd, r), x9);
                 } else {
 #pragma unroll
                     for (int c = 0; c < 9; ++c) x9[c] = rows[16 * (size_t)r + c];

@@ -700,8 +700,38 @@ __global__ void __launch_bounds__(256) k_shade(PathsView P, QueueView Q, RenderP
             if (k == kMatLambertian) gi = i - off[kMatLambertian];
             else if (k == kMatWard) gi = g4 + (i - off[kMatWard]);
             else if (k == kMatVolumeInside && rp.gd.volumes) gi = g6 + (i - off[kMatVolumeInside]);
+            if (gi != ~0u && rp.gd.max_depth) gi = rp.gd.remap[gi];  // its inference row, or unguided
         }
         shade_slot<kGuided>(rp.reqs[r], P, k, slot, gpix, rp.gd, gi);
+    }
+}
+
+// Depth-limited guiding: the guided items whose vertex is among the first
+// max_depth of its path (logic_i counts the path's segments so far) become
+// the inference rows, appended with one atomic per warp; the others keep
+// BSDF and envmap sampling.  The row order does not matter: a row's mixture
+// depends on that row alone.
+__global__ void __launch_bounds__(256) k_guide_select(PathsView P, QueueView Q, GuideRenderD gd) {
+    const uint32_t n = guided_items(Q, gd);
+    const int lane = threadIdx.x & 31;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t base = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); base < n; base += stride) {
+        const uint32_t gi = base + lane;
+        uint32_t slot = 0;
+        bool take = false;
+        if (gi < n) {
+            slot = guided_item_slot(Q, gi);
+            take = __float_as_uint(P.L[slot].w) <= gd.max_depth;
+        }
+        const unsigned m = __ballot_sync(0xffffffffu, take);
+        uint32_t first = 0;
+        if (lane == 0 && m) first = atomicAdd(gd.nsel, (uint32_t)__popc(m));
+        first = __shfl_sync(0xffffffffu, first, 0);
+        if (gi < n) {
+            const uint32_t row = first + (uint32_t)__popc(m & ((1u << lane) - 1u));
+            gd.remap[gi] = take ? row : ~0u;
+            if (take) gd.sel[row] = slot;
+        }
     }
 }
 
@@ -1106,6 +1136,11 @@ void launch_init(const PathsView& p, const QueueView& q, uint32_t seed_offset, c
 void launch_compact_new(const PathsView& p, const QueueView& q, cudaStream_t st) {
     k_compact_new<<<q.ntiles, 256, 0, st>>>(p, q);
 }
+void launch_guide_select(const PathsView& p, const QueueView& q, const GuideRenderD& gd, int grid, cudaStream_t st) {
+    cudaMemsetAsync(gd.nsel, 0, sizeof(uint32_t), st);
+    k_guide_select<<<grid, 256, 0, st>>>(p, q, gd);
+}
+
 void launch_shade(const PathsView& p, const QueueView& q, const RenderParams& rp, int grid, cudaStream_t st) {
     if (rp.gd.lobes)
         k_shade<true><<<grid, 256, 0, st>>>(p, q, rp);

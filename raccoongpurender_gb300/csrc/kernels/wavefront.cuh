@@ -135,8 +135,31 @@ struct GuideRenderD {
     float guide_frac;     // share of the non-envmap selection probability given to the guide
     int32_t volumes;      // guide in-volume vertices too
     int32_t record;       // record training samples
-    int32_t pad;
+    uint32_t max_depth;   // guide vertices 1..max_depth of a path only (0: all); then, per bounce:
+    uint32_t* sel;        //   the selected guided items' slots (the inference rows),
+    uint32_t* remap;      //   per guided item number its row, ~0u when not selected,
+    uint32_t* nsel;       //   and the number selected
 };
+
+// The guided items of this bounce as the shading kernel numbers them:
+// queue 1 (Lambertian), queue 4 (Ward), then queue 6 (in-volume) when
+// volumes are guided.
+__device__ __forceinline__ uint32_t guided_items(const QueueView& Q, const GuideRenderD& gd) {
+    return Q.counts[kMatLambertian] + Q.counts[kMatWard] + (gd.volumes ? Q.counts[kMatVolumeInside] : 0u);
+}
+__device__ __forceinline__ uint32_t guided_item_slot(const QueueView& Q, uint32_t gi) {
+    const uint32_t c1 = Q.counts[kMatLambertian], c4 = Q.counts[kMatWard];
+    if (gi < c1) return Q.items[kMatLambertian][gi];
+    if (gi < c1 + c4) return Q.items[kMatWard][gi - c1];
+    return Q.items[kMatVolumeInside][gi - c1 - c4];
+}
+// the inference rows: every guided item, or the selected ones
+__device__ __forceinline__ uint32_t guide_rows(const QueueView& Q, const GuideRenderD& gd) {
+    return gd.max_depth ? *gd.nsel : guided_items(Q, gd);
+}
+__device__ __forceinline__ uint32_t guide_row_slot(const QueueView& Q, const GuideRenderD& gd, uint32_t r) {
+    return gd.max_depth ? gd.sel[r] : guided_item_slot(Q, r);
+}
 
 struct RenderParams {
     const RequestD* reqs;             // device table, nreq entries, sample ranges ascending
@@ -151,6 +174,8 @@ struct RenderParams {
 void launch_init(const PathsView& p, const QueueView& q, uint32_t seed_offset, cudaStream_t st);
 void launch_compact_new(const PathsView& p, const QueueView& q, cudaStream_t st);
 void launch_shade(const PathsView& p, const QueueView& q, const RenderParams& rp, int grid, cudaStream_t st);
+// the guided items at vertices 1..gd.max_depth of their paths (gd.sel / remap / nsel; *nsel zeroed first)
+void launch_guide_select(const PathsView& p, const QueueView& q, const GuideRenderD& gd, int grid, cudaStream_t st);
 // How a bounce casts its extension rays: persistent = a separate persistent
 // closest-hit kernel over the slots just shaded (refilling warps, `grid`
 // CTAs, `counter` a device word it may use; launch_trace_paths, between the

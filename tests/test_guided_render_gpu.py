@@ -88,3 +88,15 @@ def test_tcgen05_guided_render_is_unbiased(rg):
     g.check()
     assert g.stats()["iterations"] > 50
     assert abs(guided.mean() / plain.mean() - 1.0) < 0.02
+
+
+def test_depth_limited_guide_is_unbiased(rg):
+    """Guiding only the first two vertices of each path (the selection pass
+    and the remapped inference rows) leaves the mean image unchanged."""
+    sm, cam = _scene(rg, "room")
+    plain = guiding.render_mean(rg, sm, cam, spp=512, seed_offset=1, path_count=1 << 18)
+    g = rg.Guide(0, max_depth=2)
+    guided = guiding.render_mean(rg, sm, cam, spp=512, seed_offset=1, path_count=1 << 18, guide=g)
+    g.check()
+    assert g.stats()["iterations"] > 20
+    assert abs(guided.mean() / plain.mean() - 1.0) < 0.02
