@@ -218,7 +218,7 @@ def load_library(build_if_missing: bool = True) -> C.CDLL:
 def _check(st: int, where: str) -> None:
     if st != RGR_OK:
         detail = load_library().rgr_last_error()
-        raise RgrError(st, where, detail.decode() if detail else "")
+        raise RgrError(st, where, detail.decode("utf-8", errors="replace") if detail else "")
 
 
 def _ptr(a: np.ndarray) -> int:
@@ -426,7 +426,7 @@ class AlembicStorage:
         _check(self._lib.rgr_alembic_describe(self._h, frame, None, 0, C.byref(need)), "rgr_alembic_describe")
         buf = C.create_string_buffer(need.value)
         _check(self._lib.rgr_alembic_describe(self._h, frame, buf, need.value, C.byref(need)), "rgr_alembic_describe")
-        return json.loads(buf.value.decode())
+        return json.loads(buf.value.decode("utf-8", errors="replace"))
 
 
 def render_config(**kw) -> rgr_render_config:

@@ -402,9 +402,11 @@ Sample Compound::array(const PropHeader& h, int64_t index) const {
         for (uint64_t i = 0; i + 8 <= dims.second; i += 8) {
             uint64_t v;
             std::memcpy(&v, dims.first + i, 8);
+            if (v != 0 && s.count > (1ull << 40) / v) throw Error("array dimensions too large in " + h.name);
             s.count *= v;
         }
     }
+    if (s.count > (1ull << 40) / (uint64_t)s.extent) throw Error("array too large in " + h.name);
     const uint64_t values = s.count * (uint64_t)s.extent;
     if (s.pod == kString ? s.strings.size() < values : s.bytes.size() < values * pod_bytes(s.pod))
         throw Error("short array sample of " + h.name);
@@ -940,10 +942,26 @@ struct Json {
     }
     void u(uint64_t v) { out += std::to_string(v); }
     void i(int64_t v) { out += std::to_string(v); }
+    static bool utf8(const std::string& t) {
+        for (size_t i = 0; i < t.size();) {
+            const unsigned char c = (unsigned char)t[i];
+            const int n = c < 0x80 ? 0 : (c >> 5) == 6 ? 1 : (c >> 4) == 14 ? 2 : (c >> 3) == 30 ? 3 : -1;
+            if (n < 0 || i + (size_t)n >= t.size()) return false;
+            for (int k = 1; k <= n; ++k)
+                if (((unsigned char)t[i + k] >> 6) != 2) return false;
+            i += (size_t)n + 1;
+        }
+        return true;
+    }
     void str(const std::string& t) {
+        const bool valid = utf8(t);  // otherwise bytes >= 0x80 are written as \u00XX
         out += '"';
         for (unsigned char c : t) {
-            if (c == '"' || c == '\\') {
+            if (!valid && c >= 0x80) {
+                char b[8];
+                std::snprintf(b, sizeof b, "\\u%04x", c);
+                out += b;
+            } else if (c == '"' || c == '\\') {
                 out += '\\';
                 out += (char)c;
             } else if (c < 0x20) {

@@ -265,3 +265,25 @@ def test_written_archive_reads_the_same_with_the_reference_reader(tmp_path):
     ref = json.loads(subprocess.run([str(tool), "dump", str(path), "0"], capture_output=True, text=True,
                                     check=True).stdout)
     assert rg.AlembicStorage(path).read(0) == ref
+
+
+def test_corrupted_archives_fail_cleanly(tmp_path):
+    """Random byte corruptions of a valid archive either still load or report
+    an error: the reader bounds every offset, size and count it reads."""
+    data = bytearray((G / "basic.abc").read_bytes())
+    shutil.copy(G / "sky_tiny.hdr", tmp_path / "sky_tiny.hdr")
+    rng = np.random.default_rng(11)
+    outcomes = {"ok": 0, "error": 0}
+    for trial in range(300):
+        bad = bytearray(data)
+        for pos in rng.integers(0, len(bad), size=int(rng.integers(1, 6))):
+            bad[pos] = int(rng.integers(0, 256))
+        path = tmp_path / "bad.abc"
+        path.write_bytes(bytes(bad))
+        try:
+            rg.AlembicStorage(path).read(0)
+            rg.SceneManager().addAlembic(path)
+            outcomes["ok"] += 1
+        except rg.RgrError:
+            outcomes["error"] += 1
+    assert outcomes["ok"] + outcomes["error"] == 300 and outcomes["error"] > 0
