@@ -147,6 +147,11 @@ RequestD request_d(const SceneView& sv, const rgr_camera& cam, const rgr_render_
 
 // scenes with fewer inner BVH nodes run the fused trace + logic kernel by default
 constexpr uint32_t kPersistentTraceMinNodes = 4096;
+// rgr_trace_closest: 2^20-ray chunks in flight on their own streams, so that
+// the copies of some overlap the traversal of another (measured end to end
+// on the closest-hit workload: 2 slots 2500 Mrays/s, 3: 2647, 4: 2705-2728,
+// 6: 2682, 8: 2627; 8 slots of 2^19 rays: 2749)
+constexpr int kTraceSlots = 4;
 
 struct rgr_context {
     int device = 0;
@@ -173,11 +178,11 @@ struct rgr_context {
     std::string graph_exec_key;  // graph_key() when graph_exec was captured
     // ray-cast service buffers
     DevBuf trays[7], tprim, tt, tread, tcounter;
-    // rgr_trace_closest pipeline: two stream slots, each with its chunk's buffers
+    // rgr_trace_closest pipeline: kTraceSlots stream slots, each with its chunk's buffers
     struct TraceSlot {
         DevBuf rays[7], prim, t, counter, err;
-    } tslot[2];
-    cudaStream_t stream2 = nullptr;
+    } tslot[kTraceSlots];
+    cudaStream_t tstream[kTraceSlots] = {};  // [0] unused: slot 0 runs on `stream`
     int trace_grid = 0;      // persistent traversal grid (SMs x resident blocks)
     int trace_refill = 24;   // refill a warp when this many lanes are idle (measured best of 1..32)
     int trace_blocks = 0;    // resident blocks per SM asked for (0: as many as fit)
@@ -193,7 +198,8 @@ struct rgr_context {
 
     ~rgr_context() {
         if (graph_exec) cudaGraphExecDestroy(graph_exec);
-        if (stream2) cudaStreamDestroy(stream2);
+        for (cudaStream_t s : tstream)
+            if (s) cudaStreamDestroy(s);
         if (stream) cudaStreamDestroy(stream);
     }
     // the resident path pool: state, queues, counters (WavefrontLane::setup, :451-522)
@@ -697,10 +703,10 @@ int rgr_trace_closest_counts_device(rgr_context* c, const rgr_ray_soa* rays, uin
     return RGR_OK;
 }
 
-// Host arrays in and out: the rays go in chunks of up to 2^20 alternating
-// over two streams, so that a chunk's copies overlap the traversal of the
-// previous one (with page-locked host memory; pageable memory still works,
-// its copies just do not overlap).
+// Host arrays in and out: the rays go in chunks of up to 2^20, round robin
+// over kTraceSlots streams, so that the copies of some chunks overlap the
+// traversal of another (with page-locked host memory; pageable memory still
+// works, its copies just do not overlap).
 int rgr_trace_closest(rgr_context* c, const rgr_ray_soa* rays, uint64_t n, int32_t* prim, float* t) {
     if (!c || !rays || !prim || !t) return RGR_E_INVALID;
     if (!c->scene.valid) return RGR_E_STATE;
@@ -709,12 +715,15 @@ int rgr_trace_closest(rgr_context* c, const rgr_ray_soa* rays, uint64_t n, int32
     for (int k = 0; k < 7; ++k)
         if (!src[k]) return RGR_E_INVALID;
     RGR_CUDA(cudaSetDevice(c->device));
-    if (!c->stream2) RGR_CUDA(cudaStreamCreateWithFlags(&c->stream2, cudaStreamNonBlocking));
+    cudaStream_t streams[kTraceSlots];
+    for (int s = 0; s < kTraceSlots; ++s) {
+        if (s > 0 && !c->tstream[s]) RGR_CUDA(cudaStreamCreateWithFlags(&c->tstream[s], cudaStreamNonBlocking));
+        streams[s] = s == 0 ? c->stream : c->tstream[s];
+    }
     const uint64_t kChunk = 1ull << 20;
     const uint64_t chunk = std::min(n, kChunk);
-    cudaStream_t streams[2] = {c->stream, c->stream2};
     int r;
-    for (int s = 0; s < 2; ++s) {
+    for (int s = 0; s < kTraceSlots; ++s) {
         rgr_context::TraceSlot& ts = c->tslot[s];
         for (int k = 0; k < 7; ++k)
             if ((r = ts.rays[k].alloc(4 * chunk)) != RGR_OK) return r;
@@ -724,7 +733,7 @@ int rgr_trace_closest(rgr_context* c, const rgr_ray_soa* rays, uint64_t n, int32
         RGR_CUDA(cudaMemsetAsync(ts.err.p, 0, 4, streams[s]));
     }
     for (uint64_t off = 0, i = 0; off < n; off += chunk, ++i) {
-        const int s = (int)(i & 1u);
+        const int s = (int)(i % kTraceSlots);
         cudaStream_t st = streams[s];
         rgr_context::TraceSlot& ts = c->tslot[s];
         const uint64_t m = std::min(chunk, n - off);
@@ -739,12 +748,14 @@ int rgr_trace_closest(rgr_context* c, const rgr_ray_soa* rays, uint64_t n, int32
         RGR_CUDA(cudaMemcpyAsync(prim + off, ts.prim.p, 4 * m, cudaMemcpyDeviceToHost, st));
         RGR_CUDA(cudaMemcpyAsync(t + off, ts.t.p, 4 * m, cudaMemcpyDeviceToHost, st));
     }
-    uint32_t err[2] = {0, 0};
-    for (int s = 0; s < 2; ++s) {
+    uint32_t err[kTraceSlots] = {};
+    uint32_t any = 0;
+    for (int s = 0; s < kTraceSlots; ++s) {
         RGR_CUDA(cudaMemcpyAsync(&err[s], c->tslot[s].err.p, 4, cudaMemcpyDeviceToHost, streams[s]));
         RGR_CUDA(cudaStreamSynchronize(streams[s]));
+        any |= err[s];
     }
-    if (err[0] | err[1]) {
+    if (any) {
         set_error("traversal stack overflow");
         return RGR_E_OVERFLOW;
     }
