@@ -599,13 +599,21 @@ def main() -> None:
                                              out_t[k].data_ptr())
             rg._check(st, "rgr_trace_closest")
 
-    e2e_step()
-    torch.cuda.synchronize(dev)
-    t0 = time.perf_counter()
-    for _ in range(args.e2e_steps):
+    def e2e_time() -> float:
         e2e_step()
-    torch.cuda.synchronize(dev)
-    e2e_s = (time.perf_counter() - t0) / args.e2e_steps
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        for _ in range(args.e2e_steps):
+            e2e_step()
+        torch.cuda.synchronize(dev)
+        return (time.perf_counter() - t0) / args.e2e_steps
+
+    # the default: the traversal kernel reads the pinned rays and writes the hits
+    # across the CPU-GPU link itself; for comparison, staged copies through device buffers
+    lane.set_trace_host_mode(rg.TRACE_HOST_COPY)
+    e2e_staged = rays_per_step / e2e_time() / 1e6
+    lane.set_trace_host_mode(rg.TRACE_HOST_AUTO)
+    e2e_s = e2e_time()
     e2e_value = rays_per_step / e2e_s / 1e6
     # the e2e hits must equal the device-resident hits
     assert (out_prim[0].numpy() == sets[0][1].cpu().numpy()).all()
@@ -659,7 +667,10 @@ def main() -> None:
                                                for t in trace_trials],
                            "parallelism": f"replicas{world}"},
                 "e2e": {"value": round(e2e_value, 1), "unit": "Mrays/s", "h2d_bytes_per_step": rays_per_step * 28,
-                        "d2h_bytes_per_step": rays_per_step * 8},
+                        "d2h_bytes_per_step": rays_per_step * 8,
+                        "path": "rgr_trace_closest on page-locked host arrays: the traversal kernel reads the rays "
+                                "and writes the hits across NVLink-C2C (zero copy)",
+                        "staged_copies_value": round(e2e_staged, 1)},
                 "gpu_launches": 2 * args.steps, "roofline": roof, "cpu_baseline": cpu, "clocks": clocks,
                 "render": render, "bvh_build": bvh, "guiding": guide}
         print(json.dumps(line), flush=True)

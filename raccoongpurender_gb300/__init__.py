@@ -94,6 +94,7 @@ class rgr_guide_config(C.Structure):
 
 
 GUIDE_TCGEN05, GUIDE_MMA_SYNC = 0, 1  # rgr_guide_config.inference_kernel
+TRACE_HOST_AUTO, TRACE_HOST_COPY = 0, 1  # rgr_set_trace_host_mode
 
 
 class rgr_guide_stats(C.Structure):
@@ -164,6 +165,7 @@ _SIGS = {
                                                   C.c_void_p, C.c_void_p, C.c_void_p]),
     "rgr_set_trace_tuning": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32]),
     "rgr_set_trace_staging": (C.c_int, [C.c_void_p, C.c_uint32]),
+    "rgr_set_trace_host_mode": (C.c_int, [C.c_void_p, C.c_int32]),
     "rgr_set_render_trace": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32]),
     "rgr_set_render_tuning": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32]),
     "rgr_batch_create": (C.c_int, [C.c_void_p, C.c_int32, C.c_uint32]),
@@ -577,6 +579,11 @@ class WavefrontLane:
         fused (False), or by scene size (-1, the default)."""
         mode = persistent if isinstance(persistent, int) and not isinstance(persistent, bool) else int(bool(persistent))
         _check(self._lib.rgr_set_render_trace(self._h, mode, refill), "rgr_set_render_trace")
+
+    def set_trace_host_mode(self, mode: int) -> None:
+        """rgr_trace_closest with host arrays: TRACE_HOST_AUTO (zero copy where the
+        GPU can address them) or TRACE_HOST_COPY (chunked copies)."""
+        _check(self._lib.rgr_set_trace_host_mode(self._h, mode), "rgr_set_trace_host_mode")
 
     def set_trace_staging(self, staged_nodes: int) -> None:
         """Top BVH nodes each traversal CTA keeps in shared memory (0 = off)."""

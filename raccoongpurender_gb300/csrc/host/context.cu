@@ -183,6 +183,7 @@ struct rgr_context {
         DevBuf rays[7], prim, t, counter, err;
     } tslot[kTraceSlots];
     cudaStream_t tstream[kTraceSlots] = {};  // [0] unused: slot 0 runs on `stream`
+    int trace_host_mode = RGR_TRACE_HOST_AUTO;  // rgr_trace_closest: zero copy where it can, or staged copies
     int trace_grid = 0;      // persistent traversal grid (SMs x resident blocks)
     int trace_refill = 24;   // refill a warp when this many lanes are idle (measured best of 1..32)
     int trace_blocks = 0;    // resident blocks per SM asked for (0: as many as fit)
@@ -677,6 +678,12 @@ int rgr_set_render_trace(rgr_context* c, int32_t persistent, int32_t refill) {
     return RGR_OK;
 }
 
+int rgr_set_trace_host_mode(rgr_context* c, int32_t mode) {
+    if (!c || (mode != RGR_TRACE_HOST_AUTO && mode != RGR_TRACE_HOST_COPY)) return RGR_E_INVALID;
+    c->trace_host_mode = mode;
+    return RGR_OK;
+}
+
 int rgr_set_trace_staging(rgr_context* c, uint32_t staged_nodes) {
     if (!c || staged_nodes > kMaxStagedNodes) return RGR_E_INVALID;
     RGR_CUDA(cudaSetDevice(c->device));
@@ -707,6 +714,23 @@ int rgr_trace_closest_counts_device(rgr_context* c, const rgr_ray_soa* rays, uin
 // over kTraceSlots streams, so that the copies of some chunks overlap the
 // traversal of another (with page-locked host memory; pageable memory still
 // works, its copies just do not overlap).
+namespace {
+// The address under which the GPU reads or writes host array p, or null:
+// page-locked (or registered) host memory has a device address; on a system
+// whose GPU walks the host's page tables (NVLink-C2C with address
+// translation) any host address is one.
+void* device_view(const void* p, bool pageable_ok) {
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    if (a.type == cudaMemoryTypeHost || a.type == cudaMemoryTypeManaged || a.type == cudaMemoryTypeDevice)
+        return a.devicePointer;
+    return pageable_ok ? const_cast<void*>(p) : nullptr;
+}
+}  // namespace
+
 int rgr_trace_closest(rgr_context* c, const rgr_ray_soa* rays, uint64_t n, int32_t* prim, float* t) {
     if (!c || !rays || !prim || !t) return RGR_E_INVALID;
     if (!c->scene.valid) return RGR_E_STATE;
@@ -715,6 +739,36 @@ int rgr_trace_closest(rgr_context* c, const rgr_ray_soa* rays, uint64_t n, int32
     for (int k = 0; k < 7; ++k)
         if (!src[k]) return RGR_E_INVALID;
     RGR_CUDA(cudaSetDevice(c->device));
+    int r;
+    if (c->trace_host_mode == RGR_TRACE_HOST_AUTO) {
+        // zero copy: the traversal kernel reads the rays from, and writes the hits to, host
+        // memory across the CPU-GPU link, one launch over all rays
+        int pageable = 0;
+        cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccessUsesHostPageTables, c->device);
+        const float* dsrc[7];
+        bool direct = true;
+        for (int k = 0; k < 7 && direct; ++k) direct = (dsrc[k] = (const float*)device_view(src[k], pageable)) != nullptr;
+        int32_t* dprim = direct ? (int32_t*)device_view(prim, pageable) : nullptr;
+        float* dt = direct ? (float*)device_view(t, pageable) : nullptr;
+        if (direct && dprim && dt) {
+            rgr_context::TraceSlot& ts = c->tslot[0];
+            if ((r = ts.counter.alloc(8)) != RGR_OK || (r = ts.err.alloc(16)) != RGR_OK) return r;
+            cudaStream_t st = c->stream;
+            RGR_CUDA(cudaMemsetAsync(ts.err.p, 0, 4, st));
+            launch_trace_rays(c->scene.sv, dsrc[0], dsrc[1], dsrc[2], dsrc[3], dsrc[4], dsrc[5], dsrc[6], n, dprim, dt,
+                              nullptr, ts.err.as<uint32_t>(), ts.counter.as<unsigned long long>(), c->trace_refill,
+                              c->trace_grid, c->trace_stage, st);
+            RGR_CUDA(cudaGetLastError());
+            uint32_t err = 0;
+            RGR_CUDA(cudaMemcpyAsync(&err, ts.err.p, 4, cudaMemcpyDeviceToHost, st));
+            RGR_CUDA(cudaStreamSynchronize(st));
+            if (err) {
+                set_error("traversal stack overflow");
+                return RGR_E_OVERFLOW;
+            }
+            return RGR_OK;
+        }
+    }
     cudaStream_t streams[kTraceSlots];
     for (int s = 0; s < kTraceSlots; ++s) {
         if (s > 0 && !c->tstream[s]) RGR_CUDA(cudaStreamCreateWithFlags(&c->tstream[s], cudaStreamNonBlocking));
@@ -722,7 +776,6 @@ int rgr_trace_closest(rgr_context* c, const rgr_ray_soa* rays, uint64_t n, int32
     }
     const uint64_t kChunk = 1ull << 20;
     const uint64_t chunk = std::min(n, kChunk);
-    int r;
     for (int s = 0; s < kTraceSlots; ++s) {
         rgr_context::TraceSlot& ts = c->tslot[s];
         for (int k = 0; k < 7; ++k)

@@ -119,22 +119,34 @@ def test_lbvh_built_on_gpu(rg, po):
         assert (q == p).mean() > 0.999
 
 
-def test_host_api_chunks(rg, po):
-    """rgr_trace_closest pipelines its rays in chunks of 2^20 over two streams:
-    a ragged count spanning several chunks gives the same hits as the
-    device-array entry point."""
+@pytest.mark.parametrize("mode,pinned", [("copy", False), ("copy", True), ("auto", False), ("auto", True)])
+def test_host_api(rg, po, mode, pinned):
+    """rgr_trace_closest with host arrays, both ways: chunks of 2^20 through
+    device buffers on four streams (a ragged count spanning several chunks),
+    and zero copy, the kernel reading and writing host memory (page-locked
+    arrays, or any where the GPU uses the host's page tables; otherwise the
+    copies).  The hits equal those of the device-array entry point."""
     torch = pytest.importorskip("torch")
     mesh = scenes.displaced_icosphere(5, seed=7)
     sm, _ = build(mesh)
     lane = rg.WavefrontLane(0, 1024)
     lane.setup(sm)
+    lane.set_trace_host_mode(rg.TRACE_HOST_COPY if mode == "copy" else rg.TRACE_HOST_AUTO)
     rays = scenes.random_rays(2_500_017, (-1.3, -1.3, -1.3), (1.3, 1.3, 1.3), seed=9)
-    prim, t = lane.trace_closest(rays)
-    soa = [torch.from_numpy(np.ascontiguousarray(a)).cuda() for a in rays.soa()]
+    host = [torch.from_numpy(np.ascontiguousarray(a)) for a in rays.soa()]
+    if pinned:
+        host = [a.pin_memory() for a in host]
+    hp = torch.full((len(rays),), -7, dtype=torch.int32)
+    ht = torch.zeros(len(rays), dtype=torch.float32)
+    if pinned:
+        hp, ht = hp.pin_memory(), ht.pin_memory()
+    r = rg.rgr_ray_soa(*[a.data_ptr() for a in host])
+    rg._check(lane._lib.rgr_trace_closest(lane.handle, rg.C.byref(r), len(rays), hp.data_ptr(), ht.data_ptr()), "t")
+    soa = [a.cuda() for a in host]
     p2 = torch.empty(len(rays), dtype=torch.int32, device="cuda")
     t2 = torch.empty(len(rays), dtype=torch.float32, device="cuda")
     torch.cuda.synchronize()  # the context stream does not wait for torch's stream
     lane.trace_closest_device([a.data_ptr() for a in soa], len(rays), p2.data_ptr(), t2.data_ptr())
     lane.synchronize()
-    assert (prim == p2.cpu().numpy()).all()
-    assert (bits(t) == bits(t2.cpu().numpy())).all()
+    assert (hp.numpy() == p2.cpu().numpy()).all()
+    assert (bits(ht.numpy()) == bits(t2.cpu().numpy())).all()
