@@ -549,6 +549,9 @@ def main() -> None:
         stream.synchronize()
         counts.append((float(nodes.double().mean()), float(prims.double().mean()), float((prim >= 0).double().mean())))
     bytes_per_ray = [28 + 8 + 64 * c[0] + 48 * c[1] for c in counts]
+    # FP32 operations per ray: 2 slab tests of 6 subtractions, 6 multiplications and
+    # 12 min/max each per inner node visited, about 40 per triangle test
+    flops_per_ray = [48 * c[0] + 40 * c[1] for c in counts]
 
     for _ in range(args.warmup):
         step()
@@ -628,6 +631,11 @@ def main() -> None:
             "traffic_note": "DRAM bytes per step (both launches) from ncu, profiles/k_trace_rays_closest_hit_1.31M.md;"
                             f" algorithmic bytes per step {int(coh_bytes + inc_bytes)}: the tree is L2-resident",
             "peak_source": peaks["source"] + " hbm_gbs",
+            "fp32": {"flops_per_ray": [round(f, 1) for f in flops_per_ray],
+                     "achieved_tflops": round((flops_per_ray[0] + flops_per_ray[1]) * n_each /
+                                              ((coh_ms + inc_ms) * 1e-3) / 1e12, 2),
+                     "note": "48 per inner node (two slab tests), 40 per triangle; far below the SMs' FP32 "
+                             "rate: the memory roof binds, and divergence (8 of 32 lanes) the kernel"},
             "per_set": {"coherent": {"ms": round(coh_ms, 3), "mrays_s": round(n_each / coh_ms / 1e3, 1),
                                      "nodes_per_ray": round(counts[0][0], 2), "prims_per_ray": round(counts[0][1], 2),
                                      "bytes_per_ray": round(bytes_per_ray[0], 1), "hit_rate": round(counts[0][2], 4)},
