@@ -269,11 +269,11 @@ rgr_context* rgr_batch_context(rgr_batch* b);
 typedef struct rgr_ray_soa {
     const float *ox, *oy, *oz, *dx, *dy, *dz, *tmax;
 } rgr_ray_soa;
-/* host arrays in, host arrays out.  RGR_TRACE_HOST_AUTO (default): when every array is
-   device-accessible host memory (page-locked, or any host memory on a system whose GPU
-   uses the host's page tables), one traversal launch reads the rays from and writes the
-   hits to host memory directly; otherwise, and with RGR_TRACE_HOST_COPY, the rays go
-   through device buffers in chunks of 2^20 on four streams, copies overlapping traversal. */
+/* host arrays in, host arrays out.  RGR_TRACE_HOST_AUTO (default): on a system whose GPU
+   shares the host's page tables (a coherent link such as NVLink-C2C), one traversal launch
+   reads the rays from and writes the hits to the host arrays directly (page-locked or
+   pageable); otherwise, and with RGR_TRACE_HOST_COPY, the rays go through device buffers
+   in chunks of 2^20 on four streams, copies overlapping traversal. */
 int rgr_trace_closest(rgr_context* c, const rgr_ray_soa* rays, uint64_t n, int32_t* prim, float* t);
 #define RGR_TRACE_HOST_AUTO 0
 #define RGR_TRACE_HOST_COPY 1

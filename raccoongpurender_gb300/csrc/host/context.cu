@@ -740,11 +740,12 @@ int rgr_trace_closest(rgr_context* c, const rgr_ray_soa* rays, uint64_t n, int32
         if (!src[k]) return RGR_E_INVALID;
     RGR_CUDA(cudaSetDevice(c->device));
     int r;
-    if (c->trace_host_mode == RGR_TRACE_HOST_AUTO) {
+    int pageable = 0;  // the GPU shares the host's page tables: a coherent CPU-GPU link (NVLink-C2C)
+    cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccessUsesHostPageTables, c->device);
+    if (c->trace_host_mode == RGR_TRACE_HOST_AUTO && pageable) {
         // zero copy: the traversal kernel reads the rays from, and writes the hits to, host
-        // memory across the CPU-GPU link, one launch over all rays
-        int pageable = 0;
-        cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccessUsesHostPageTables, c->device);
+        // memory across the link, one launch over all rays.  Over PCIe the staged copies
+        // below are faster, so zero copy is only taken on a coherent link.
         const float* dsrc[7];
         bool direct = true;
         for (int k = 0; k < 7 && direct; ++k) direct = (dsrc[k] = (const float*)device_view(src[k], pageable)) != nullptr;
