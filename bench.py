@@ -266,10 +266,11 @@ def bvh_bench(dev_index: int, mesh, sets, stream: int, sah_build_s: float) -> di
             "lbvh_inner_nodes": int(info.num_inner_nodes)}
 
 
-def guide_kernels_bench(dev_index: int) -> dict:
+def guide_kernels_bench(dev_index: int, inference_kernel: int | None = None) -> dict:
     """The guiding network's kernels on 2^18 random samples: one training
     iteration (forward + loss + backward on the tensor cores, gradient flush,
-    Adam) and inference, timed with CUDA events on the stream they run on.
+    Adam) and inference (the guide's default inference kernel, or
+    `inference_kernel`), timed with CUDA events on the stream they run on.
     FLOPs are the network's own (36-64-64-64-64-40: 34,304 per sample forward,
     2x that backward), not the zero padding the kernels also multiply."""
     import numpy as np
@@ -277,7 +278,7 @@ def guide_kernels_bench(dev_index: int) -> dict:
     import raccoongpurender_gb300 as rg
     n = 1 << 18
     fwd = 2 * (36 * 64 + 3 * 64 * 64 + 64 * 40)
-    g = rg.Guide(dev_index)
+    g = rg.Guide(dev_index) if inference_kernel is None else rg.Guide(dev_index, inference_kernel=inference_kernel)
     g.set_bounds((-1, -1, -1), (1, 1, 1))
     rng = np.random.default_rng(5)
     rows = np.zeros((n, 16), np.float32)
@@ -375,10 +376,11 @@ def scene_load_bench(repeats: int = 3) -> dict:
             "write_s": round(write_s, 2), "threads": 1}
 
 
-def guided_render_cost(dev_index: int, spp: int = 64) -> dict:
+def guided_render_cost(dev_index: int, spp: int = 64, inference_kernel: int | None = None) -> dict:
     """What a frozen guide costs per sample: the sky-lit room at 960x540
     rendered once guided while the guide trains, then plain and with the
-    (now frozen) guide at the same spp; wall times of the last two."""
+    (now frozen) guide at the same spp; wall times of the last two.  The
+    guide's default inference kernel, or `inference_kernel`."""
     import raccoongpurender_gb300 as rg
     from raccoongpurender_gb300 import guiding, scenes
     mesh, env, camd = scenes.sky_room(level=6)
@@ -389,7 +391,7 @@ def guided_render_cost(dev_index: int, spp: int = 64) -> dict:
     cam = rg.camera_look_at(camd["eye"], camd["target"], camd["up"], camd["vfov"], 960, 540)
     lane = rg.WavefrontLane(dev_index, 1 << 22)
     lane.setup(sm)
-    g = rg.Guide(dev_index)
+    g = rg.Guide(dev_index) if inference_kernel is None else rg.Guide(dev_index, inference_kernel=inference_kernel)
     guiding.render(rg, sm, cam, spp, 77, guide=g, lane=lane)
     g.set_config(train=0)
     _, _, tp = guiding.render(rg, sm, cam, spp, 5, lane=lane)

@@ -358,10 +358,11 @@ typedef struct rgr_guide_config {
                                 envmap sampling stay; guiding it doubles the largest per-vertex weight) */
     uint32_t train_interval; /* bounces per training iteration (1): samples of all of them feed it */
     uint32_t max_iterations; /* stop training (and recording samples) after this many iterations (0: never) */
-    int32_t inference_kernel; /* RGR_GUIDE_MMA_SYNC (default): warp-level mma.sync with the whole
-                                 network in register fragments; RGR_GUIDE_TCGEN05: tcgen05.mma with
-                                 TMEM accumulators, one thread per row (1.9x slower for this
-                                 64-wide network: the per-row scalar work, not the MMA, bounds it) */
+    int32_t inference_kernel; /* RGR_GUIDE_TCGEN05 (default): tcgen05.mma with TMEM accumulators and
+                                 activations, MMA-issuing warps apart from the row threads, two
+                                 tiles in flight per group (1.8x faster than mma.sync);
+                                 RGR_GUIDE_MMA_SYNC: warp-level mma.sync with the whole network in
+                                 register fragments.  Training always runs on mma.sync kernels. */
     uint32_t max_depth;      /* guide only the first max_depth vertices of a path (0: every vertex); the
                                 others use BSDF and envmap sampling alone and cost no inference */
     uint64_t seed;           /* weight initialisation (1) */

@@ -171,7 +171,7 @@ void rgr_guide_config_default(rgr_guide_config* c) {
     c->guide_volumes = 0;
     c->train_interval = 1;
     c->max_iterations = 0;
-    c->inference_kernel = RGR_GUIDE_MMA_SYNC;
+    c->inference_kernel = RGR_GUIDE_TCGEN05;
     c->max_depth = 0;
     c->seed = 1;
 }
@@ -259,11 +259,22 @@ int rgr_guide_set_weights(rgr_guide* g, const float* w, const float* b) {
     }
     std::vector<uint16_t> hbf(kGuideWeights);
     for (int i = 0; i < kGuideWeights; ++i) hbf[i] = to_bf16(w[i]);
-    std::vector<unsigned char> hsw(kGuideWtBytes);
-    for (uint32_t l = 0; l < (uint32_t)kGuideLayers; ++l)
+    std::vector<unsigned char> hsw(kGuideWtBytes, 0);
+    for (uint32_t l = 0; l < (uint32_t)kGuideLayers; ++l) {
         for (uint32_t in = 0; in < 64; ++in)
             for (uint32_t out = 0; out < 64; ++out)
                 memcpy(&hsw[wt_sw_offset(l, in, out)], &hbf[(l * 64 + in) * 64 + out], 2);
+        for (uint32_t out = 0; out < 64; ++out) {  // after the weights: layer 0's sits on padding inputs
+            const float bias = b[l * 64 + out];
+            const uint16_t hi = to_bf16(bias);
+            const uint32_t hi_bits = (uint32_t)hi << 16;
+            float hi_f;
+            memcpy(&hi_f, &hi_bits, 4);
+            const uint16_t lo = to_bf16(bias - hi_f);
+            memcpy(&hsw[wt_bias_offset(l, out, 0)], &hi, 2);
+            memcpy(&hsw[wt_bias_offset(l, out, 1)], &lo, 2);
+        }
+    }
     RGR_CUDA(cudaSetDevice(g->device));
     RGR_CUDA(cudaDeviceSynchronize());
     RGR_CUDA(cudaMemcpy(g->w.p, w, 4 * kGuideWeights, cudaMemcpyHostToDevice));

@@ -50,7 +50,13 @@ struct GuideView {
     GuideParams params;
 };
 
-constexpr uint32_t kGuideWtBytes = kGuideLayers * 64 * 128;
+// wt_sw: the five W^T tiles (8 KB each), then per layer a 16-wide K chunk
+// (64 output rows x 16 bf16, 2 KB) whose columns 0 and 1 hold each bias as the
+// sum of two bf16 values; the tcgen05 kernel multiplies it by a chunk of ones
+// to start the accumulator at the bias (layers 1..4; layer 0's chunk stays
+// zero, wt_bias_offset).
+constexpr uint32_t kGuideWtMainBytes = kGuideLayers * 64 * 128;
+constexpr uint32_t kGuideWtBytes = kGuideWtMainBytes + kGuideLayers * 64 * 32;
 
 // byte offset of 16-byte chunk c of row r in a K-major 128-byte-swizzled tile
 // (the chunk sits at position c ^ (r % 8) of its 128-byte line; 8-line groups
@@ -61,6 +67,24 @@ __host__ __device__ __forceinline__ uint32_t sw128_offset(uint32_t r, uint32_t c
 // where weight W[l][in][out] lives in wt_sw
 __host__ __device__ __forceinline__ uint32_t wt_sw_offset(uint32_t l, uint32_t in, uint32_t out) {
     return l * 8192u + sw128_offset(out, in >> 3) + (in & 7u) * 2u;
+}
+// byte offset of element (r, k) of a K-major 16-wide chunk without swizzle:
+// 8-row x 16-byte core matrices, the two K halves 128 bytes apart, 8-row
+// groups 256 bytes apart
+__host__ __device__ __forceinline__ uint32_t k16_offset(uint32_t r, uint32_t k) {
+    return (r >> 3) * 256u + (k >> 3) * 128u + (r & 7u) * 16u + (k & 7u) * 2u;
+}
+// where part h (0: bf16 of the bias, 1: bf16 of the remainder) of the bias of
+// output `out` of layer l lives in wt_sw.  Layer 0's rides on the padding
+// inputs 36 and 37 of its W^T tile instead (the kernel sets those inputs to
+// 1.0), which saves that layer the bias chunk's MMA.
+__host__ __device__ __forceinline__ uint32_t wt_bias_offset(uint32_t l, uint32_t out, uint32_t h) {
+    return l == 0u ? wt_sw_offset(0u, (uint32_t)kGuideInputs + h, out)
+                   : kGuideWtMainBytes + l * 2048u + k16_offset(out, h);
+}
+// W^T entries of wt_sw that hold layer 0's bias, not a (zero) padding weight
+__host__ __device__ __forceinline__ bool wt_is_bias_slot(uint32_t l, uint32_t in) {
+    return l == 0u && (in == (uint32_t)kGuideInputs || in == (uint32_t)kGuideInputs + 1u);
 }
 
 // ------------------------------------------------------------ vMF mixture

@@ -557,7 +557,13 @@ __global__ void k_guide_adam(GuideView g, const uint32_t* count, uint32_t min_co
         const __nv_bfloat16 h = __float2bfloat16_rn(nv);
         g.wbf[i] = h;
         const uint32_t l = (uint32_t)i / 4096u, in = ((uint32_t)i / 64u) % 64u, out = (uint32_t)i % 64u;
-        *reinterpret_cast<__nv_bfloat16*>(g.wt_sw + wt_sw_offset(l, in, out)) = h;
+        if (!wt_is_bias_slot(l, in)) *reinterpret_cast<__nv_bfloat16*>(g.wt_sw + wt_sw_offset(l, in, out)) = h;
+    } else {
+        const uint32_t j = (uint32_t)(i - kGuideWeights), l = j / 64u, out = j % 64u;
+        const __nv_bfloat16 hi = __float2bfloat16_rn(nv);
+        const __nv_bfloat16 lo = __float2bfloat16_rn(nv - __bfloat162float(hi));
+        *reinterpret_cast<__nv_bfloat16*>(g.wt_sw + wt_bias_offset(l, out, 0)) = hi;
+        *reinterpret_cast<__nv_bfloat16*>(g.wt_sw + wt_bias_offset(l, out, 1)) = lo;
     }
 }
 

@@ -79,11 +79,12 @@ def test_trained_guide_lowers_error_in_the_sky_room(rg):
     assert e_guided < 0.75 * e_plain
 
 
-def test_tcgen05_guided_render_is_unbiased(rg):
-    """The same guided render with the tcgen05/TMEM inference kernel."""
+def test_mma_sync_guided_render_is_unbiased(rg):
+    """The same guided render with the mma.sync inference kernel (the default
+    is the tcgen05/TMEM one)."""
     sm, cam = _scene(rg, "room")
     plain = guiding.render_mean(rg, sm, cam, spp=512, seed_offset=1, path_count=1 << 18)
-    g = rg.Guide(0, inference_kernel=rg.GUIDE_TCGEN05)
+    g = rg.Guide(0, inference_kernel=rg.GUIDE_MMA_SYNC)
     guided = guiding.render_mean(rg, sm, cam, spp=512, seed_offset=1, path_count=1 << 18, guide=g)
     g.check()
     assert g.stats()["iterations"] > 50
