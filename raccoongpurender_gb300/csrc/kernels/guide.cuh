@@ -93,52 +93,39 @@ __device__ __forceinline__ float vmf_pdf(float kappa, float c) {
     return kappa / (6.283185307179586f * -expm1f(-2.0f * kappa)) * expf(kappa * (c - 1.0f));
 }
 
-// Inferred mixture of one guided vertex: lobes[i] = (mean, kappa), weights in
-// w[0..7] (normalised).
-struct GuideMixture {
-    float4 lobe[kGuideLobes];
-    float w[kGuideLobes];
-};
-__device__ __forceinline__ void load_mixture(const float4* p, GuideMixture& m) {
-#pragma unroll
-    for (int i = 0; i < kGuideLobes; ++i) m.lobe[i] = p[i];
-    const float4 a = p[8], b = p[9];
-    m.w[0] = a.x;
-    m.w[1] = a.y;
-    m.w[2] = a.z;
-    m.w[3] = a.w;
-    m.w[4] = b.x;
-    m.w[5] = b.y;
-    m.w[6] = b.z;
-    m.w[7] = b.w;
-}
-__device__ __forceinline__ float mixture_pdf(const GuideMixture& m, float dx, float dy, float dz) {
-    float p = 0.0f;
+// The inferred mixture of one guided vertex, kGuideLobeVecs float4 in
+// global memory: p[i] = (mean, kappa) of lobe i, p[8], p[9] = the eight
+// normalised weights.  The shading kernel reads it where it needs it (through
+// the read-only cache) instead of holding its 40 floats in registers.
+__device__ __forceinline__ float mixture_pdf(const float4* p, float dx, float dy, float dz) {
+    const float4 wa = __ldg(p + 8), wb = __ldg(p + 9);
+    const float w[kGuideLobes] = {wa.x, wa.y, wa.z, wa.w, wb.x, wb.y, wb.z, wb.w};
+    float pdf = 0.0f;
 #pragma unroll
     for (int i = 0; i < kGuideLobes; ++i) {
-        const float c = m.lobe[i].x * dx + m.lobe[i].y * dy + m.lobe[i].z * dz;
-        p += m.w[i] * vmf_pdf(m.lobe[i].w, c);
+        const float4 L = __ldg(p + i);
+        pdf += w[i] * vmf_pdf(L.w, L.x * dx + L.y * dy + L.z * dz);
     }
-    return p;
+    return pdf;
 }
 // Sample the mixture with three uniforms: lobe by weight, then the vMF
 // cosine by inversion (W = 1 + log(u + (1 - u) e^{-2 kappa}) / kappa) and a
 // uniform azimuth in the lobe's frame (Frisvad / Duff branchless basis).
-__device__ __forceinline__ void mixture_sample(const GuideMixture& m, float u0, float u1, float u2, float* d) {
+__device__ __forceinline__ void mixture_sample(const float4* p, float u0, float u1, float u2, float* d) {
+    const float4 wa = __ldg(p + 8), wb = __ldg(p + 9);
+    const float w[kGuideLobes] = {wa.x, wa.y, wa.z, wa.w, wb.x, wb.y, wb.z, wb.w};
     int k = kGuideLobes - 1;
     float acc = 0.0f;
 #pragma unroll
     for (int i = 0; i < kGuideLobes - 1; ++i) {
-        acc += m.w[i];
+        acc += w[i];
         if (u0 < acc && k == kGuideLobes - 1) k = i;
     }
-    float4 L = m.lobe[0];  // m.lobe[k] by selects: a run-time index would put the mixture in local memory
-#pragma unroll
-    for (int i = 1; i < kGuideLobes; ++i) L = (k == i) ? m.lobe[i] : L;
+    const float4 L = __ldg(p + k);
     const float kappa = L.w;
-    float w = 1.0f + logf(u1 + (1.0f - u1) * expf(-2.0f * kappa)) / kappa;
-    w = fminf(fmaxf(w, -1.0f), 1.0f);
-    const float s = sqrtf(fmaxf(0.0f, 1.0f - w * w));
+    float wc = 1.0f + logf(u1 + (1.0f - u1) * expf(-2.0f * kappa)) / kappa;
+    wc = fminf(fmaxf(wc, -1.0f), 1.0f);
+    const float s = sqrtf(fmaxf(0.0f, 1.0f - wc * wc));
     float sp, cp;
     sincospif(2.0f * u2, &sp, &cp);
     const float sign = L.z >= 0.0f ? 1.0f : -1.0f;
@@ -146,9 +133,9 @@ __device__ __forceinline__ void mixture_sample(const GuideMixture& m, float u0, 
     const float bb = L.x * L.y * a;
     const float tx = 1.0f + sign * L.x * L.x * a, ty = sign * bb, tz = -sign * L.x;
     const float bx = bb, by = sign + L.y * L.y * a, bz = -L.y;
-    float x = w * L.x + s * (cp * tx + sp * bx);
-    float y = w * L.y + s * (cp * ty + sp * by);
-    float z = w * L.z + s * (cp * tz + sp * bz);
+    float x = wc * L.x + s * (cp * tx + sp * bx);
+    float y = wc * L.y + s * (cp * ty + sp * by);
+    float z = wc * L.z + s * (cp * tz + sp * bz);
     const float n = sqrtf(x * x + y * y + z * z);
     d[0] = x / n;
     d[1] = y / n;

@@ -306,17 +306,14 @@ RGR_DEV void shade_slot(const RequestD& rq, const PathsView& P, int k, uint32_t 
             envq = is.strategy == kEnv ? sq : eq;
         }
     }
-    GuideMixture mix;
-    if (kGuided && gi != ~0u) {
-        load_mixture(gd.lobes + (size_t)kGuideLobeVecs * gi, mix);
-        if (is.strategy == kGuide) {
-            const float u0 = rng.uniform();
-            const float u1 = rng.uniform();
-            const float u2 = rng.uniform();
-            float d[3];
-            mixture_sample(mix, u0, u1, u2, d);
-            is.wi = mk(d[0], d[1], d[2]);
-        }
+    const float4* mix = (kGuided && gi != ~0u) ? gd.lobes + (size_t)kGuideLobeVecs * gi : nullptr;
+    if (kGuided && gi != ~0u && is.strategy == kGuide) {
+        const float u0 = rng.uniform();
+        const float u1 = rng.uniform();
+        const float u2 = rng.uniform();
+        float d[3];
+        mixture_sample(mix, u0, u1, u2, d);
+        is.wi = mk(d[0], d[1], d[2]);
     }
     const size_t count = (size_t)sc.env_w * sc.env_h;
     // sample_envmap_6axis_stage / sample_envmap_stage (envmap_sampling.cl:169-248)
@@ -663,7 +660,7 @@ __global__ void __launch_bounds__(256) k_compact_new(PathsView P, QueueView Q) {
 }
 
 template <bool kGuided>
-__global__ void __launch_bounds__(256) k_shade(PathsView P, QueueView Q, RenderParams rp) {
+__device__ __forceinline__ void shade_items(const PathsView& P, const QueueView& Q, const RenderParams& rp) {
     uint32_t off[kNumQueues + 1];
     off[0] = 0;
 #pragma unroll
@@ -704,6 +701,21 @@ __global__ void __launch_bounds__(256) k_shade(PathsView P, QueueView Q, RenderP
         }
         shade_slot<kGuided>(rp.reqs[r], P, k, slot, gpix, rp.gd, gi);
     }
+}
+
+// The plain and guided shading kernels: one queue item per thread, all
+// queues in one launch.  Their launch bounds differ: the plain kernel's
+// registers are left to the compiler, the guided one is held to
+// RGR_SHADE_GUIDED_MIN_BLOCKS resident blocks per SM.
+#ifndef RGR_SHADE_GUIDED_MIN_BLOCKS
+#define RGR_SHADE_GUIDED_MIN_BLOCKS 3
+#endif
+__global__ void __launch_bounds__(256) k_shade(PathsView P, QueueView Q, RenderParams rp) {
+    shade_items<false>(P, Q, rp);
+}
+__global__ void __launch_bounds__(256, RGR_SHADE_GUIDED_MIN_BLOCKS) k_shade_guided(PathsView P, QueueView Q,
+                                                                                  RenderParams rp) {
+    shade_items<true>(P, Q, rp);
 }
 
 // Depth-limited guiding: the guided items whose vertex is among the first
@@ -1143,9 +1155,9 @@ void launch_guide_select(const PathsView& p, const QueueView& q, const GuideRend
 
 void launch_shade(const PathsView& p, const QueueView& q, const RenderParams& rp, int grid, cudaStream_t st) {
     if (rp.gd.lobes)
-        k_shade<true><<<grid, 256, 0, st>>>(p, q, rp);
+        k_shade_guided<<<grid, 256, 0, st>>>(p, q, rp);
     else
-        k_shade<false><<<grid, 256, 0, st>>>(p, q, rp);
+        k_shade<<<grid, 256, 0, st>>>(p, q, rp);
 }
 void launch_trace_paths(const PathsView& p, const QueueView& q, const RenderParams& rp, const TraceShape& ts,
                         cudaStream_t st) {
