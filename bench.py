@@ -320,7 +320,8 @@ def guiding_bench(dev_index: int, w: int = 960, h: int = 540, spp: int = 256, re
     given the same wall time: "cold" (the guide starts untrained and trains
     online on the render's own samples for its first 120 iterations, then is
     frozen; inference and training inside the time) and "warm" (a guide
-    trained online by an earlier 1024-spp render of the same view, frozen).  Medians over 3 seeds.  Scenes: the full-render glossy/volume scene (the 1.31M-triangle
+    trained online by an earlier 1024-spp render of the same view, frozen; in
+    the room also by a 4096-spp render).  Medians over 3 seeds.  Scenes: the full-render glossy/volume scene (the 1.31M-triangle
     sphere, ground, volume box, sky + sun) and the sky-lit room."""
     import raccoongpurender_gb300 as rg
     from raccoongpurender_gb300 import guiding, scenes
@@ -338,7 +339,8 @@ def guiding_bench(dev_index: int, w: int = 960, h: int = 540, spp: int = 256, re
         t0 = time.perf_counter()
         ref = guiding.render_mean(rg, sm, cam, spp=ref_spp, seed_offset=1 << 30, path_count=1 << 22)
         ref_s = time.perf_counter() - t0
-        r = guiding.equal_time(rg, sm, cam, ref, spp, path_count=1 << 22, guide_kw=dict(max_iterations=120))
+        r = guiding.equal_time(rg, sm, cam, ref, spp, path_count=1 << 22, guide_kw=dict(max_iterations=120),
+                               longer_warm_spp=(4096,) if name == "sky_room" else ())
         r.update({"resolution": f"{w}x{h}", "reference_spp": ref_spp, "reference_s": round(ref_s, 2),
                   "triangles": int(mesh.ntris)})
         out[name] = r

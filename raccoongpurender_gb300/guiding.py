@@ -56,7 +56,8 @@ def render_mean(rg, scene, cam, spp: int, seed_offset: int, path_count: int = 1 
 
 
 def equal_time(rg, scene, cam, ref: np.ndarray, spp_plain: int, path_count: int = 1 << 22, seed_offset: int = 1,
-               guide_kw: dict | None = None, repeats: int = 3, warm_spp: int | None = None) -> dict:
+               guide_kw: dict | None = None, repeats: int = 3, warm_spp: int | None = None,
+               longer_warm_spp: tuple = ()) -> dict:
     """Plain rendering at spp_plain against guided rendering given the same
     wall time, relMSE against `ref` (medians over `repeats` seeds: single
     sun-caustic samples of radiance ~1e4 dominate individual runs).
@@ -65,7 +66,9 @@ def equal_time(rg, scene, cam, ref: np.ndarray, spp_plain: int, path_count: int 
       warm: a guide trained online, without an iteration limit, by an earlier
             render of the same view at warm_spp (default 4 x spp_plain)
             samples per pixel, then frozen (no training cost), as when a guide
-            persists across the frames of an interactive session.
+            persists across the frames of an interactive session;
+      warm_<n>spp: the same with a guide trained by an n-spp render, for each
+            n in longer_warm_spp.
     The guided spp for each is calibrated from a guided run at spp_plain."""
     guide_kw = dict(guide_kw or {})
     lane = rg.WavefrontLane(0, path_count)
@@ -95,33 +98,39 @@ def equal_time(rg, scene, cam, ref: np.ndarray, spp_plain: int, path_count: int 
         cold_t.append(t)
         cold_e.append(relmse(mean_image(acc), ref))
     # warm: trained by an earlier render of the same view, frozen
-    warm_kw = dict(guide_kw)
-    warm_kw["max_iterations"] = 0
-    trained = rg.Guide(0, **warm_kw)
-    render(rg, scene, cam, warm_spp or 4 * spp_plain, seed_offset + (repeats + 3) * path_count, lane=lane,
-           guide=trained)
-    warm_iters = trained.stats()["iterations"]
-    trained.set_config(train=0)
-    _, _, tw = render(rg, scene, cam, spp_plain, seed_offset + 7, lane=lane, guide=trained)
-    spp_warm = max(1, int(spp_plain * tp / tw))
-    warm_t, warm_e, warm_same = [], [], []
-    for sd in seeds:
-        _, acc, t = render(rg, scene, cam, spp_warm, sd, lane=lane, guide=trained)
-        warm_t.append(t)
-        warm_e.append(relmse(mean_image(acc), ref))
-        _, acc, _ = render(rg, scene, cam, spp_plain, sd, lane=lane, guide=trained)
-        warm_same.append(relmse(mean_image(acc), ref))
-    ec, ew = float(np.median(cold_e)), float(np.median(warm_e))
-    return {
+    def warm(train_spp: int) -> dict:
+        warm_kw = dict(guide_kw)
+        warm_kw["max_iterations"] = 0
+        trained = rg.Guide(0, **warm_kw)
+        render(rg, scene, cam, train_spp, seed_offset + (repeats + 3) * path_count, lane=lane, guide=trained)
+        warm_iters = trained.stats()["iterations"]
+        trained.set_config(train=0)
+        _, _, tw = render(rg, scene, cam, spp_plain, seed_offset + 7, lane=lane, guide=trained)
+        spp_warm = max(1, int(spp_plain * tp / tw))
+        warm_t, warm_e, warm_same = [], [], []
+        for sd in seeds:
+            _, acc, t = render(rg, scene, cam, spp_warm, sd, lane=lane, guide=trained)
+            warm_t.append(t)
+            warm_e.append(relmse(mean_image(acc), ref))
+            _, acc, _ = render(rg, scene, cam, spp_plain, sd, lane=lane, guide=trained)
+            warm_same.append(relmse(mean_image(acc), ref))
+        ew = float(np.median(warm_e))
+        return {"spp": spp_warm, "time_s": round(float(np.median(warm_t)), 4), "relmse": ew,
+                "trained_by": f"{train_spp} spp render, {warm_iters} iterations",
+                "relmse_runs": [round(e, 6) for e in warm_e],
+                "relmse_ratio_equal_time": round(ep / ew, 3) if ew > 0 else None,
+                "relmse_same_spp": float(np.median(warm_same))}
+
+    ec = float(np.median(cold_e))
+    out = {
         "spp_plain": spp_plain, "time_plain_s": round(tp, 4), "relmse_plain": ep,
         "relmse_plain_runs": [round(e, 6) for e in plain_e],
         "cold": {"spp": spp_cold, "time_s": round(float(np.median(cold_t)), 4), "relmse": ec,
                  "relmse_runs": [round(e, 6) for e in cold_e],
                  "relmse_ratio_equal_time": round(ep / ec, 3) if ec > 0 else None,
                  "relmse_same_spp": float(np.median(same_e)), "training_iterations": int(np.median(iters))},
-        "warm": {"spp": spp_warm, "time_s": round(float(np.median(warm_t)), 4), "relmse": ew,
-                 "trained_by": f"{warm_spp or 4 * spp_plain} spp render, {warm_iters} iterations",
-                 "relmse_runs": [round(e, 6) for e in warm_e],
-                 "relmse_ratio_equal_time": round(ep / ew, 3) if ew > 0 else None,
-                 "relmse_same_spp": float(np.median(warm_same))},
+        "warm": warm(warm_spp or 4 * spp_plain),
     }
+    for n in longer_warm_spp:
+        out[f"warm_{n}spp"] = warm(n)
+    return out
