@@ -169,3 +169,27 @@ def test_tcgen05_and_mma_sync_agree(rg):
         outs.append(out.cpu().numpy())
     assert np.isfinite(outs[0]).all() and np.isfinite(outs[1]).all()
     assert _rel(outs[0], outs[1]) < 2e-3
+
+
+@pytest.mark.parametrize("n", [1, 127, 128, 129, 255, 256, 257, 38913])
+def test_tcgen05_ragged_row_counts(rg, n):
+    """Row counts around the 128-row tile and the 256 rows of one CTA's tiles
+    in flight: every row computed, nothing written past the last one."""
+    torch = _torch()
+    W, b = go.init_weights(6)
+    s = go.random_samples(n, seed=15)
+    rows = torch.from_numpy(s).cuda()
+    outs = []
+    for k in (rg.GUIDE_TCGEN05, rg.GUIDE_MMA_SYNC):
+        g = rg.Guide(0, inference_kernel=k)
+        g.set_weights(W, b)
+        g.set_bounds(LO, HI)
+        out = torch.full((n + 64, go.OUTPUTS), float("nan"), dtype=torch.float32, device="cuda")
+        g.infer_device(rows.data_ptr(), n, out.data_ptr())
+        torch.cuda.synchronize()
+        g.check()
+        outs.append(out.cpu().numpy())
+    tc, ms = outs
+    assert np.isfinite(tc[:n]).all()
+    assert np.isnan(tc[n:]).all()  # the rows after the last one are untouched
+    assert _rel(tc[:n], ms[:n]) < 2e-3
