@@ -3,9 +3,9 @@
 // tensor memory (TMEM) and the weights in shared memory.
 //
 // A CTA (one per SM) holds kTcGroups groups of 128 row threads and kMmaWarps
-// warps that only issue MMAs.  A group works on tiles of 128 rows, two tiles
-// in flight (buffers 0 and 1); thread t of the group owns row t of both from
-// the input encoding to the result.  Per tile in flight TMEM holds the
+// warps that only issue MMAs.  A group works on tiles of 128 rows, kBufs tiles
+// in flight (buffers); thread t of the group owns row t of each from the input
+// encoding to the result.  Per tile in flight TMEM holds the
 // 128 x 64 FP32 accumulator and the layer's input as 64 bf16 a row (lane =
 // row).  Per layer and buffer:
 //  * the row threads write the layer's input into TMEM (tcgen05.st): the
@@ -22,8 +22,8 @@
 //    to the buffer's d_full mbarrier;
 //  * the row threads wait on d_full (a bounded wait) and read the
 //    accumulators back (tcgen05.ld).
-// While the tensor core runs one buffer's layer, the row threads run the
-// other buffer's epilogue.  After the last layer each thread has its row's 40
+// While the tensor core runs one tile's layer, the row threads of the other
+// tiles (other groups, or the group's other buffers) run their epilogues.  After the last layer each thread has its row's 40
 // outputs in registers and computes the mixture (or keeps the raw outputs)
 // without any exchange; the tile's 160-byte results are staged in shared
 // memory and leave in one bulk copy.  Weights and bias chunks are staged once
@@ -37,18 +37,25 @@ namespace rgr {
 namespace dev {
 namespace {
 
-// 128-row groups of epilogue threads per CTA (each with two tiles in flight)
+// 128-row groups of row threads per CTA, and tiles in flight per group.  Five
+// groups of one tile each (2^18 rows: 19.0 us) beat two of two tiles (21.1 us)
+// and one of four or five (27 us): the row threads' encoding, epilogues and
+// mixtures, more than the MMAs, need the parallelism.  Five tiles of 96 TMEM
+// columns and the ones chunk fill the SM's 512 columns.
 #ifndef RGR_GUIDE_TC_GROUPS
-#define RGR_GUIDE_TC_GROUPS 2
+#define RGR_GUIDE_TC_GROUPS 5
 #endif
 constexpr int kTcGroups = RGR_GUIDE_TC_GROUPS;
-constexpr int kBufs = 2;                              // tiles in flight per group
+#ifndef RGR_GUIDE_TC_BUFS
+#define RGR_GUIDE_TC_BUFS 1
+#endif
+constexpr int kBufs = RGR_GUIDE_TC_BUFS;              // tiles in flight per group
 constexpr int kGroupThreads = 128;                    // rows per tile, one per thread
 // warps that issue the MMAs: warp kMmaWarp + m serves the buffers b = i kBufs + j
 // (group i, buffer j) with b % kMmaWarps == m (an issuing thread waits out
 // most of each MMA's issue latency, so buffers that share a warp share it)
 #ifndef RGR_GUIDE_TC_MMA_WARPS
-#define RGR_GUIDE_TC_MMA_WARPS 2
+#define RGR_GUIDE_TC_MMA_WARPS 3
 #endif
 constexpr int kMmaWarps = RGR_GUIDE_TC_MMA_WARPS;
 constexpr int kMmaWarp = kTcGroups * 4;               // the first MMA warp
@@ -349,12 +356,11 @@ __device__ __forceinline__ void issue_layer(uint32_t l, uint32_t tm, uint32_t ta
 // otherwise rows of 16 floats in `rows`, output 40 raw floats per row.
 //
 // Tile k of group g is tile (blockIdx.x + k gridDim.x) kTcGroups + g of the
-// rows; the group runs its tiles in pairs, tile k in buffer k % 2.  Per layer
-// and buffer the group's threads write the A tile and arrive on a_full; the
-// MMA warp, polling all a_full barriers, issues that buffer's next layer and
-// commits it to d_full; the threads wait on d_full and run the epilogue.  So
-// while the tensor core works on one buffer's layer the threads run the
-// other's epilogue.
+// rows; the group runs its tiles kBufs at a time, tile k in buffer k % kBufs.
+// Per layer and buffer the group's threads write the layer's input and arrive
+// on a_full; the MMA warp serving the buffer, polling its a_full barriers,
+// issues that buffer's next layer and commits it to d_full; the threads wait
+// on d_full and run the epilogue.
 template <bool kPaths>
 __global__ void __launch_bounds__(kTcThreads, 1)
     k_guide_infer_tc(GuideView gv, const float* __restrict__ rows, uint32_t nrows, float* __restrict__ out,
@@ -467,7 +473,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         const uint32_t lane_off = (32u * (warp & 3u)) << 16;  // this warp's 32 TMEM lanes
         const uint32_t kt = failed0 ? 0u : tiles_of(g);
         const uint32_t base = blockIdx.x * kTcGroups + g;
-        uint32_t pd[kBufs] = {0u, 0u};
+        uint32_t pd[kBufs] = {};
         bool timed_out = false;
         // inputs of the next pair, loaded while the current pair runs its layers
         RowIn in[kBufs] = {};
