@@ -142,7 +142,8 @@ def render_bench(dev_index: int, which: str, repeats: int = 2, pools=(1 << 22,))
              Lambertian/Ward/dielectric, 1024x512 sky + sun envmap,
              1920x1080, 64 spp, depth 8.
     Each resident-path pool size in `pools` is timed (2^22 is the reference's
-    kWavefrontPathCountGPU); the fastest is reported, all under by_pool."""
+    kWavefrontPathCountGPU; the Cornell box's 256x256x4 paths fit 2^18); the
+    fastest is reported, all under by_pool."""
     import raccoongpurender_gb300 as rg
     from raccoongpurender_gb300 import scenes
     if which == "cornell":
@@ -659,7 +660,7 @@ def main() -> None:
                                        "hit_rate": round(counts[1][2], 4)}}}
     render = None
     if not args.no_render:
-        render = {"cornell_256_4spp": render_bench(local, "cornell"),
+        render = {"cornell_256_4spp": render_bench(local, "cornell", pools=(1 << 18, 1 << 22)),
                   "mixed_1080p_64spp": render_bench(local, "mixed", pools=(1 << 22, 1 << 23)),
                   "batch_32_requests": batch_bench(local),
                   "scene_load_alembic": scene_load_bench()}
