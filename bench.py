@@ -661,7 +661,7 @@ def main() -> None:
     render = None
     if not args.no_render:
         render = {"cornell_256_4spp": render_bench(local, "cornell", pools=(1 << 18, 1 << 22)),
-                  "mixed_1080p_64spp": render_bench(local, "mixed", pools=(1 << 22, 1 << 23)),
+                  "mixed_1080p_64spp": render_bench(local, "mixed", pools=(1 << 22, 1 << 23, 1 << 24)),
                   "batch_32_requests": batch_bench(local),
                   "scene_load_alembic": scene_load_bench()}
     bvh = bvh_bench(local, mesh, [([a.data_ptr() for a in soa], n, prim.data_ptr(), t.data_ptr())

@@ -24,7 +24,7 @@ import time
 from pathlib import Path
 
 DEFAULTS = dict(path_count=1 << 22, graph_steps=8, shade_blocks=8)
-CANDIDATES = dict(path_count=[1 << 20, 1 << 21, 1 << 22, 1 << 23], graph_steps=[4, 8, 16], shade_blocks=[4, 8, 16])
+CANDIDATES = dict(path_count=[1 << 20, 1 << 21, 1 << 22, 1 << 23, 1 << 24], graph_steps=[4, 8, 16], shade_blocks=[4, 8, 16])
 TRACE_DEFAULTS = dict(trace_refill=24, trace_stage=0)
 TRACE_CANDIDATES = dict(trace_refill=[8, 16, 24, 32], trace_stage=[0, 64, 256, 1024])
 
