@@ -359,8 +359,8 @@ typedef struct rgr_guide_config {
     uint32_t train_interval; /* bounces per training iteration (1): samples of all of them feed it */
     uint32_t max_iterations; /* stop training (and recording samples) after this many iterations (0: never) */
     int32_t inference_kernel; /* RGR_GUIDE_TCGEN05 (default): tcgen05.mma with TMEM accumulators and
-                                 activations, MMA-issuing warps apart from the row threads, two
-                                 tiles in flight per group (1.8x faster than mma.sync);
+                                 activations, MMA-issuing warps apart from the row threads, five
+                                 128-row tiles in flight per SM (2x faster than mma.sync);
                                  RGR_GUIDE_MMA_SYNC: warp-level mma.sync with the whole network in
                                  register fragments.  Training always runs on mma.sync kernels. */
     uint32_t max_depth;      /* guide only the first max_depth vertices of a path (0: every vertex); the
