@@ -308,7 +308,7 @@ struct rgr_context {
         }
         const size_t n = (size_t)ntiles * kTile;
         int r;
-        if ((r = globes.alloc(16 * kGuideLobeVecs * n)) != RGR_OK) return r;
+        if ((r = globes.alloc(16 * kGuideMixVecs * n)) != RGR_OK) return r;
         if ((r = grecords.alloc(16 * 5 * kGuideRecords * n)) != RGR_OK) return r;
         if ((r = gnrec.alloc(n)) != RGR_OK) return r;
         if (guide->cfg.max_depth) {
@@ -328,7 +328,7 @@ struct rgr_context {
             if ((r = guide->set_bounds(lo, hi)) != RGR_OK) return r;
         }
         GuideRenderD& gd = rp.gd;
-        gd.lobes = globes.as<float4>();
+        gd.lobes = globes.as<uint4>();
         gd.records = grecords.as<float4>();
         gd.nrec = gnrec.as<uint8_t>();
         gd.train = guide->train;

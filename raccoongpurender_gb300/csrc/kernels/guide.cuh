@@ -11,6 +11,7 @@
 // so every sample stays unbiased whatever the network has learned.
 #pragma once
 #include <cuda_bf16.h>
+#include <cuda_fp16.h>
 
 #include "wavefront.cuh"
 
@@ -93,17 +94,44 @@ __device__ __forceinline__ float vmf_pdf(float kappa, float c) {
     return kappa / (6.283185307179586f * -expm1f(-2.0f * kappa)) * expf(kappa * (c - 1.0f));
 }
 
-// The inferred mixture of one guided vertex, kGuideLobeVecs float4 in
-// global memory: p[i] = (mean, kappa) of lobe i, p[8], p[9] = the eight
-// normalised weights.  The shading kernel reads it where it needs it (through
-// the read-only cache) instead of holding its 40 floats in registers.
-__device__ __forceinline__ float mixture_pdf(const float4* p, float dx, float dy, float dz) {
-    const float4 wa = __ldg(p + 8), wb = __ldg(p + 9);
-    const float w[kGuideLobes] = {wa.x, wa.y, wa.z, wa.w, wb.x, wb.y, wb.z, wb.w};
+// The inferred mixture of one guided vertex as the shading kernel reads it,
+// kGuideMixVecs 16-byte words in global memory (FP16): lobe i's mean xyz and
+// kappa in halves 4i..4i+3, the eight weights in halves 32..39.  Sampling and
+// the pdf decode it the same way (means and weights normalised after the
+// FP16 rounding), so the density evaluated is exactly the one sampled.
+__device__ __forceinline__ uint32_t half2_bits(float lo, float hi) {
+    const __half2 h = __floats2half2_rn(lo, hi);
+    return *reinterpret_cast<const uint32_t*>(&h);
+}
+__device__ __forceinline__ float2 half2_float2(uint32_t v) {
+    return __half22float2(*reinterpret_cast<const __half2*>(&v));
+}
+// lobe i of the record: unit mean (xyz) and kappa (w)
+__device__ __forceinline__ float4 mixture_lobe(const uint4* p, int i) {
+    const uint2 q = __ldg(reinterpret_cast<const uint2*>(p) + i);
+    const float2 xy = half2_float2(q.x), zk = half2_float2(q.y);
+    const float inv = 1.0f / sqrtf(fmaxf(xy.x * xy.x + xy.y * xy.y + zk.x * zk.x, 1.0e-30f));
+    return make_float4(xy.x * inv, xy.y * inv, zk.x * inv, zk.y);
+}
+// the eight weights of the record, normalised
+__device__ __forceinline__ void mixture_weights(const uint4* p, float* w) {
+    const uint4 q = __ldg(p + 4);
+    const float2 a = half2_float2(q.x), b = half2_float2(q.y), c = half2_float2(q.z), d = half2_float2(q.w);
+    w[0] = a.x, w[1] = a.y, w[2] = b.x, w[3] = b.y, w[4] = c.x, w[5] = c.y, w[6] = d.x, w[7] = d.y;
+    float sum = 0.0f;
+#pragma unroll
+    for (int i = 0; i < kGuideLobes; ++i) sum += w[i];
+    const float inv = 1.0f / fmaxf(sum, 1.0e-30f);
+#pragma unroll
+    for (int i = 0; i < kGuideLobes; ++i) w[i] *= inv;
+}
+__device__ __forceinline__ float mixture_pdf(const uint4* p, float dx, float dy, float dz) {
+    float w[kGuideLobes];
+    mixture_weights(p, w);
     float pdf = 0.0f;
 #pragma unroll
     for (int i = 0; i < kGuideLobes; ++i) {
-        const float4 L = __ldg(p + i);
+        const float4 L = mixture_lobe(p, i);
         pdf += w[i] * vmf_pdf(L.w, L.x * dx + L.y * dy + L.z * dz);
     }
     return pdf;
@@ -111,9 +139,9 @@ __device__ __forceinline__ float mixture_pdf(const float4* p, float dx, float dy
 // Sample the mixture with three uniforms: lobe by weight, then the vMF
 // cosine by inversion (W = 1 + log(u + (1 - u) e^{-2 kappa}) / kappa) and a
 // uniform azimuth in the lobe's frame (Frisvad / Duff branchless basis).
-__device__ __forceinline__ void mixture_sample(const float4* p, float u0, float u1, float u2, float* d) {
-    const float4 wa = __ldg(p + 8), wb = __ldg(p + 9);
-    const float w[kGuideLobes] = {wa.x, wa.y, wa.z, wa.w, wb.x, wb.y, wb.z, wb.w};
+__device__ __forceinline__ void mixture_sample(const uint4* p, float u0, float u1, float u2, float* d) {
+    float w[kGuideLobes];
+    mixture_weights(p, w);
     int k = kGuideLobes - 1;
     float acc = 0.0f;
 #pragma unroll
@@ -121,7 +149,7 @@ __device__ __forceinline__ void mixture_sample(const float4* p, float u0, float 
         acc += w[i];
         if (u0 < acc && k == kGuideLobes - 1) k = i;
     }
-    const float4 L = __ldg(p + k);
+    const float4 L = mixture_lobe(p, k);
     const float kappa = L.w;
     float wc = 1.0f + logf(u1 + (1.0f - u1) * expf(-2.0f * kappa)) / kappa;
     wc = fminf(fmaxf(wc, -1.0f), 1.0f);

@@ -357,10 +357,10 @@ __global__ void __launch_bounds__(32 * kInferWarps, 4) k_guide_infer_paths(Guide
             mixture_quad(o, h, L, w);
             const uint32_t r = base + g + 8 * h;
             if (r >= n) continue;
-            float4* dst = gd.lobes + (size_t)kGuideLobeVecs * r;
-            dst[2 * q] = make_float4(L[0].mx, L[0].my, L[0].mz, L[0].kappa);
-            dst[2 * q + 1] = make_float4(L[1].mx, L[1].my, L[1].mz, L[1].kappa);
-            reinterpret_cast<float2*>(dst + 8)[q] = make_float2(w[0], w[1]);
+            uint4* dst = gd.lobes + (size_t)kGuideMixVecs * r;  // FP16 record (guide.cuh)
+            dst[q] = make_uint4(half2_bits(L[0].mx, L[0].my), half2_bits(L[0].mz, L[0].kappa),
+                                half2_bits(L[1].mx, L[1].my), half2_bits(L[1].mz, L[1].kappa));
+            reinterpret_cast<uint32_t*>(dst + 4)[q] = half2_bits(w[0], w[1]);
         }
     }
 }

@@ -25,8 +25,9 @@
 // While the tensor core runs one tile's layer, the row threads of the other
 // tiles (other groups, or the group's other buffers) run their epilogues.  After the last layer each thread has its row's 40
 // outputs in registers and computes the mixture (or keeps the raw outputs)
-// without any exchange; the tile's 160-byte results are staged in shared
-// memory and leave in one bulk copy.  Weights and bias chunks are staged once
+// without any exchange; the tile's results (80-byte FP16 mixture records, or
+// 160 bytes of raw outputs) are staged in shared memory and leave in one bulk
+// copy.  Weights and bias chunks are staged once
 // per CTA by one bulk copy.  Every wait is bounded: on a timeout the CTA
 // records an error, stops issuing and frees its TMEM.
 #include <cuda_bf16.h>
@@ -76,7 +77,7 @@ constexpr uint32_t kErrTimeout = 1u;
 
 struct __align__(1024) SmemTc {
     unsigned char wt[kGuideWtBytes];                // the staged weights and bias chunks (50 x 1024 B)
-    unsigned char out[kTcGroups][128 * 160];        // a tile's 160-byte output rows, stored by one bulk copy
+    unsigned char out[kTcGroups][128 * 160];        // a tile's output rows (80 or 160 bytes), stored by one bulk copy
     unsigned long long wbar;                        // the weights' bulk copy
     unsigned long long a_full[kTcGroups][kBufs];    // the A tile of the next layer is written (128 arrivals)
     unsigned long long d_full[kTcGroups][kBufs];    // the layer's MMAs are done (one commit)
@@ -273,11 +274,11 @@ __device__ __forceinline__ float tanh_approx(float x) {
 }
 __device__ __forceinline__ float softplus_fast(float x) { return x > 20.0f ? x : __logf(1.0f + __expf(x)); }
 
-// The mixture of one row's 40 raw outputs (field-major), the functions of
-// guide_mlp.cu's lobe_of in hardware approximations: the mixture only has to
-// be the one the shading kernel samples and evaluates, which reads it from
-// here.
-__device__ __forceinline__ void row_mixture(const float* o, float4* dst) {
+// The mixture of one row's 40 raw outputs (field-major) as the FP16 record
+// the shading kernel reads (guide.cuh), the functions of guide_mlp.cu's
+// lobe_of in hardware approximations: the mixture only has to be the one the
+// shading kernel samples and evaluates, which decodes it from here.
+__device__ __forceinline__ void row_mixture(const float* o, uint4* dst) {
     float w[kGuideLobes], mx = -3.0e38f;
 #pragma unroll
     for (int i = 0; i < kGuideLobes; ++i) {
@@ -285,17 +286,21 @@ __device__ __forceinline__ void row_mixture(const float* o, float4* dst) {
         mx = fmaxf(mx, w[i]);
     }
     float den = 0.0f;
+    uint2 lobe[kGuideLobes];
 #pragma unroll
     for (int i = 0; i < kGuideLobes; ++i) {
         const float x = o[i], y = o[8 + i], z = o[16 + i];
         const float inv = rsqrtf(fmaxf(x * x + y * y + z * z, 1.0e-24f));
-        dst[i] = make_float4(x * inv, y * inv, z * inv, fminf(softplus_fast(o[24 + i]) + 0.01f, kGuideKappaMax));
+        lobe[i] = make_uint2(half2_bits(x * inv, y * inv),
+                             half2_bits(z * inv, fminf(softplus_fast(o[24 + i]) + 0.01f, kGuideKappaMax)));
         w[i] = __expf(w[i] - mx);
         den += w[i];
     }
     const float r = 1.0f / den;
-    dst[8] = make_float4(w[0] * r, w[1] * r, w[2] * r, w[3] * r);
-    dst[9] = make_float4(w[4] * r, w[5] * r, w[6] * r, w[7] * r);
+#pragma unroll
+    for (int i = 0; i < 4; ++i) dst[i] = make_uint4(lobe[2 * i].x, lobe[2 * i].y, lobe[2 * i + 1].x, lobe[2 * i + 1].y);
+    dst[4] = make_uint4(half2_bits(w[0] * r, w[1] * r), half2_bits(w[2] * r, w[3] * r), half2_bits(w[4] * r, w[5] * r),
+                        half2_bits(w[6] * r, w[7] * r));
 }
 
 // The 48 bytes a row's input comes from: the slot's (ro, rd, ng) for a
@@ -532,19 +537,22 @@ __global__ void __launch_bounds__(kTcThreads, 1)
                         timed_out = true;
                         break;
                     }
-                    // the row's 160-byte result (mixture or raw outputs), then the
-                    // tile's rows to global memory in one bulk copy
-                    float4* row_out = reinterpret_cast<float4*>(S.out[g] + 160u * lt);
+                    // the row's result (the 80-byte FP16 mixture record, or the 160
+                    // bytes of raw outputs), then the tile's rows to global memory
+                    // in one bulk copy
+                    constexpr uint32_t kRowBytes = kPaths ? 16u * kGuideMixVecs : 4u * kGuideOutputs;
+                    unsigned char* row_out = S.out[g] + kRowBytes * lt;
                     if (r < n) {
                         float of[40];
 #pragma unroll
                         for (int q = 0; q < 40; ++q) of[q] = __uint_as_float(o[q]);
                         if (kPaths) {
-                            row_mixture(of, row_out);
+                            row_mixture(of, reinterpret_cast<uint4*>(row_out));
                         } else {
 #pragma unroll
                             for (int q = 0; q < kGuideOutputs / 4; ++q)
-                                row_out[q] = make_float4(of[4 * q], of[4 * q + 1], of[4 * q + 2], of[4 * q + 3]);
+                                reinterpret_cast<float4*>(row_out)[q] =
+                                    make_float4(of[4 * q], of[4 * q + 1], of[4 * q + 2], of[4 * q + 3]);
                         }
                     }
                     fence_async_smem();
@@ -554,8 +562,8 @@ __global__ void __launch_bounds__(kTcThreads, 1)
                             kPaths ? reinterpret_cast<unsigned char*>(gd.lobes) : reinterpret_cast<unsigned char*>(out);
                         asm volatile(
                             "cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;\n"
-                            "cp.async.bulk.commit_group;\n" ::"l"(dst + (size_t)160u * tile * 128u),
-                            "r"(smem_u32(S.out[g])), "r"(160u * min(128u, n - tile * 128u))
+                            "cp.async.bulk.commit_group;\n" ::"l"(dst + (size_t)kRowBytes * tile * 128u),
+                            "r"(smem_u32(S.out[g])), "r"(kRowBytes * min(128u, n - tile * 128u))
                             : "memory");
                     }
                 }

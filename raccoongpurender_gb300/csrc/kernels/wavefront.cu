@@ -306,7 +306,7 @@ RGR_DEV void shade_slot(const RequestD& rq, const PathsView& P, int k, uint32_t 
             envq = is.strategy == kEnv ? sq : eq;
         }
     }
-    const float4* mix = (kGuided && gi != ~0u) ? gd.lobes + (size_t)kGuideLobeVecs * gi : nullptr;
+    const uint4* mix = (kGuided && gi != ~0u) ? gd.lobes + (size_t)kGuideMixVecs * gi : nullptr;
     if (kGuided && gi != ~0u && is.strategy == kGuide) {
         const float u0 = rng.uniform();
         const float u1 = rng.uniform();

@@ -119,7 +119,7 @@ struct GuideTrainD {
 };
 constexpr uint32_t kLossHist = 4096;
 constexpr int kGuideRecords = 3;   // training records kept per path (its first guided vertices)
-constexpr int kGuideLobeVecs = 10;  // float4 per inferred mixture: 8 x (mean, kappa) + 2 x 4 weights
+constexpr int kGuideMixVecs = 5;    // 16-byte words per inferred mixture: 8 x FP16 (mean xyz, kappa) + 8 FP16 weights
 
 // training still wanted (iteration budget not used up)
 __device__ __forceinline__ bool guide_training_open(const GuideTrainD& t) {
@@ -128,7 +128,7 @@ __device__ __forceinline__ bool guide_training_open(const GuideTrainD& t) {
 
 // per-render guiding state the wavefront kernels read
 struct GuideRenderD {
-    float4* lobes;        // kGuideLobeVecs per guided queue item of this bounce
+    uint4* lobes;         // kGuideMixVecs per guided queue item of this bounce
     float4* records;      // per slot kGuideRecords x 5 float4
     uint8_t* nrec;        // records written on the slot's current path
     GuideTrainD train;
