@@ -403,8 +403,14 @@ int rgr_guide_infer_device(rgr_guide* g, const float* rows, uint32_t n, float* o
 int rgr_guide_train_device(rgr_guide* g, const float* samples, uint32_t n, float weight_scale, int32_t apply_adam,
                            float* grads, float* loss, void* stream);
 int rgr_guide_stats_get(rgr_guide* g, rgr_guide_stats* st);
-/* RGR_OK, or RGR_E_CUDA when a tensor-core wait of the guide's kernels timed out */
+/* RGR_OK, or RGR_E_CUDA when a tensor-core wait of the guide's kernels timed out since the
+   last check (each wait gives up after about a second; the kernel then stops, frees its
+   tensor memory and records the error, and the guide stays usable) */
 int rgr_guide_check(rgr_guide* g);
+/* Failure-detection tests: with on != 0 the MMA-issuing warps of the tcgen05 inference kernel
+   issue nothing, so its row threads' waits run out and the next rgr_guide_check reports it.
+   No GPU fault is involved. */
+int rgr_guide_set_stall(rgr_guide* g, int32_t on);
 /* losses of the last min(max, iterations) iterations, oldest first; *count receives how many */
 int rgr_guide_loss_history(rgr_guide* g, float* out, uint32_t max, uint32_t* count);
 /* the training samples of the last iteration of a guided render (16 floats each, as

@@ -193,6 +193,7 @@ _SIGS = {
     "rgr_guide_loss_history": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p]),
     "rgr_guide_last_batch": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p]),
     "rgr_guide_check": (C.c_int, [C.c_void_p]),
+    "rgr_guide_set_stall": (C.c_int, [C.c_void_p, C.c_int32]),
 }
 
 _lib = None
@@ -675,8 +676,13 @@ class Guide:
         return loss.value
 
     def check(self) -> None:
-        """Raise if a tensor-core wait of the guide's kernels timed out."""
+        """Raise if a tensor-core wait of the guide's kernels timed out since the last check."""
         _check(self._lib.rgr_guide_check(self._h), "rgr_guide_check")
+
+    def set_stall(self, on: bool) -> None:
+        """Failure-detection tests: the tcgen05 inference kernel's MMA warps issue
+        nothing while on, so its bounded waits run out (rgr_guide_set_stall)."""
+        _check(self._lib.rgr_guide_set_stall(self._h, 1 if on else 0), "rgr_guide_set_stall")
 
     def stats(self) -> dict:
         st = rgr_guide_stats()

@@ -346,9 +346,16 @@ int rgr_guide_check(rgr_guide* g) {
     uint32_t e = 0;
     RGR_CUDA(cudaMemcpy(&e, g->error_word(), 4, cudaMemcpyDeviceToHost));
     if (e) {
+        RGR_CUDA(cudaMemset(g->error_word(), 0, 4));  // reported once; the guide stays usable
         set_error("guide: a tensor-core wait timed out (error bits " + std::to_string(e) + ")");
         return RGR_E_CUDA;
     }
+    return RGR_OK;
+}
+
+int rgr_guide_set_stall(rgr_guide* g, int32_t on) {
+    if (!g) return RGR_E_INVALID;
+    g->view.stall_mma = on ? 1u : 0u;
     return RGR_OK;
 }
 

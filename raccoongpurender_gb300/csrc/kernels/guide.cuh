@@ -49,6 +49,8 @@ struct GuideView {
     float* v;
     float* loss;           // sum of sample losses of the last batch
     GuideParams params;
+    uint32_t stall_mma;    // failure-detection tests: the tcgen05 inference kernel's MMA warps
+                           // issue nothing, so its row threads' bounded waits run out
 };
 
 // wt_sw: the five W^T tiles (8 KB each), then per layer a 16-wide K chunk

@@ -71,8 +71,8 @@ constexpr uint32_t kAccCols = 96;
 constexpr uint32_t kOnesCol = kAccs * kAccCols;
 constexpr int kTcCols = 512;                          // TMEM columns allocated (a power of two)
 static_assert(kOnesCol + 32 <= (uint32_t)kTcCols, "TMEM columns");
-constexpr uint32_t kWaitLimit = 1u << 26;             // mbarrier polls before giving up
-constexpr uint32_t kIdleLimit = 1u << 24;             // MMA-warp polling rounds without progress before giving up
+constexpr uint32_t kWaitNs = 1000000000u;             // a wait gives up after 1 s (%globaltimer)
+constexpr uint32_t kWaitPolls = 1u << 30;             // and after this many polls whatever the timer says
 constexpr uint32_t kErrTimeout = 1u;
 
 struct __align__(1024) SmemTc {
@@ -135,10 +135,21 @@ __device__ __forceinline__ bool mbar_try_wait(uint32_t mbar, uint32_t parity) {
         : "memory");
     return ok != 0u;
 }
-// bounded wait for the phase with the given parity; false after kWaitLimit polls
+// low 32 bits of %globaltimer (ns): differences stay right across its
+// 4.3 s wrap, far longer than kWaitNs
+__device__ __forceinline__ uint32_t global_ns() {
+    uint32_t t;
+    asm volatile("mov.u32 %0, %%globaltimer_lo;" : "=r"(t));
+    return t;
+}
+// bounded wait for the phase with the given parity: false after kWaitNs (or
+// kWaitPolls polls)
 __device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity) {
-    for (uint32_t i = 0; i < kWaitLimit; ++i)
+    const uint32_t t0 = global_ns();
+    for (uint32_t i = 0; i < kWaitPolls; ++i) {
         if (mbar_try_wait(mbar, parity)) return true;
+        if ((i & 63u) == 63u && global_ns() - t0 > kWaitNs) return false;
+    }
     return false;
 }
 // true in one lane of the (converged) warp
@@ -434,7 +445,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         uint32_t left[kTcGroups][kBufs], lay[kTcGroups][kBufs], ph[kTcGroups][kBufs];
 #pragma unroll
         for (int i = 0; i < kTcGroups; ++i) {
-            const uint32_t k = failed0 ? 0u : tiles_of(i);
+            const uint32_t k = (failed0 || gv.stall_mma) ? 0u : tiles_of(i);  // a stalled warp issues nothing
 #pragma unroll
             for (int j = 0; j < kBufs; ++j) {
                 const bool mine = (uint32_t)((i * kBufs + j) % kMmaWarps) == mw;
@@ -443,6 +454,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
                 ph[i][j] = 0u;
             }
         }
+        uint32_t last = global_ns();  // when the warp last issued
         uint32_t idle = 0;
         for (;;) {
             bool any = false, progressed = false;
@@ -468,8 +480,9 @@ __global__ void __launch_bounds__(kTcThreads, 1)
             }
             if (!any) break;
             idle = progressed ? 0u : idle + 1u;
-            if (idle > kIdleLimit) {
-                if (elect_one()) S.error = kErrTimeout;
+            if (progressed) last = global_ns();
+            if (idle >= kWaitPolls || ((idle & 63u) == 63u && global_ns() - last > kWaitNs)) {
+                if (elect_one()) S.error = kErrTimeout;  // no buffer became ready within the limit
                 break;
             }
         }
@@ -512,7 +525,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
                 for (int j = 0; j < kBufs; ++j) {
                     if ((uint32_t)j >= nb) break;
                     const uint32_t tile = base + (k + j) * stride, r = tile * 128u + lt;
-                    if (!mbar_wait(smem_u32(&S.d_full[g][j]), pd[j])) {
+                    if (timed_out || !mbar_wait(smem_u32(&S.d_full[g][j]), pd[j])) {  // after one timeout, no more waits
                         timed_out = true;
                         S.error = kErrTimeout;
                     }

@@ -193,3 +193,34 @@ def test_tcgen05_ragged_row_counts(rg, n):
     assert np.isfinite(tc[:n]).all()
     assert np.isnan(tc[n:]).all()  # the rows after the last one are untouched
     assert _rel(tc[:n], ms[:n]) < 2e-3
+
+
+def test_tcgen05_wait_timeout_is_reported_and_the_guide_recovers(rg):
+    """Failure detection without a GPU fault: with its MMA warps stalled the
+    tcgen05 inference kernel's row threads wait about a second, give up,
+    free their tensor memory and record the error; rgr_guide_check reports it
+    once, and the next inference computes the right values."""
+    import time
+    torch = _torch()
+    W, b = go.init_weights(8)
+    s = go.random_samples(5000, seed=16)
+    rows = torch.from_numpy(s).cuda()
+    g = rg.Guide(0, inference_kernel=rg.GUIDE_TCGEN05)
+    g.set_weights(W, b)
+    g.set_bounds(LO, HI)
+    out = torch.zeros((len(s), go.OUTPUTS), dtype=torch.float32, device="cuda")
+    g.set_stall(True)
+    t0 = time.perf_counter()
+    g.infer_device(rows.data_ptr(), len(s), out.data_ptr())
+    torch.cuda.synchronize()
+    waited = time.perf_counter() - t0
+    with pytest.raises(RuntimeError, match="timed out"):
+        g.check()
+    assert 0.5 < waited < 30.0
+    g.check()  # reported once
+    g.set_stall(False)
+    g.infer_device(rows.data_ptr(), len(s), out.data_ptr())
+    torch.cuda.synchronize()
+    g.check()
+    ref, _ = go.forward(W, b, go.encode(s[:, 0:9], LO, IE), bf16_round=True)
+    assert _rel(out.cpu().numpy(), ref) < 1e-2
