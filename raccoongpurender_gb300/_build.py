@@ -48,8 +48,10 @@ def _cuda_flags() -> list[str]:
 
 
 def _cxx_flags() -> list[str]:
+    # the CUDA include directory for the header-only NVTX ranges of the host sources
+    cuda_include = Path(_nvcc()).resolve().parent.parent / "include"
     return ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall", "-Wno-unused-function",
-            "-I", str(ROOT / "include")]
+            "-I", str(ROOT / "include"), "-I", str(cuda_include)]
 
 
 def _digest(paths: list[Path], extra: str) -> str:

@@ -49,6 +49,7 @@
 #include <vector>
 
 #include "../rgr_internal.h"
+#include "nvtx.h"
 
 namespace rgr {
 namespace abc {
@@ -1442,6 +1443,7 @@ int rgr_alembic_describe(rgr_alembic* a, uint32_t frame, char* buf, uint64_t cap
 }
 
 int rgr_alembic_load(rgr_alembic* a, uint32_t frame, rgr_scene* scene, rgr_alembic_info* info) {
+    RGR_NVTX_RANGE("rgr_alembic_load");
     if (!a || !scene) return RGR_E_INVALID;
     try {
         using namespace rgr::abc;

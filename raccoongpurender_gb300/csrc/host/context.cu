@@ -15,6 +15,7 @@
 #include "../rgr_internal.h"
 #include "devbuf.h"
 #include "guide_host.h"
+#include "nvtx.h"
 
 using namespace rgr;
 using namespace rgr::dev;
@@ -459,6 +460,7 @@ int rgr_set_graph_mode(rgr_context* c, int32_t enabled) {
 }
 
 int rgr_device_upload(rgr_context* c, const rgr_scene* s) {
+    RGR_NVTX_RANGE("rgr_device_upload");
     if (!c || !s) return RGR_E_INVALID;
     RGR_CUDA(cudaSetDevice(c->device));
     int r = c->scene.upload(s, c->stream);
@@ -470,6 +472,7 @@ int rgr_device_upload(rgr_context* c, const rgr_scene* s) {
 }
 
 int rgr_render_begin(rgr_context* c, const rgr_camera* cam, const rgr_render_config* cfg) {
+    RGR_NVTX_RANGE("rgr_render_begin");
     if (!c || !cam) return RGR_E_INVALID;
     if (!c->scene.valid) {
         set_error("rgr_render_begin: upload a scene first");
@@ -511,6 +514,7 @@ int rgr_context_set_guide(rgr_context* c, rgr_guide* g) {
 }
 
 int rgr_render_step(rgr_context* c, int32_t steps) {
+    RGR_NVTX_RANGE("rgr_render_step");
     if (!c || steps < 0) return RGR_E_INVALID;
     if (!c->begun) return RGR_E_STATE;
     RGR_CUDA(cudaSetDevice(c->device));
@@ -533,6 +537,7 @@ int rgr_synchronize(rgr_context* c) {
 }
 
 int rgr_render_until_done(rgr_context* c, int32_t max_steps, int32_t* steps_done) {
+    RGR_NVTX_RANGE("rgr_render_until_done");
     if (!c || max_steps < 0) return RGR_E_INVALID;
     if (!c->begun || c->rp.sample_limit == 0) return RGR_E_STATE;
     int32_t done = 0;
@@ -555,6 +560,7 @@ int rgr_render_until_done(rgr_context* c, int32_t max_steps, int32_t* steps_done
 }
 
 int rgr_render_readback(rgr_context* c, int32_t fmt, void* dst, uint64_t dst_bytes) {
+    RGR_NVTX_RANGE("rgr_render_readback");
     if (!c || !dst) return RGR_E_INVALID;
     if (!c->begun) return RGR_E_STATE;
     RGR_CUDA(cudaSetDevice(c->device));
@@ -623,6 +629,7 @@ int rgr_accum_merge(rgr_context* dst, rgr_context* src) {
 
 int rgr_trace_closest_device(rgr_context* c, const rgr_ray_soa* rays, uint64_t n, int32_t* prim, float* t,
                              float* ng_xyz, void* stream) {
+    RGR_NVTX_RANGE("rgr_trace_closest_device");
     if (!c || !rays || !prim || !t) return RGR_E_INVALID;
     if (!c->scene.valid) return RGR_E_STATE;
     if (n == 0) return RGR_OK;
@@ -733,6 +740,7 @@ void* device_view(const void* p, bool pageable_ok) {
 }  // namespace
 
 int rgr_trace_closest(rgr_context* c, const rgr_ray_soa* rays, uint64_t n, int32_t* prim, float* t) {
+    RGR_NVTX_RANGE("rgr_trace_closest");
     if (!c || !rays || !prim || !t) return RGR_E_INVALID;
     if (!c->scene.valid) return RGR_E_STATE;
     if (n == 0) return RGR_OK;
@@ -934,6 +942,7 @@ int rgr_batch_add(rgr_batch* b, const rgr_scene* s, const rgr_camera* cam, const
 
 int rgr_batch_run(rgr_batch* b, int32_t order_policy, int32_t steps_per_launch, int32_t max_steps,
                   int32_t* steps_done) {
+    RGR_NVTX_RANGE("rgr_batch_run");
     if (!b || b->reqs.empty() || steps_per_launch < 1 || max_steps < 1) return RGR_E_INVALID;
     rgr_context* c = b->ctx;
     RGR_CUDA(cudaSetDevice(c->device));

@@ -10,6 +10,7 @@
 #include <vector>
 
 #include "guide_host.h"
+#include "nvtx.h"
 
 using namespace rgr;
 using namespace rgr::dev;
@@ -294,6 +295,7 @@ int rgr_guide_set_weights(rgr_guide* g, const float* w, const float* b) {
 }
 
 int rgr_guide_infer_device(rgr_guide* g, const float* rows, uint32_t n, float* out, void* stream) {
+    RGR_NVTX_RANGE("rgr_guide_infer_device");
     if (!g || (n && (!rows || !out))) return RGR_E_INVALID;
     if (n == 0) return RGR_OK;
     RGR_CUDA(cudaSetDevice(g->device));
@@ -310,6 +312,7 @@ int rgr_guide_infer_device(rgr_guide* g, const float* rows, uint32_t n, float* o
 
 int rgr_guide_train_device(rgr_guide* g, const float* samples, uint32_t n, float weight_scale, int32_t apply_adam,
                            float* grads, float* loss, void* stream) {
+    RGR_NVTX_RANGE("rgr_guide_train_device");
     if (!g || (n && !samples) || !std::isfinite(weight_scale)) return RGR_E_INVALID;
     RGR_CUDA(cudaSetDevice(g->device));
     cudaStream_t st = (cudaStream_t)stream;

@@ -1,6 +1,7 @@
 // scene.cpp — the scene half of the C ABI (rgr_scene_*), replacing
 // rt::SceneManager (common/scene_manager.hpp:330-672).
 #include "../rgr_internal.h"
+#include "nvtx.h"
 
 #include <cmath>
 #include <cstring>
@@ -218,6 +219,7 @@ int rgr_scene_envmap_tables_gpu(rgr_scene* s, int32_t device) {
 }
 
 int rgr_scene_build_bvh(rgr_scene* s, const rgr_bvh_params* p) {
+    RGR_NVTX_RANGE("rgr_scene_build_bvh");
     if (!s) return RGR_E_INVALID;
     rgr_bvh_params d;
     rgr_bvh_params_default(&d);
