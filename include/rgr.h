@@ -227,6 +227,15 @@ int rgr_render_until_done(rgr_context* c, int32_t max_steps, int32_t* steps_done
 /* update_intermediate + finalize_color (:942-1007), stat_avg_sample (:1148-1151); synchronous */
 int rgr_render_readback(rgr_context* c, int32_t fmt, void* dst, uint64_t dst_bytes);
 int rgr_render_stats(rgr_context* c, rgr_stats* st);
+/* Checkpoint / resume of a render begun with rgr_render_begin (not a guided one): the
+   resident path pool, its queues and counters, the RNG states and the FP64 accumulator, as
+   an opaque host blob.  rgr_render_restore loads it into a context on which rgr_render_begin
+   was called with the same scene, camera, config and path_count; continuing from there
+   renders the same samples as the original context would have (FP64 sums equal up to the
+   order of their atomic additions; counts exactly).  Synchronous. */
+int rgr_render_checkpoint_size(rgr_context* c, uint64_t* bytes);
+int rgr_render_checkpoint(rgr_context* c, void* dst, uint64_t dst_bytes);
+int rgr_render_restore(rgr_context* c, const void* src, uint64_t src_bytes);
 /* merge_from (:963-991): add src's accumulation into dst (replicas on several GPUs) */
 int rgr_accum_merge(rgr_context* dst, rgr_context* src);
 int rgr_synchronize(rgr_context* c);

@@ -194,6 +194,9 @@ _SIGS = {
     "rgr_guide_last_batch": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p]),
     "rgr_guide_check": (C.c_int, [C.c_void_p]),
     "rgr_guide_set_stall": (C.c_int, [C.c_void_p, C.c_int32]),
+    "rgr_render_checkpoint_size": (C.c_int, [C.c_void_p, C.POINTER(C.c_uint64)]),
+    "rgr_render_checkpoint": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64]),
+    "rgr_render_restore": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64]),
 }
 
 _lib = None
@@ -529,6 +532,19 @@ class WavefrontLane:
         s = rgr_stats()
         _check(self._lib.rgr_render_stats(self._h, C.byref(s)), "rgr_render_stats")
         return s
+
+    def checkpoint(self) -> np.ndarray:
+        """The render's device state (path pool, queues, counters, RNG, FP64 sums) as bytes."""
+        n = C.c_uint64(0)
+        _check(self._lib.rgr_render_checkpoint_size(self._h, C.byref(n)), "rgr_render_checkpoint_size")
+        out = np.empty(n.value, np.uint8)
+        _check(self._lib.rgr_render_checkpoint(self._h, _ptr(out), out.nbytes), "rgr_render_checkpoint")
+        return out
+
+    def restore(self, state: np.ndarray) -> None:
+        """Load a checkpoint into this lane, initialised with the same scene, camera and config."""
+        state = np.ascontiguousarray(state, np.uint8)
+        _check(self._lib.rgr_render_restore(self._h, _ptr(state), state.nbytes), "rgr_render_restore")
 
     def stat_avg_sample(self) -> float:
         return self.stats().avg_spp

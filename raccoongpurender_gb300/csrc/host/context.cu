@@ -559,6 +559,91 @@ int rgr_render_until_done(rgr_context* c, int32_t max_steps, int32_t* steps_done
     return rgr_synchronize(c);
 }
 
+namespace {
+// the device state of a begun render, in checkpoint order
+struct StatePart {
+    DevBuf* buf;
+    size_t bytes;
+};
+std::vector<StatePart> render_state(rgr_context* c) {
+    const size_t n = (size_t)c->ntiles * kTile;
+    std::vector<StatePart> v = {{&c->ro, 16 * n},   {&c->rd, 16 * n},  {&c->T, 16 * n},      {&c->L, 16 * n},
+                                {&c->ng, 16 * n},   {&c->rng, 16 * n}, {&c->vols, 32 * n},   {&c->qid, n},
+                                {&c->req, 2 * n},   {&c->counts, 32},  {&c->tile_new, 4 * (size_t)c->ntiles},
+                                {&c->scalars, 64},  {&c->err, 16},     {&c->accum, 32 * (size_t)c->npix},
+                                {&c->done, 16}};
+    for (int q = 0; q < kNumQueues; ++q) v.push_back({&c->queues[q], 4 * n});
+    return v;
+}
+struct CheckpointHeader {
+    char magic[8];  // "RGRCKPT1"
+    uint64_t npaths, ntiles, npix, steps, bytes;
+};
+int checkpointable(rgr_context* c) {
+    if (!c) return RGR_E_INVALID;
+    if (!c->begun || c->guided || c->rp.nreq != 1) {
+        set_error("checkpoint: a render begun with rgr_render_begin, not a guided one, is needed");
+        return RGR_E_STATE;
+    }
+    return RGR_OK;
+}
+uint64_t checkpoint_bytes(rgr_context* c) {
+    uint64_t b = sizeof(CheckpointHeader);
+    for (const StatePart& s : render_state(c)) b += s.bytes;
+    return b;
+}
+}  // namespace
+
+int rgr_render_checkpoint_size(rgr_context* c, uint64_t* bytes) {
+    int r = checkpointable(c);
+    if (r != RGR_OK) return r;
+    if (!bytes) return RGR_E_INVALID;
+    *bytes = checkpoint_bytes(c);
+    return RGR_OK;
+}
+
+int rgr_render_checkpoint(rgr_context* c, void* dst, uint64_t dst_bytes) {
+    RGR_NVTX_RANGE("rgr_render_checkpoint");
+    int r = checkpointable(c);
+    if (r != RGR_OK) return r;
+    const uint64_t total = checkpoint_bytes(c);
+    if (!dst || dst_bytes < total) return RGR_E_INVALID;
+    RGR_CUDA(cudaSetDevice(c->device));
+    RGR_CUDA(cudaStreamSynchronize(c->stream));
+    CheckpointHeader h{{'R', 'G', 'R', 'C', 'K', 'P', 'T', '1'}, c->npaths, c->ntiles, c->npix, c->steps, total};
+    unsigned char* p = static_cast<unsigned char*>(dst);
+    memcpy(p, &h, sizeof(h));
+    p += sizeof(h);
+    for (const StatePart& s : render_state(c)) {
+        RGR_CUDA(cudaMemcpy(p, s.buf->p, s.bytes, cudaMemcpyDeviceToHost));
+        p += s.bytes;
+    }
+    return RGR_OK;
+}
+
+int rgr_render_restore(rgr_context* c, const void* src, uint64_t src_bytes) {
+    RGR_NVTX_RANGE("rgr_render_restore");
+    int r = checkpointable(c);
+    if (r != RGR_OK) return r;
+    CheckpointHeader h;
+    if (!src || src_bytes < sizeof(h)) return RGR_E_INVALID;
+    memcpy(&h, src, sizeof(h));
+    if (memcmp(h.magic, "RGRCKPT1", 8) != 0 || h.npaths != c->npaths || h.ntiles != c->ntiles ||
+        h.npix != c->npix || h.bytes != checkpoint_bytes(c) || src_bytes < h.bytes) {
+        set_error("rgr_render_restore: not a checkpoint of a render of this shape");
+        return RGR_E_INVALID;
+    }
+    RGR_CUDA(cudaSetDevice(c->device));
+    RGR_CUDA(cudaStreamSynchronize(c->stream));
+    const unsigned char* p = static_cast<const unsigned char*>(src) + sizeof(h);
+    for (const StatePart& s : render_state(c)) {
+        RGR_CUDA(cudaMemcpy(s.buf->p, p, s.bytes, cudaMemcpyHostToDevice));
+        p += s.bytes;
+    }
+    c->steps = h.steps;
+    return RGR_OK;
+}
+
 int rgr_render_readback(rgr_context* c, int32_t fmt, void* dst, uint64_t dst_bytes) {
     RGR_NVTX_RANGE("rgr_render_readback");
     if (!c || !dst) return RGR_E_INVALID;
