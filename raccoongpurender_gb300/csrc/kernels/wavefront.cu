@@ -1169,12 +1169,15 @@ void launch_trace_paths(const PathsView& p, const QueueView& q, const RenderPara
 void launch_trace_logic(const PathsView& p, const QueueView& q, const RenderParams& rp, const TraceShape& ts,
                         cudaStream_t st) {
     const unsigned nb = (p.n + 127) / 128;
+    // the guided variant differs only in recording training samples: a render
+    // with a frozen guide runs the plain one (fewer registers)
+    const bool recording = rp.gd.lobes && rp.gd.record;
     if (ts.persistent) {
-        if (rp.gd.lobes)
+        if (recording)
             k_trace_logic<true, true><<<nb, 128, 0, st>>>(p, q, rp);
         else
             k_trace_logic<false, true><<<nb, 128, 0, st>>>(p, q, rp);
-    } else if (rp.gd.lobes) {
+    } else if (recording) {
         k_trace_logic<true, false><<<nb, 128, 0, st>>>(p, q, rp);
     } else {
         k_trace_logic<false, false><<<nb, 128, 0, st>>>(p, q, rp);
