@@ -16,9 +16,12 @@ C ABI with pinned host buffers, host-to-device copy of the rays and
 device-to-host copy of the hits inside the timed region.  The rays (224 MB)
 are larger than the 129 MB L2, so consecutive steps do not reuse them.
 
-``--impl reference`` times the reference traversal on the host cores (the
-oracle's restatement of kernels/extension_ray_cast_stackless.cl, all
-threads, on a bounded sample of the same rays).
+``--impl reference`` times the reference traversal on the host cores: the
+oracle's restatement of kernels/extension_ray_cast_stackless.cl on all host
+threads, all 8,388,608 rays per step, over a tree the oracle builds itself
+(binned SAH flattened as common/stackless_bvh.hpp:283-341 does).  That arm
+loads no product library: the mesh and rays come from the seeded numpy
+generators.
 """
 from __future__ import annotations
 
@@ -37,20 +40,6 @@ if ROOT not in sys.path:
 
 WORKLOAD = "closest-hit: 1.31M-tri displaced icosphere, 4M coherent + 4M incoherent rays"
 METRIC = "closest-hit Mrays/s (1 GB300)"
-
-
-def measured_traffic() -> int | None:
-    """DRAM bytes per step of the closest-hit kernel from the committed ncu
-    summary (profiles/k_trace_rays_closest_hit_1.31M.md), or None."""
-    p = os.path.join(ROOT, "profiles", "k_trace_rays_closest_hit_1.31M.md")
-    try:
-        with open(p) as f:
-            for line in f:
-                if line.startswith("traffic_bytes_per_step = "):
-                    return int(line.split("=")[1])
-    except OSError:
-        pass
-    return None
 
 
 def measured_peaks() -> dict:
@@ -403,22 +392,74 @@ def guided_render_cost(dev_index: int, spp: int = 64, inference_kernel: int | No
             "cost_per_sample": round(tg / tp - 1.0, 3), "training_iterations": g.stats()["iterations"]}
 
 
-def cpu_baseline(mesh, sm, coherent, incoherent, sample: int = 1048576) -> dict:
+def cpu_baseline(mesh, sm, coherent, incoherent, gpu_hits, sample: int = 1048576) -> dict:
     """The oracle traversal (kernels/extension_ray_cast_stackless.cl restated)
     on all host threads over a bounded sample: the first `sample` rays of each
-    set, with the same 1:1 coherent/incoherent mix."""
+    set, with the same 1:1 coherent/incoherent mix, on the tree the GPU run
+    used.  Its hits are compared bit for bit with the GPU's hits of the timed
+    run (`gpu_hits`: per set, prim and t on the host): the parity record."""
     import numpy as np
     from oracle import pyoracle as po
     osc = po.OracleScene.from_scene(sm, mesh.points, mesh.indices)
     threads = os.cpu_count() or 1
     idx = np.arange(sample)
-    rays = np.concatenate([coherent.subset(idx).packed8(), incoherent.subset(idx).packed8()])
-    osc.trace(rays[:1024], threads=threads)  # warm
+    sets = [coherent.subset(idx).packed8(), incoherent.subset(idx).packed8()]
+    rays = np.concatenate(sets)
+    osc.trace(rays[:1024], threads=threads, normals=False)  # warm
     t0 = time.perf_counter()
-    osc.trace(rays, threads=threads)
+    oprim, ot, _ = osc.trace(rays, threads=threads, normals=False)
     dt = time.perf_counter() - t0
+    gprim = np.concatenate([h[0][:sample] for h in gpu_hits])
+    gt = np.concatenate([h[1][:sample] for h in gpu_hits])
+    parity = {"rays": int(rays.shape[0]), "prim_mismatch": int((gprim != oprim).sum()),
+              "t_mismatch": int((gt.view(np.uint32) != ot.view(np.uint32)).sum()),
+              "hits": int((oprim >= 0).sum()),
+              "what": f"oracle vs GPU hits of the timed run on the first {sample} coherent + {sample} "
+                      "incoherent rays, same tree; t compared as bits"}
     return {"value": round(rays.shape[0] / dt / 1e6, 3), "unit": "Mrays/s", "cores": threads, "kind": "port",
-            "sample": f"{sample} coherent + {sample} incoherent rays of the same workload, {dt:.2f} s"}
+            "sample": f"{sample} coherent + {sample} incoherent rays of the same workload, {dt:.2f} s",
+            "parity": parity}
+
+
+def image_error(dev_index: int, which: str, ref_spp: int) -> dict:
+    """The configuration's image against an FP64-accumulated render of the same
+    scene at `ref_spp` samples per pixel with other seeds (the GPU's FP64
+    render, which follows the oracle sample for sample): per-pixel relative
+    luminance error |Y - Y_ref| / (Y_ref + 0.01) and relMSE, with the
+    reference's constants (radiance discard at 1000).
+    cornell: 256x256, 4 spp, depth 5; mixed: 1920x1080, 64 spp, depth 8."""
+    import numpy as np
+    import raccoongpurender_gb300 as rg
+    from raccoongpurender_gb300 import guiding, scenes
+    if which == "cornell":
+        mesh, env = scenes.cornell_box(), None
+        camd = scenes.cornell_camera(256, 256)
+        spp, depth, dof = 4, 5, 0.0
+    else:
+        mesh, env, camd = scenes.mixed_scene(level=8, seed=3)
+        spp, depth, dof = 64, 8, 0.0045
+    sm = rg.SceneManager()
+    sm.addMesh(mesh)
+    if env is not None:
+        sm.setEnvmap(env)
+    sm.buildBVH(max_leaf_size=4)
+    cam = rg.camera_look_at(camd["eye"], camd["target"], camd["up"], camd["vfov"], camd["w"], camd["h"])
+    lane = rg.WavefrontLane(dev_index, 1 << 22)
+    lane.setup(sm)
+    imgs = []
+    for n, seed in ((spp, 1), (ref_spp, 1 << 30)):
+        lane.initialize(cam, rg.render_config(spp=n, max_depth=depth, dof=dof, seed_offset=seed))
+        lane.render_until_done(1 << 30)
+        imgs.append(guiding.mean_image(lane.accumulation()))
+    w = np.array([0.2126, 0.7152, 0.0722])
+    y, yr = imgs[0] @ w, imgs[1] @ w
+    rel = np.abs(y - yr) / (yr + 0.01)
+    return {"spp": spp, "reference_spp": ref_spp, "pixels": int(rel.size),
+            "rel_err_mean": round(float(rel.mean()), 5), "rel_err_median": round(float(np.median(rel)), 5),
+            "rel_err_p99": round(float(np.quantile(rel, 0.99)), 4), "rel_err_max": round(float(rel.max()), 4),
+            "relmse": round(guiding.relmse(imgs[0], imgs[1]), 6),
+            "note": "Monte Carlo noise of the image at its spp (the reference render's own noise is "
+                    f"{spp / ref_spp:.3f} of it in variance)"}
 
 
 def render_gpu_for_oracle(dev_index: int, which: str) -> dict:
@@ -472,26 +513,70 @@ def cpu_render_baseline(gpu: dict, name: str) -> dict:
                                     "pixels": npix}}
 
 
+def envmap_filter_record() -> dict:
+    """Bound on the software bilinear envmap filter against texture-unit
+    filtering with 8-bit weights (the OpenCL image the reference samples on a
+    camera ray's first segment), on the full-render envmap: over 1M uniform
+    directions and over the 1920x1080 camera's pixel-centre directions."""
+    import numpy as np
+    import raccoongpurender_gb300 as rg
+    from oracle import pyoracle as po
+    from raccoongpurender_gb300 import scenes
+    mesh, env, camd = scenes.mixed_scene(level=3, seed=3)
+    sm = rg.SceneManager()
+    sm.addMesh(mesh)
+    sm.setEnvmap(env)
+    sm.buildBVH(max_leaf_size=4)
+    osc = po.OracleScene.from_scene(sm, mesh.points, mesh.indices)
+    rng = np.random.default_rng(1)
+    v = rng.normal(size=(1 << 20, 3))
+    v /= np.linalg.norm(v, axis=1, keepdims=True)
+    cam = rg.camera_look_at(camd["eye"], camd["target"], camd["up"], camd["vfov"], camd["w"], camd["h"])
+    rays = scenes.pinhole_rays(camd["eye"], camd["target"], camd["up"], np.tan(np.radians(camd["vfov"] / 2)),
+                               int(cam.image_w), int(cam.image_h))
+    return {"uniform_sphere": po.envmap_filter_bound(osc, v), "camera_1080p": po.envmap_filter_bound(osc, rays.d)}
+
+
 def run_reference(args) -> None:
+    """The reference arm: the reference traversal restated by the oracle, on
+    all host threads, over all 8,388,608 rays of the workload per step.  The
+    mesh and rays come from the seeded numpy generators and the tree from the
+    oracle's own builder, so no product library is loaded.  Under torchrun
+    only rank 0 runs."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    mesh, sm, coherent, incoherent, _ = build_workload()
-    # the reference has no GPU implementation available here: its traversal
-    # restated on the host cores is the comparison arm
-    vals = []
+    import numpy as np
+    from oracle import pyoracle as po
+    from raccoongpurender_gb300 import scenes  # numpy generators; loads no library
+    mesh = scenes.displaced_icosphere(8, seed=7)
+    coherent, incoherent = scenes.closest_hit_rays(mesh, res=2048, n_random=2048 * 2048, seed=11)
+    threads = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    osc = po.OracleScene.from_mesh(mesh.points, mesh.indices, max_leaf=4, threads=threads)
+    build_s = time.perf_counter() - t0
+    rays = np.concatenate([coherent.packed8(), incoherent.packed8()])
+    del coherent, incoherent
+    n = rays.shape[0]
     for _ in range(args.warmup):
-        cpu_baseline(mesh, sm, coherent, incoherent, sample=8192)
+        osc.trace(rays, threads=threads, normals=False)
+    times = []
     for _ in range(args.steps):
-        vals.append(cpu_baseline(mesh, sm, coherent, incoherent, sample=32768))
-    v = sorted(x["value"] for x in vals)[len(vals) // 2]
-    base = vals[0]
+        t0 = time.perf_counter()
+        osc.trace(rays, threads=threads, normals=False)
+        times.append(time.perf_counter() - t0)
+    ms_per_step = sum(times) / len(times) * 1e3
+    v = round(n / (ms_per_step * 1e-3) / 1e6, 3)
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "Mrays/s", "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "triangles": int(mesh.ntris), "rays_per_step": 2 * 32768},
-            "cpu_baseline": {"value": v, "unit": "Mrays/s", "cores": base["cores"], "kind": "port",
-                             "sample": base["sample"]},
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_per_step, 2),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "triangles": int(mesh.ntris), "rays_per_step": int(n),
+                       "bvh": {"max_leaf": 4, "builder": "oracle binned SAH (32 bins, 1:1 costs), reference "
+                                                         "stackless flattening", "nodes": int(osc.nodes.shape[0]),
+                               "build_s": round(build_s, 2)},
+                       "parallelism": "host threads"},
+            "cpu_baseline": {"value": v, "unit": "Mrays/s", "cores": threads, "kind": "port",
+                             "sample": f"all {n} rays per step (4M coherent + 4M incoherent), {args.steps} steps"},
             "e2e": {"value": v, "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -506,6 +591,9 @@ def main() -> None:
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--no-render", action="store_true", help="skip the full-render measurements")
     ap.add_argument("--no-guiding", action="store_true", help="skip the learned-guiding measurements")
+    ap.add_argument("--traffic-bytes", type=int, default=None,
+                    help="DRAM bytes per step of the closest-hit launches from an ncu capture, to attach to the "
+                         "roofline record")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -632,19 +720,31 @@ def main() -> None:
     lane.set_trace_host_mode(rg.TRACE_HOST_AUTO)
     e2e_s = e2e_time()
     e2e_value = rays_per_step / e2e_s / 1e6
+    # the hits of the timed run, for the parity record of the CPU leg
+    gpu_hits = [(prim.cpu().numpy(), t.cpu().numpy()) for _, prim, t, _ in sets]
     # the e2e hits must equal the device-resident hits
-    assert (out_prim[0].numpy() == sets[0][1].cpu().numpy()).all()
+    assert (out_prim[0].numpy() == gpu_hits[0][0]).all() and (out_prim[1].numpy() == gpu_hits[1][0]).all()
 
     peaks = measured_peaks()
     coh_bytes = bytes_per_ray[0] * n_each
     inc_bytes = bytes_per_ray[1] * n_each
     achieved = (coh_bytes + inc_bytes) / ((coh_ms + inc_ms) * 1e-3) / 1e9
-    traffic = measured_traffic()
-    roof = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peaks["hbm_gbs"], "unit": "GB/s",
-            "frac": round(achieved / peaks["hbm_gbs"], 4), "traffic": traffic,
-            "traffic_note": "DRAM bytes per step (both launches) from ncu, profiles/k_trace_rays_closest_hit_1.31M.md;"
-                            f" algorithmic bytes per step {int(coh_bytes + inc_bytes)}: the tree is L2-resident",
-            "peak_source": peaks["source"] + " hbm_gbs",
+    # the roof: the tree (inner nodes + primitive records) is L2-resident, so the
+    # denominator is the L2 read bandwidth measured now over a buffer of its size;
+    # an HBM-sized read of the same probe and the measured HBM copy rate beside it
+    info0 = sm.info()
+    ws_bytes = int(info0.num_inner_nodes) * 64 + int(mesh.ntris) * 48
+    l2_gbs = rg.probe_read_bandwidth(local, ws_bytes, reps=50)
+    hbm_read_gbs = rg.probe_read_bandwidth(local, 4 << 30, reps=10)
+    traffic = args.traffic_bytes
+    roof = {"bound": "l2", "achieved": round(achieved, 1), "peak": round(l2_gbs, 1), "unit": "GB/s",
+            "frac": round(achieved / l2_gbs, 4), "traffic": traffic,
+            "peak_source": f"measured in this run: L2 read bandwidth over {ws_bytes / 1e6:.1f} MB (the tree's "
+                           "inner nodes and primitive records), 16-byte loads bypassing L1",
+            "hbm": {"peak": peaks["hbm_gbs"], "frac": round(achieved / peaks["hbm_gbs"], 4),
+                    "source": peaks["source"] + " hbm_gbs (copy)", "read_probe_4gib_gbs": round(hbm_read_gbs, 1)},
+            "traffic_note": (f"algorithmic bytes per step {int(coh_bytes + inc_bytes)}; DRAM traffic comes from an "
+                             "ncu capture, not from this run (null unless --traffic-bytes gives it)"),
             "fp32": {"flops_per_ray": [round(f, 1) for f in flops_per_ray],
                      "achieved_tflops": round((flops_per_ray[0] + flops_per_ray[1]) * n_each /
                                               ((coh_ms + inc_ms) * 1e-3) / 1e12, 2),
@@ -663,7 +763,9 @@ def main() -> None:
         render = {"cornell_256_4spp": render_bench(local, "cornell", pools=(1 << 18, 1 << 22)),
                   "mixed_1080p_64spp": render_bench(local, "mixed", pools=(1 << 22, 1 << 23, 1 << 24)),
                   "batch_32_requests": batch_bench(local),
-                  "scene_load_alembic": scene_load_bench()}
+                  "scene_load_alembic": scene_load_bench(),
+                  "image_error_vs_fp64_reference": {"cornell_256_4spp": image_error(local, "cornell", 4096),
+                                                    "mixed_1080p_64spp": image_error(local, "mixed", 1024)}}
     bvh = bvh_bench(local, mesh, [([a.data_ptr() for a in soa], n, prim.data_ptr(), t.data_ptr())
                                   for soa, prim, t, n in sets], sptr, build_s) if not args.no_render else None
     guide = None
@@ -672,9 +774,10 @@ def main() -> None:
                  "equal_time": guiding_bench(local)}
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        cpu = cpu_baseline(mesh, sm, coherent, incoherent)
+        cpu = cpu_baseline(mesh, sm, coherent, incoherent, gpu_hits)
         if not args.no_render:
             cpu["render"] = {w: cpu_render_baseline(render_gpu_for_oracle(local, w), w) for w in ("cornell", "mixed")}
+        cpu["envmap_filter_bound"] = envmap_filter_record()
     info = sm.info()
     if rank == 0:
         line = {"metric": METRIC, "value": round(value, 1), "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
@@ -693,7 +796,8 @@ def main() -> None:
                         "path": "rgr_trace_closest on page-locked host arrays: the traversal kernel reads the rays "
                                 "and writes the hits across NVLink-C2C (zero copy)",
                         "staged_copies_value": round(e2e_staged, 1)},
-                "gpu_launches": 2 * args.steps, "roofline": roof, "cpu_baseline": cpu, "clocks": clocks,
+                "gpu_launches": 2 * args.steps, "roofline": roof, "cpu_baseline": cpu,
+                "parity": cpu["parity"] if cpu else None, "clocks": clocks,
                 "render": render, "bvh_build": bvh, "guiding": guide}
         print(json.dumps(line), flush=True)
     if world > 1:

@@ -308,10 +308,11 @@ int rgr_trace_closest_counts_device(rgr_context* c, const rgr_ray_soa* rays, uin
    RGR_E_INVALID.  The caller passes a context with an uploaded scene (input)
    and accum_out, a device buffer of 4 doubles (r, g, b, count) per pixel
    (output, cleared by the call).  Runs on `stream` (NULL: the default stream)
-   and returns when the work is done.  All calls on a device share the array:
-   calls that overlap on the GPU race and give wrong results.  The first call
-   on a device looks up the array's address, so make that first call before
-   any stream capture starts on that device. */
+   and is synchronous: it waits for that work to finish before it returns, and
+   leaves the caller's current device unchanged.  All calls on a device share
+   the array: calls that overlap on the GPU race and give wrong results.  The
+   first call on a device looks up the array's address, so make that first call
+   before any stream capture starts on that device. */
 int rgr_render_noalloc(rgr_context* c, const rgr_camera* cam, const rgr_render_config* cfg, uint32_t path_count,
                        int32_t steps, double* accum_out, void* stream);
 
@@ -427,6 +428,11 @@ int rgr_guide_loss_history(rgr_guide* g, float* out, uint32_t max, uint32_t* cou
 int rgr_guide_last_batch(rgr_guide* g, float* out, uint32_t max, uint32_t* count);
 
 /* ---- diagnostics --------------------------------------------------------- */
+/* Read bandwidth of `device` over a buffer of `bytes` (no reference counterpart: the
+   denominator of the closest-hit roofline).  Streams the buffer with 16-byte loads that
+   bypass L1 after a warm-up pass, so a buffer smaller than L2 measures L2 read bandwidth
+   and a larger one HBM; *gbs = bytes * reps / time.  Allocates its own buffer. */
+int rgr_probe_read_bandwidth(int32_t device, uint64_t bytes, int32_t reps, double* gbs);
 const char* rgr_status_string(int status);
 const char* rgr_last_error(void);
 /* per-slot path state after the last step, 34 uint32 words per slot in this order:

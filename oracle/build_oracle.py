@@ -33,7 +33,9 @@ REF_OUT = HERE / "_ref"
 LIB = BUILD / "liboracle.so"
 REF_LIB = REF_OUT / "libref.so"
 FMATH = ROOT / "raccoongpurender_gb300" / "csrc" / "rgr_fmath.h"
-CXX = ["g++", "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off"]
+# -O3 without -march/-mcpu=native: the same build must give the same results on the
+# x86 development machines and the Arm GPU machines
+CXX = ["g++", "-O3", "-std=c++17", "-fPIC", "-ffp-contract=off"]
 
 
 def reference_dir() -> Path | None:

@@ -56,6 +56,7 @@ _ORC_SIGS = {
     "orc_random_uniform_integer": (None, [VP, VP, I32]),
     "orc_trace": (None, [VP, VP, U64, VP, VP, VP, VP, VP, I32]),
     "orc_envmap_build": (I32, [VP, I32, I32, VP, VP, VP, VP]),
+    "orc_build_bvh": (C.c_int64, [VP, VP, U32, VP, U32, I32, I32, I32, VP, U64, VP, U64]),
     "orc_render": (U64, [VP, VP, VP, U32, I32, VP, VP, I32]),
     "orc_render_batch": (U64, [VP, VP, VP, VP, VP, I32, U32, I32, VP, VP, I32]),
     "orc_intermediate": (None, [VP, U64, VP]),
@@ -70,6 +71,7 @@ _ORC_SIGS = {
     "orc_pdf_ward": (F32C, [VP, VP, VP, F32C]),
     "orc_envmap_value": (None, [VP, VP, I32, VP]),
     "orc_envmap_index": (I32, [VP, I32, I32]),
+    "orc_envmap_filter_compare": (None, [VP, VP, U64, I32, VP, VP]),
     "orc_fm": (F32C, [I32, F32C, F32C]),
 }
 _REF_SIGS = {
@@ -183,11 +185,47 @@ class OracleScene:
                                                                 P(env["frag"]))
         return o
 
-    def trace(self, rays8: np.ndarray, counters: bool = False, threads: int = 8):
+    @classmethod
+    def from_mesh(cls, points, indices, max_leaf: int = 4, bins: int = 32, threads: int = 8):
+        """Traversal-only view of a triangle mesh with a tree the oracle builds
+        itself (orc_build_bvh: binned SAH flattened as create_stackless_bvh
+        does), so that no product code is involved.  Materials are unset:
+        for closest-hit queries only."""
+        o = cls()
+        pts = np.zeros((points.shape[0], 4), np.float32)
+        pts[:, :3] = points
+        o.points = pts
+        o.indices = np.ascontiguousarray(indices, np.uint32).reshape(-1)
+        ntri = o.indices.shape[0] // 3
+        o.spheres = np.zeros((1, 4), np.float32)
+        cap = 2 * ntri
+        nodes = np.zeros((cap, 24), np.uint32)
+        prim_ids = np.zeros(ntri, np.uint32)
+        nn = lib().orc_build_bvh(P(o.points), P(o.indices), ntri, P(o.spheres), 0, max_leaf, bins, threads,
+                                 P(nodes), cap, P(prim_ids), ntri)
+        if nn <= 0:
+            raise ValueError("orc_build_bvh rejected its arguments")
+        o.nodes = np.ascontiguousarray(nodes[:nn])
+        del nodes
+        o.prim_ids = prim_ids
+        o.mat = np.zeros((max(ntri, 1), 2), np.int32)
+        o.mat[:, 0] = 1
+        o.lam = np.zeros((1, 12), np.float32)
+        o.ward = np.zeros((1, 16), np.float32)
+        o.vol = np.zeros((1, 8), np.float32)
+        s = o.s
+        s.points, s.indices, s.ntris = P(o.points), P(o.indices), ntri
+        s.spheres, s.nspheres, s.sphere_begin = P(o.spheres), 0, ntri
+        s.nodes, s.nnodes = P(o.nodes), o.nodes.shape[0]
+        s.prim_ids, s.nprim_ids = P(o.prim_ids), o.prim_ids.shape[0]
+        s.materials, s.lambertians, s.wards, s.volumes = P(o.mat), P(o.lam), P(o.ward), P(o.vol)
+        return o
+
+    def trace(self, rays8: np.ndarray, counters: bool = False, threads: int = 8, normals: bool = True):
         n = rays8.shape[0]
         prim = np.empty(n, np.int32)
         t = np.empty(n, np.float32)
-        ng = np.empty((n, 3), np.float32)
+        ng = np.empty((n, 3), np.float32) if normals else None
         nv = np.empty(n, np.uint32) if counters else None
         nt = np.empty(n, np.uint32) if counters else None
         lib().orc_trace(C.byref(self.s), P(rays8), n, P(prim), P(t), P(ng), P(nv), P(nt), threads)
@@ -244,3 +282,20 @@ def config_from_rgr(cfg, npix: int) -> orc_config:
     o.fix_backside_env_pdf = 1 if (cfg.flags & 1) else 0
     o.two_sided_lambertian = 1 if (cfg.flags & 2) else 0
     return o
+
+
+def envmap_filter_bound(osc: OracleScene, dirs: np.ndarray, frac_bits: int = 8) -> dict:
+    """How far the software bilinear envmap lookup (FP32 weights; the oracle's and
+    the CUDA path's) is from texture-unit filtering with weights of `frac_bits`
+    fractional bits, over the directions `dirs` (n, 3): relative difference of
+    the luminance, |Y_q - Y| / Y, per direction."""
+    n = dirs.shape[0]
+    d = np.ascontiguousarray(dirs, np.float32)
+    exact = np.empty((n, 3), np.float32)
+    quant = np.empty((n, 3), np.float32)
+    lib().orc_envmap_filter_compare(C.byref(osc.s), P(d), n, frac_bits, P(exact), P(quant))
+    w = np.array([0.2126, 0.7152, 0.0722])
+    ye, yq = exact.astype(np.float64) @ w, quant.astype(np.float64) @ w
+    rel = np.abs(yq - ye) / np.maximum(ye, 1e-30)
+    return {"directions": int(n), "frac_bits": frac_bits, "rel_max": float(rel.max()), "rel_mean": float(rel.mean()),
+            "rel_p999": float(np.quantile(rel, 0.999)), "share_above_1e-3": float((rel > 1e-3).mean())}

@@ -27,6 +27,8 @@
 #include <vector>
 #include <thread>
 #include <algorithm>
+#include <atomic>
+#include <memory>
 
 using namespace rgr::fm;
 
@@ -318,6 +320,33 @@ inline f3 read_image_repeat(const orc_scene* s, float su, float sv, bool linear)
     j1 = std::min(std::max(j1, 0), h - 1);
     float a = uu - floor_(uu);
     float b = vv - floor_(vv);
+    float w00 = (1.0f - a) * (1.0f - b), w10 = a * (1.0f - b);
+    float w01 = (1.0f - a) * b, w11 = a * b;
+    f3 t00 = texel(s, i0, j0), t10 = texel(s, i1, j0), t01 = texel(s, i0, j1), t11 = texel(s, i1, j1);
+    return ((t00 * w00 + t10 * w10) + t01 * w01) + t11 * w11;
+}
+// The bilinear lookup above with the two filter weights rounded to multiples of
+// 2^-frac_bits, as GPU texture units hold them (8 fractional bits on NVIDIA
+// hardware): the filtering an OpenCL image sampler gives, for bounding the
+// difference to the FP32-weight filter that both this file and the CUDA path use.
+inline f3 read_image_repeat_quantized(const orc_scene* s, float su, float sv, int frac_bits) {
+    int w = s->env_w, h = s->env_h;
+    float u = (su - floor_(su)) * (float)w;
+    float v = (sv - floor_(sv)) * (float)h;
+    float uu = u - 0.5f, vv = v - 0.5f;
+    int i0 = to_int(floor_(uu)), j0 = to_int(floor_(vv));
+    int i1 = i0 + 1, j1 = j0 + 1;
+    if (i0 < 0) i0 = w + i0;
+    if (i1 > w - 1) i1 = i1 - w;
+    if (j0 < 0) j0 = h + j0;
+    if (j1 > h - 1) j1 = j1 - h;
+    i0 = std::min(std::max(i0, 0), w - 1);
+    i1 = std::min(std::max(i1, 0), w - 1);
+    j0 = std::min(std::max(j0, 0), h - 1);
+    j1 = std::min(std::max(j1, 0), h - 1);
+    const float scale = (float)(1 << frac_bits);
+    float a = std::nearbyint((uu - floor_(uu)) * scale) / scale;
+    float b = std::nearbyint((vv - floor_(vv)) * scale) / scale;
     float w00 = (1.0f - a) * (1.0f - b), w10 = a * (1.0f - b);
     float w01 = (1.0f - a) * b, w11 = a * b;
     f3 t00 = texel(s, i0, j0), t10 = texel(s, i1, j0), t01 = texel(s, i0, j1), t11 = texel(s, i1, j1);
@@ -929,7 +958,7 @@ void orc_random_uniform_integer(uint32_t* state4, uint64_t* out, int32_t n) {
 
 void orc_trace(const orc_scene* s, const float* rays, uint64_t n, int32_t* prim, float* t,
                float* ng, uint32_t* node_visits, uint32_t* prim_tests, int32_t nthreads) {
-    auto work = [&](uint64_t beg, uint64_t end) {
+    auto trace_range = [&](uint64_t beg, uint64_t end) {
         for (uint64_t i = beg; i < end; ++i) {
             const float* r = rays + 8 * i;
             f3 ro = ld3(r), rd = ld3(r + 4);
@@ -948,15 +977,21 @@ void orc_trace(const orc_scene* s, const float* rays, uint64_t n, int32_t* prim,
         }
     };
     if (nthreads <= 1 || n < 4096) {
-        work(0, n);
+        trace_range(0, n);
         return;
     }
+    // threads take chunks of 4096 rays from a shared counter: coherent and
+    // incoherent rays cost very different amounts, so static halves would idle
+    std::atomic<uint64_t> next{0};
+    auto worker = [&]() {
+        for (;;) {
+            uint64_t b = next.fetch_add(4096);
+            if (b >= n) return;
+            trace_range(b, std::min<uint64_t>(n, b + 4096));
+        }
+    };
     std::vector<std::thread> th;
-    uint64_t chunk = (n + nthreads - 1) / nthreads;
-    for (int k = 0; k < nthreads; ++k) {
-        uint64_t b = k * chunk, e = std::min<uint64_t>(n, b + chunk);
-        if (b < e) th.emplace_back(work, b, e);
-    }
+    for (int k = 0; k < nthreads; ++k) th.emplace_back(worker);
     for (auto& x : th) x.join();
 }
 
@@ -1215,6 +1250,16 @@ void orc_envmap_value(const orc_scene* s, const float* rd3, int32_t filter, floa
     st3(out3, get_envmap_value(s, ld3(rd3), filter != 0));
 }
 int32_t orc_envmap_index(const float* wi3, int32_t w, int32_t h) { return envmap_index(ld3(wi3), w, h); }
+void orc_envmap_filter_compare(const orc_scene* s, const float* rd3, uint64_t n, int32_t frac_bits, float* exact3,
+                               float* quant3) {
+    const float pi = kPiF;
+    for (uint64_t i = 0; i < n; ++i) {
+        float theta, phi;
+        cartesian_to_polar(ld3(rd3 + 3 * i), &theta, &phi);
+        st3(exact3 + 3 * i, get_envmap_value(s, ld3(rd3 + 3 * i), true));
+        st3(quant3 + 3 * i, read_image_repeat_quantized(s, 1.0f - phi / (2.0f * pi), theta / pi, frac_bits));
+    }
+}
 
 float orc_fm(int32_t fn, float x, float y) {
     switch (fn) {
@@ -1230,3 +1275,229 @@ float orc_fm(int32_t fn, float x, float y) {
 }
 
 }  // extern "C"
+
+// ------------------------------------------------------------ tree build
+// The reference builds a binary tree with Embree (rtcBuildBVH, RTC_BUILD_QUALITY_HIGH,
+// maxBranchingFactor 2, leaves of 1..5 primitives, Embree's default SAH costs;
+// common/stackless_bvh.hpp:108-130) and flattens it with create_stackless_bvh
+// (stackless_bvh.hpp:283-341).  Embree is not vendored, so a plain binned SAH stands in
+// for it here (node visit and primitive test priced 1 : 1, as Embree's defaults), and
+// the flattening follows the reference: node indices in preorder (left subtree first,
+// allocate_stacklessBVH), each child's sibling link pointing at the other child, the
+// root's parent and sibling links 0, and each leaf's primitive ids appended to one list
+// in that same preorder (build_stacklessBVH).  Leaves are the nodes with
+// primitive_indices_end > 0, as the traversal tells them apart.
+// This builder exists so that the reference arm of the benchmark can run without the
+// product library; closest hits do not depend on the tree except for exact ties.
+namespace {
+
+struct BuildPrim {
+    float lo[3], hi[3], c[3];
+    uint32_t id;
+};
+
+struct BuildNode {
+    float lo[3], hi[3];
+    std::unique_ptr<BuildNode> L, R;
+    uint32_t beg = 0, end = 0;  // leaf: range into the primitive array
+    bool leaf = false;
+};
+
+inline float half_area(const float* lo, const float* hi) {
+    float dx = hi[0] - lo[0], dy = hi[1] - lo[1], dz = hi[2] - lo[2];
+    return dx * dy + dy * dz + dz * dx;
+}
+
+struct Builder {
+    std::vector<BuildPrim>& prims;
+    int max_leaf;
+    int bins;
+    int spawn_depth;
+
+    std::unique_ptr<BuildNode> build(uint32_t b, uint32_t e, int depth) {
+        auto node = std::make_unique<BuildNode>();
+        float clo[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, chi[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+        for (int a = 0; a < 3; ++a) {
+            node->lo[a] = FLT_MAX;
+            node->hi[a] = -FLT_MAX;
+        }
+        for (uint32_t i = b; i < e; ++i) {
+            const BuildPrim& p = prims[i];
+            for (int a = 0; a < 3; ++a) {
+                node->lo[a] = std::min(node->lo[a], p.lo[a]);
+                node->hi[a] = std::max(node->hi[a], p.hi[a]);
+                clo[a] = std::min(clo[a], p.c[a]);
+                chi[a] = std::max(chi[a], p.c[a]);
+            }
+        }
+        uint32_t n = e - b;
+        if (n == 1) {
+            node->leaf = true;
+            node->beg = b;
+            node->end = e;
+            return node;
+        }
+        // binned SAH over the centroid bounds: cost = 1 + (A_L N_L + A_R N_R) / A
+        int best_axis = -1, best_bin = -1;
+        float best_cost = FLT_MAX;
+        const float parent_area = half_area(node->lo, node->hi);
+        std::vector<float> blo(3 * bins), bhi(3 * bins), rarea(bins);
+        std::vector<uint32_t> bcount(bins), rcount(bins);
+        for (int a = 0; a < 3; ++a) {
+            float extent = chi[a] - clo[a];
+            if (!(extent > 0.0f)) continue;
+            float scale = (float)bins / extent;
+            std::fill(bcount.begin(), bcount.end(), 0u);
+            for (int k = 0; k < bins; ++k)
+                for (int c = 0; c < 3; ++c) {
+                    blo[3 * k + c] = FLT_MAX;
+                    bhi[3 * k + c] = -FLT_MAX;
+                }
+            for (uint32_t i = b; i < e; ++i) {
+                const BuildPrim& p = prims[i];
+                int k = std::min(bins - 1, (int)((p.c[a] - clo[a]) * scale));
+                bcount[k]++;
+                for (int c = 0; c < 3; ++c) {
+                    blo[3 * k + c] = std::min(blo[3 * k + c], p.lo[c]);
+                    bhi[3 * k + c] = std::max(bhi[3 * k + c], p.hi[c]);
+                }
+            }
+            // right sweep: area and count of bins k..bins-1
+            float rlo[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, rhi[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+            uint32_t rc = 0;
+            for (int k = bins - 1; k >= 1; --k) {
+                rc += bcount[k];
+                for (int c = 0; c < 3; ++c) {
+                    rlo[c] = std::min(rlo[c], blo[3 * k + c]);
+                    rhi[c] = std::max(rhi[c], bhi[3 * k + c]);
+                }
+                rcount[k] = rc;
+                rarea[k] = rc ? half_area(rlo, rhi) : 0.0f;
+            }
+            float llo[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, lhi[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+            uint32_t lc = 0;
+            for (int k = 1; k < bins; ++k) {  // split between bin k-1 and bin k
+                lc += bcount[k - 1];
+                for (int c = 0; c < 3; ++c) {
+                    llo[c] = std::min(llo[c], blo[3 * (k - 1) + c]);
+                    lhi[c] = std::max(lhi[c], bhi[3 * (k - 1) + c]);
+                }
+                if (lc == 0 || rcount[k] == 0) continue;
+                float cost = 1.0f + (half_area(llo, lhi) * (float)lc + rarea[k] * (float)rcount[k]) / parent_area;
+                if (cost < best_cost) {
+                    best_cost = cost;
+                    best_axis = a;
+                    best_bin = k;
+                }
+            }
+        }
+        if (n <= (uint32_t)max_leaf && (best_axis < 0 || (float)n <= best_cost)) {
+            node->leaf = true;
+            node->beg = b;
+            node->end = e;
+            return node;
+        }
+        uint32_t mid;
+        if (best_axis >= 0 && depth < 56) {
+            float extent = chi[best_axis] - clo[best_axis];
+            float scale = (float)bins / extent;
+            auto it = std::partition(prims.begin() + b, prims.begin() + e, [&](const BuildPrim& p) {
+                return std::min(bins - 1, (int)((p.c[best_axis] - clo[best_axis]) * scale)) < best_bin;
+            });
+            mid = (uint32_t)(it - prims.begin());
+        } else {
+            // all centroids equal (or the tree is too deep for the traversal's 64-bit bit
+            // stack): split the range at its middle, ordered along the widest axis
+            int a = 0;
+            for (int c = 1; c < 3; ++c)
+                if (chi[c] - clo[c] > chi[a] - clo[a]) a = c;
+            mid = b + n / 2;
+            std::nth_element(prims.begin() + b, prims.begin() + mid, prims.begin() + e,
+                             [&](const BuildPrim& x, const BuildPrim& y) {
+                                 return x.c[a] < y.c[a] || (x.c[a] == y.c[a] && x.id < y.id);
+                             });
+        }
+        if (mid == b || mid == e) mid = b + n / 2;
+        if (depth < spawn_depth && n > 65536) {
+            std::unique_ptr<BuildNode> right;
+            std::thread th([&]() { right = build(mid, e, depth + 1); });
+            node->L = build(b, mid, depth + 1);
+            th.join();
+            node->R = std::move(right);
+        } else {
+            node->L = build(b, mid, depth + 1);
+            node->R = build(mid, e, depth + 1);
+        }
+        return node;
+    }
+};
+
+uint64_t count_nodes(const BuildNode* n) { return n->leaf ? 1 : 1 + count_nodes(n->L.get()) + count_nodes(n->R.get()); }
+
+// allocate_stacklessBVH + build_stacklessBVH (stackless_bvh.hpp:283-326)
+uint32_t flatten(const BuildNode* n, const std::vector<BuildPrim>& prims, orc_node* nodes, uint32_t* prim_ids,
+                 uint32_t* next_node, uint32_t* next_prim, uint32_t parent, bool has_parent) {
+    uint32_t me = (*next_node)++;
+    orc_node& o = nodes[me];
+    memset(&o, 0, sizeof(o));
+    if (has_parent) o.link_parent = parent;
+    if (!n->leaf) {
+        uint32_t L = flatten(n->L.get(), prims, nodes, prim_ids, next_node, next_prim, me, true);
+        uint32_t R = flatten(n->R.get(), prims, nodes, prim_ids, next_node, next_prim, me, true);
+        orc_node& p = nodes[me];
+        p.link_L = L;
+        p.link_R = R;
+        for (int a = 0; a < 3; ++a) {
+            p.L_lower[a] = n->L->lo[a];
+            p.L_upper[a] = n->L->hi[a];
+            p.R_lower[a] = n->R->lo[a];
+            p.R_upper[a] = n->R->hi[a];
+        }
+        nodes[L].link_sibling = R;
+        nodes[R].link_sibling = L;
+    } else {
+        o.primitive_indices_beg = *next_prim;
+        for (uint32_t i = n->beg; i < n->end; ++i) prim_ids[(*next_prim)++] = prims[i].id;
+        o.primitive_indices_end = *next_prim;
+    }
+    return me;
+}
+
+}  // namespace
+
+extern "C" int64_t orc_build_bvh(const float* points4, const uint32_t* indices, uint32_t ntris, const float* spheres4,
+                                 uint32_t nspheres, int32_t max_leaf, int32_t bins, int32_t nthreads, orc_node* nodes,
+                                 uint64_t node_cap, uint32_t* prim_ids, uint64_t prim_cap) {
+    uint64_t nprim = (uint64_t)ntris + nspheres;
+    if (nprim == 0 || max_leaf < 1 || max_leaf > 5 || bins < 2 || prim_cap < nprim) return -1;
+    std::vector<BuildPrim> prims(nprim);
+    for (uint64_t i = 0; i < ntris; ++i) {
+        BuildPrim& p = prims[i];
+        p.id = (uint32_t)i;
+        for (int a = 0; a < 3; ++a) {
+            float v0 = points4[4 * (size_t)indices[3 * i] + a], v1 = points4[4 * (size_t)indices[3 * i + 1] + a],
+                  v2 = points4[4 * (size_t)indices[3 * i + 2] + a];
+            p.lo[a] = std::min(v0, std::min(v1, v2));
+            p.hi[a] = std::max(v0, std::max(v1, v2));
+        }
+    }
+    for (uint64_t k = 0; k < nspheres; ++k) {
+        BuildPrim& p = prims[ntris + k];
+        p.id = (uint32_t)(ntris + k);
+        for (int a = 0; a < 3; ++a) {
+            p.lo[a] = spheres4[4 * k + a] - spheres4[4 * k + 3];
+            p.hi[a] = spheres4[4 * k + a] + spheres4[4 * k + 3];
+        }
+    }
+    for (auto& p : prims)
+        for (int a = 0; a < 3; ++a) p.c[a] = (p.lo[a] + p.hi[a]) * 0.5f;
+    int spawn = 0;
+    while ((1 << spawn) < std::max(1, nthreads)) ++spawn;
+    Builder bld{prims, max_leaf, bins, spawn};
+    std::unique_ptr<BuildNode> root = bld.build(0, (uint32_t)nprim, 0);
+    uint64_t nn = count_nodes(root.get());
+    if (nodes == nullptr || node_cap < nn) return (int64_t)nn;  // size query
+    uint32_t next_node = 0, next_prim = 0;
+    flatten(root.get(), prims, nodes, prim_ids, &next_node, &next_prim, 0, false);
+    return (int64_t)nn;
+}

@@ -113,6 +113,15 @@ void orc_trace(const orc_scene* s, const float* rays, uint64_t n, int32_t* prim,
                float* t, float* ng, uint32_t* node_visits, uint32_t* prim_tests,
                int32_t nthreads);
 
+/* tree build: binned SAH (1:1 costs, standing in for the reference's Embree build,
+   stackless_bvh.hpp:108-130) flattened as create_stackless_bvh does
+   (stackless_bvh.hpp:283-341).  points4 is float4 per vertex, spheres4 (center, radius).
+   Returns the node count, or -1 on bad arguments; with nodes == NULL or node_cap too
+   small it only returns the count (prim_ids still needs ntris + nspheres entries). */
+int64_t orc_build_bvh(const float* points4, const uint32_t* indices, uint32_t ntris, const float* spheres4,
+                      uint32_t nspheres, int32_t max_leaf, int32_t bins, int32_t nthreads, orc_node* nodes,
+                      uint64_t node_cap, uint32_t* prim_ids, uint64_t prim_cap);
+
 /* envmap tables (envmap.hpp:160-242, alias_method.hpp:47-114) */
 int32_t orc_envmap_build(const float* rgba, int32_t w, int32_t h, float* pdf,
                          float* height, int32_t* alias, float* frag);
@@ -146,6 +155,11 @@ void orc_sample_ward(const float* wo3, const float* z3, float alpha, float u0, f
 float orc_pdf_ward(const float* wo3, const float* wi3, const float* z3, float alpha);
 void orc_envmap_value(const orc_scene* s, const float* rd3, int32_t filter, float* out3);
 int32_t orc_envmap_index(const float* wi3, int32_t w, int32_t h);
+/* for n directions (3 floats each): get_envmap_value's filtered lookup (exact3) and the
+   same lookup with its filter weights rounded to multiples of 2^-frac_bits, as texture
+   units filter (quant3): bounds the software filter's difference to hardware filtering */
+void orc_envmap_filter_compare(const orc_scene* s, const float* rd3, uint64_t n, int32_t frac_bits, float* exact3,
+                               float* quant3);
 
 /* deterministic math wrappers (rgr_fmath.h), for accuracy tests */
 float orc_fm(int32_t fn, float x, float y);

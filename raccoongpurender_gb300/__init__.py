@@ -124,6 +124,7 @@ assert STACKLESS_NODE_DTYPE.itemsize == 96
 # exported C symbols and their signatures (include/rgr.h)
 _SIGS = {
     "rgr_status_string": (C.c_char_p, [C.c_int]),
+    "rgr_probe_read_bandwidth": (C.c_int, [C.c_int32, C.c_uint64, C.c_int32, C.POINTER(C.c_double)]),
     "rgr_last_error": (C.c_char_p, []),
     "rgr_bvh_params_default": (None, [C.c_void_p]),
     "rgr_scene_create": (C.c_int, [C.c_void_p]),
@@ -717,6 +718,14 @@ class Guide:
         n = C.c_uint32()
         _check(self._lib.rgr_guide_loss_history(self._h, _ptr(out), max_count, C.byref(n)), "rgr_guide_loss_history")
         return out[:n.value].copy()
+
+
+def probe_read_bandwidth(device: int, nbytes: int, reps: int = 20) -> float:
+    """Read bandwidth (GB/s) over a buffer of `nbytes` on `device`: L2 when the
+    buffer fits in L2, HBM when it does not (rgr_probe_read_bandwidth)."""
+    g = C.c_double()
+    _check(load_library().rgr_probe_read_bandwidth(device, nbytes, reps, C.byref(g)), "rgr_probe_read_bandwidth")
+    return float(g.value)
 
 
 def merge_intermediate_device(a_ptr: int, b_ptr: int, npix: int, stream: int = 0) -> None:

@@ -27,7 +27,7 @@ LIB = LIB_DIR / "librgr.so"
 
 CUDA_SOURCES = ["kernels/trace.cu", "kernels/wavefront.cu", "kernels/guide_mlp.cu", "kernels/guide_tc.cu",
                 "kernels/envmap_gpu.cu", "kernels/bvh_gpu.cu",
-                "host/context.cu", "host/noalloc.cu", "host/guide.cu"]
+                "host/context.cu", "host/noalloc.cu", "host/guide.cu", "host/probe.cu"]
 CXX_SOURCES = ["host/scene.cpp", "host/bvh_build.cpp", "host/envmap_tables.cpp", "host/alembic.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

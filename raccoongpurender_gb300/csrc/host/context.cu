@@ -168,6 +168,10 @@ struct rgr_context {
     QueueView qv{};
     RenderParams rp{};
     bool begun = false;
+    // set by rgr_render_begin (one request accumulating into `accum`), cleared by
+    // every other start: only such a render can be checkpointed
+    bool single_render = false;
+    uint64_t render_sig = 0;  // render_signature() of that render
     uint64_t steps = 0;
     uint32_t npix = 0;
     int shade_grid = 0;
@@ -281,6 +285,7 @@ struct rgr_context {
         graph_steps = (graph_steps + ti - 1) / ti * ti;
         steps = 0;
         begun = true;
+        single_render = false;
         return RGR_OK;
     }
     // train_now: a guided render ends a training interval with this bounce
@@ -289,7 +294,7 @@ struct rgr_context {
         if (guided && rp.gd.max_depth) launch_guide_select(pv, qv, rp.gd, shade_grid, st);
         if (guided) guide->infer_paths(pv, qv, rp.gd, st);
         launch_shade(pv, qv, rp, shade_grid, st);
-        launch_trace_paths(pv, qv, rp, render_trace, st);
+        RGR_CUDA(launch_trace_paths(pv, qv, rp, render_trace, st));
         RGR_CUDA(cudaMemsetAsync(qv.counts + 1, 0, sizeof(uint32_t) * (kNumQueues - 1), st));
         RGR_CUDA(cudaMemsetAsync(qv.tile_new, 0, sizeof(uint32_t) * ntiles, st));
         launch_trace_logic(pv, qv, rp, render_trace, st);
@@ -417,6 +422,33 @@ const rgr::dev::SceneView* rgr_context_scene_view(const rgr_context* c, int* dev
     return &c->scene.sv;
 }
 
+namespace {
+// FNV-1a over the pointer-free description of a render begun with rgr_render_begin:
+// the scene's sizes and bounds, the camera, every config field and the pool size.
+// A checkpoint carries it, and a restore into a render of another scene, camera,
+// spp, seed or flags is refused.
+uint64_t render_signature(const SceneView& sv, const rgr_camera& cam, const rgr_render_config& k, uint32_t npaths) {
+    uint64_t h = 1469598103934665603ull;
+    auto mix = [&h](const void* p, size_t n) {
+        const unsigned char* b = static_cast<const unsigned char*>(p);
+        for (size_t i = 0; i < n; ++i) h = (h ^ b[i]) * 1099511628211ull;
+    };
+    const uint32_t scene[8] = {sv.root_link, sv.num_prims, (uint32_t)sv.sphere_begin, sv.num_nodes,
+                               (uint32_t)sv.env_w, (uint32_t)sv.env_h, (uint32_t)sv.has_env, npaths};
+    mix(scene, sizeof(scene));
+    mix(&cam, sizeof(cam));
+    mix(&k.dof, 4);
+    mix(&k.rr_depth, 4);
+    mix(&k.radiance_clamp, 4);
+    mix(&k.env_select_prob, 4);
+    mix(&k.max_depth, 4);
+    mix(&k.seed_offset, 4);
+    mix(&k.spp, 8);
+    mix(&k.flags, 4);
+    return h;
+}
+}  // namespace
+
 extern "C" {
 
 int rgr_context_create(rgr_context** out, int32_t device, uint32_t path_count) {
@@ -496,7 +528,10 @@ int rgr_render_begin(rgr_context* c, const rgr_camera* cam, const rgr_render_con
                            c->done.as<unsigned long long>());
     if ((r = c->setup_guiding()) != RGR_OK) return r;
     if (c->guided) q.flags |= kFlagFixBacksideEnvPdf | kFlagTwoSidedLambertian;
-    return c->start(&q, 1, limit, k.seed_offset);
+    if ((r = c->start(&q, 1, limit, k.seed_offset)) != RGR_OK) return r;
+    c->single_render = true;
+    c->render_sig = render_signature(c->scene.sv, *cam, k, c->npaths);
+    return RGR_OK;
 }
 
 int rgr_context_set_guide(rgr_context* c, rgr_guide* g) {
@@ -576,13 +611,14 @@ std::vector<StatePart> render_state(rgr_context* c) {
     return v;
 }
 struct CheckpointHeader {
-    char magic[8];  // "RGRCKPT1"
+    char magic[8];  // "RGRCKPT2"
     uint64_t npaths, ntiles, npix, steps, bytes;
+    uint64_t signature;  // render_signature() of the render: scene, camera, config
 };
 int checkpointable(rgr_context* c) {
     if (!c) return RGR_E_INVALID;
-    if (!c->begun || c->guided || c->rp.nreq != 1) {
-        set_error("checkpoint: a render begun with rgr_render_begin, not a guided one, is needed");
+    if (!c->begun || !c->single_render || c->guided || c->rp.nreq != 1 || c->npix == 0) {
+        set_error("checkpoint: a render begun with rgr_render_begin, not a guided one or a batch, is needed");
         return RGR_E_STATE;
     }
     return RGR_OK;
@@ -610,7 +646,8 @@ int rgr_render_checkpoint(rgr_context* c, void* dst, uint64_t dst_bytes) {
     if (!dst || dst_bytes < total) return RGR_E_INVALID;
     RGR_CUDA(cudaSetDevice(c->device));
     RGR_CUDA(cudaStreamSynchronize(c->stream));
-    CheckpointHeader h{{'R', 'G', 'R', 'C', 'K', 'P', 'T', '1'}, c->npaths, c->ntiles, c->npix, c->steps, total};
+    CheckpointHeader h{{'R', 'G', 'R', 'C', 'K', 'P', 'T', '2'}, c->npaths, c->ntiles, c->npix, c->steps, total,
+                       c->render_sig};
     unsigned char* p = static_cast<unsigned char*>(dst);
     memcpy(p, &h, sizeof(h));
     p += sizeof(h);
@@ -628,9 +665,13 @@ int rgr_render_restore(rgr_context* c, const void* src, uint64_t src_bytes) {
     CheckpointHeader h;
     if (!src || src_bytes < sizeof(h)) return RGR_E_INVALID;
     memcpy(&h, src, sizeof(h));
-    if (memcmp(h.magic, "RGRCKPT1", 8) != 0 || h.npaths != c->npaths || h.ntiles != c->ntiles ||
+    if (memcmp(h.magic, "RGRCKPT2", 8) != 0 || h.npaths != c->npaths || h.ntiles != c->ntiles ||
         h.npix != c->npix || h.bytes != checkpoint_bytes(c) || src_bytes < h.bytes) {
         set_error("rgr_render_restore: not a checkpoint of a render of this shape");
+        return RGR_E_INVALID;
+    }
+    if (h.signature != c->render_sig) {
+        set_error("rgr_render_restore: the checkpoint is of a render with another scene, camera or config");
         return RGR_E_INVALID;
     }
     RGR_CUDA(cudaSetDevice(c->device));

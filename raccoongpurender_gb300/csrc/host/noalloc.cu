@@ -21,7 +21,9 @@
 //    host threads) race on the array and give wrong results;
 //  * the first call on a device looks up the array's device address
 //    (cudaGetSymbolAddress), so that first call should come before any stream
-//    capture begins on that device.
+//    capture begins on that device;
+//  * the call is synchronous: it waits for its work on `stream` before it
+//    returns, and it leaves the caller's current device as it found it.
 #include <cuda_runtime.h>
 
 #include <cstring>
@@ -91,6 +93,17 @@ bool ok(cudaError_t e, const char* what) {
     return false;
 }
 
+// puts the caller's current device back on every return
+struct DeviceRestore {
+    int prev = -1;
+    DeviceRestore() {
+        if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
+    }
+    ~DeviceRestore() {
+        if (prev >= 0) cudaSetDevice(prev);
+    }
+};
+
 }  // namespace
 
 extern "C" int rgr_render_noalloc(rgr_context* c, const rgr_camera* cam, const rgr_render_config* cfg,
@@ -109,7 +122,11 @@ extern "C" int rgr_render_noalloc(rgr_context* c, const rgr_camera* cam, const r
         set_error("rgr_render_noalloc: upload a scene to the context first");
         return RGR_E_STATE;
     }
+    DeviceRestore restore_device;
     if (!ok(cudaSetDevice(device), "cudaSetDevice")) return RGR_E_CUDA;
+    int sms = 0;
+    if (!ok(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device), "cudaDeviceGetAttribute"))
+        return RGR_E_CUDA;
     unsigned char* base = nullptr;
     int r = scratch_address(device, &base);
     if (r != RGR_OK) return r;
@@ -182,20 +199,20 @@ extern "C" int rgr_render_noalloc(rgr_context* c, const rgr_camera* cam, const r
         !ok(cudaMemcpyAsync(base + kOffRequest, &rq, sizeof(rq), cudaMemcpyHostToDevice, st), "cudaMemcpyAsync"))
         return RGR_E_CUDA;
     launch_init(p, q, k.seed_offset, st);
-    int sms = 152;
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+    if (!ok(cudaGetLastError(), "kernel launch")) return RGR_E_CUDA;
     const TraceShape ts{true, 24, sms * (trace_paths_max_blocks_per_sm() > 0 ? trace_paths_max_blocks_per_sm() : 1),
                         scal + 3};
     for (int32_t i = 0; i < steps; ++i) {
         launch_compact_new(p, q, st);
         launch_shade(p, q, rp, sms * 8, st);
-        launch_trace_paths(p, q, rp, ts, st);
-        if (!ok(cudaMemsetAsync(q.counts + 1, 0, sizeof(uint32_t) * (kNumQueues - 1), st), "cudaMemsetAsync") ||
+        if (!ok(launch_trace_paths(p, q, rp, ts, st), "cudaMemsetAsync") ||
+            !ok(cudaMemsetAsync(q.counts + 1, 0, sizeof(uint32_t) * (kNumQueues - 1), st), "cudaMemsetAsync") ||
             !ok(cudaMemsetAsync(q.tile_new, 0, sizeof(uint32_t) * ntiles, st), "cudaMemsetAsync"))
             return RGR_E_CUDA;
         launch_trace_logic(p, q, rp, ts, st);
+        // a failed launch stops the call at the bounce it happened in
+        if (!ok(cudaGetLastError(), "kernel launch")) return RGR_E_CUDA;
     }
-    if (!ok(cudaGetLastError(), "kernel launch")) return RGR_E_CUDA;
     uint32_t err = 0;
     if (!ok(cudaMemcpyAsync(&err, rp.err, 4, cudaMemcpyDeviceToHost, st), "cudaMemcpyAsync") ||
         !ok(cudaStreamSynchronize(st), "cudaStreamSynchronize"))

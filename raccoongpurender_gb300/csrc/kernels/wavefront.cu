@@ -1159,11 +1159,13 @@ void launch_shade(const PathsView& p, const QueueView& q, const RenderParams& rp
     else
         k_shade<<<grid, 256, 0, st>>>(p, q, rp);
 }
-void launch_trace_paths(const PathsView& p, const QueueView& q, const RenderParams& rp, const TraceShape& ts,
-                        cudaStream_t st) {
-    if (!ts.persistent) return;
-    cudaMemsetAsync(ts.counter, 0, sizeof(unsigned long long), st);
+cudaError_t launch_trace_paths(const PathsView& p, const QueueView& q, const RenderParams& rp, const TraceShape& ts,
+                               cudaStream_t st) {
+    if (!ts.persistent) return cudaSuccess;
+    const cudaError_t e = cudaMemsetAsync(ts.counter, 0, sizeof(unsigned long long), st);
+    if (e != cudaSuccess) return e;
     k_trace_paths<<<ts.grid, kStackThreads, 0, st>>>(p, q, rp, ts.counter, ts.refill);
+    return cudaSuccess;
 }
 
 void launch_trace_logic(const PathsView& p, const QueueView& q, const RenderParams& rp, const TraceShape& ts,

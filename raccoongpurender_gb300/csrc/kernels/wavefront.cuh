@@ -187,8 +187,9 @@ struct TraceShape {
     int grid;
     unsigned long long* counter;
 };
-void launch_trace_paths(const PathsView& p, const QueueView& q, const RenderParams& rp, const TraceShape& ts,
-                        cudaStream_t st);
+// returns the status of its counter reset (launch errors: cudaGetLastError)
+cudaError_t launch_trace_paths(const PathsView& p, const QueueView& q, const RenderParams& rp, const TraceShape& ts,
+                               cudaStream_t st);
 void launch_trace_logic(const PathsView& p, const QueueView& q, const RenderParams& rp, const TraceShape& ts,
                         cudaStream_t st);
 int trace_paths_max_blocks_per_sm();

@@ -105,3 +105,38 @@ def test_traversal_matches_brute_force(rg, po):
         hit = np.isfinite(ref)
         assert (p >= 0).sum() == hit.sum()
         np.testing.assert_allclose(t[hit], ref[hit], rtol=1e-5, atol=1e-6)
+
+
+def test_oracle_builder_tree_and_hits(po):
+    """The oracle's own tree (binned SAH flattened as create_stackless_bvh does,
+    the reference arm's tree): preorder numbering with sibling and parent
+    links, every triangle in exactly one leaf of at most 4, child boxes that
+    hold their primitives, and closest hits equal to those on the product's
+    tree (the oracle traversal on both)."""
+    mesh = scenes.displaced_icosphere(5, seed=7)
+    osc = po.OracleScene.from_mesh(mesh.points, mesh.indices, max_leaf=4, threads=4)
+    nodes = osc.nodes.view(np.float32).reshape(-1, 24)
+    links = osc.nodes.reshape(-1, 24)
+    parent, L, R, sib, beg, end = (links[:, 16 + k] for k in range(6))
+    n = links.shape[0]
+    tri = mesh.points[mesh.indices]
+    lo, hi = tri.min(1), tri.max(1)
+    assert parent[0] == 0 and sib[0] == 0
+    leaves = end > 0
+    assert (end[leaves] - beg[leaves] <= 4).all()
+    assert sorted(osc.prim_ids.tolist()) == list(range(mesh.ntris))
+    for i in np.nonzero(~leaves)[0]:
+        l, r = int(L[i]), int(R[i])
+        assert l == i + 1 and parent[l] == i and parent[r] == i and sib[l] == r and sib[r] == l
+    for i in np.nonzero(leaves)[0]:
+        p = int(parent[i])
+        box = (nodes[p, 0:3], nodes[p, 4:7]) if int(L[p]) == i else (nodes[p, 8:11], nodes[p, 12:15])
+        ids = osc.prim_ids[beg[i]:end[i]]
+        assert (lo[ids] >= box[0]).all() and (hi[ids] <= box[1]).all()
+    assert n == 2 * leaves.sum() - 1
+    sm, prod = build(mesh)
+    co, inc = scenes.closest_hit_rays(mesh, res=96, n_random=20000, seed=3)
+    for rays in (co, inc):
+        a = osc.trace(rays.packed8(), threads=4, normals=False)
+        b = prod.trace(rays.packed8(), threads=4, normals=False)
+        assert (a[0] == b[0]).all() and (a[1].view(np.uint32) == b[1].view(np.uint32)).all()

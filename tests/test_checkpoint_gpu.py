@@ -50,3 +50,36 @@ def test_checkpoint_resume(rg, which):
     c = _lane(rg, sm, cam, cfg, pool * 2)
     with pytest.raises(rg.RgrError):
         c.restore(state)
+
+
+def test_checkpoint_refuses_another_render(rg):
+    """A checkpoint restores only into a render of the same scene, camera and
+    config: another seed, spp or camera is refused, and so is a checkpoint of a
+    batch context (its sums live in the requests' own buffers)."""
+    mesh = scenes.cornell_box()
+    sm = rg.SceneManager()
+    sm.addMesh(mesh)
+    sm.buildBVH(max_leaf_size=4)
+    camd = scenes.cornell_camera(64, 64)
+    cam = rg.camera_look_at(camd["eye"], camd["target"], camd["up"], camd["vfov"], 64, 64)
+    cfg = rg.render_config(spp=4, max_depth=5, dof=0.0)
+    pool = 1 << 12
+    a = _lane(rg, sm, cam, cfg, pool)
+    a.step(2)
+    state = a.checkpoint()
+    same = _lane(rg, sm, cam, cfg, pool)
+    same.restore(state)  # accepted
+    cam2 = rg.camera_look_at(camd["eye"], (0.0, 0.9, 0.0), camd["up"], camd["vfov"], 64, 64)
+    for other_cam, other_cfg in ((cam, rg.render_config(spp=4, max_depth=5, dof=0.0, seed_offset=7)),
+                                 (cam, rg.render_config(spp=8, max_depth=5, dof=0.0)),
+                                 (cam2, cfg)):
+        other = _lane(rg, sm, other_cam, other_cfg, pool)
+        with pytest.raises(rg.RgrError) as e:
+            other.restore(state)
+        assert e.value.status == -1
+    b = rg.Batch(0, pool)
+    b.add(sm, cam, cfg)
+    b.run(steps_per_launch=4)
+    lib = b._lib
+    n = rg.C.c_uint64(0)
+    assert lib.rgr_render_checkpoint_size(lib.rgr_batch_context(b._h), rg.C.byref(n)) == -4

@@ -150,3 +150,32 @@ def test_host_api(rg, po, mode, pinned):
     lane.synchronize()
     assert (hp.numpy() == p2.cpu().numpy()).all()
     assert (bits(ht.numpy()) == bits(t2.cpu().numpy())).all()
+
+
+def test_headline_scale_level8(rg, po):
+    """The closest-hit workload itself: the 1,310,720-triangle level-8
+    displaced icosphere with its SAH tree (leaves of at most 4), and every
+    16th ray of the 2048x2048 coherent and the 4M incoherent ray sets
+    (262,144 of each), traced through the host entry point and through the
+    device entry point with the autotuned refill threshold."""
+    import torch
+    mesh = scenes.displaced_icosphere(8, seed=7)
+    assert mesh.ntris == 1310720
+    sm, osc = build(mesh, leaf=4)
+    lane = rg.WavefrontLane(0, 1024)
+    lane.setup(sm)
+    coherent, incoherent = scenes.closest_hit_rays(mesh, res=2048, n_random=2048 * 2048, seed=11)
+    idx = np.arange(0, 2048 * 2048, 16)
+    for rays in (coherent.subset(idx), incoherent.subset(idx)):
+        assert len(rays) == 262144
+        p = _check(lane, osc, rays)
+        assert 0.3 < (p >= 0).mean() < 0.99
+        soa = [torch.from_numpy(np.ascontiguousarray(a)).cuda() for a in rays.soa()]
+        dprim = torch.empty(len(rays), dtype=torch.int32, device="cuda")
+        dt = torch.empty(len(rays), dtype=torch.float32, device="cuda")
+        lane.set_trace_tuning(refill=24)
+        lane.trace_closest_device([a.data_ptr() for a in soa], len(rays), dprim.data_ptr(), dt.data_ptr())
+        lane.synchronize()
+        assert (dprim.cpu().numpy() == p).all()
+        oprim, ot, _ = osc.trace(rays.packed8(), threads=16, normals=False)
+        assert (bits(dt.cpu().numpy()) == bits(ot)).all()
