@@ -176,6 +176,71 @@ def render_bench(dev_index: int, which: str, repeats: int = 2, pools=(1 << 22,))
             "config": f"{camd['w']}x{camd['h']}, {spp} spp, max depth {depth}, {mesh.ntris} triangles"}
 
 
+# Algorithmic bytes per extension segment of the wavefront render in this
+# library's structure-of-arrays layout (16-byte vectors per slot), traversal
+# excluded.  Per shaded queue item: the item (4), request id (2), material
+# reference (8), ro, rd, T, L, ng and RNG in (6 x 16) and out (6 x 16), the
+# volume list in (32); the persistent trace: the item (4), ro and rd in (32),
+# ng, t and the volume hit out (24); the logic: queue id (1), request id (2),
+# rd, ng, T, L and RNG in (5 x 16), T, L and RNG out (3 x 16), queue id and
+# queue item out (5); the new-path compaction: the queue id of a slot (1).
+RENDER_STATE_BYTES = (4 + 2 + 8 + 96 + 96 + 32) + (4 + 32 + 24) + (1 + 2 + 80 + 48 + 5) + 1
+
+
+def render_roofline(dev_index: int, mrays_s: float, mpaths_s: float, l2_gbs: float, hbm_gbs: float) -> dict:
+    """Roofline of the mixed 1080p render: bytes per extension segment = the
+    path-state traffic of the SoA layout (RENDER_STATE_BYTES) + 64 per BVH
+    node visited + 48 per primitive tested, the counts measured by the
+    instrumented closest-hit kernel on the extension rays of the render's
+    third bounce (2^22 resident paths).  The state streams from HBM, the tree
+    from L2; both fractions are stated, against the HBM copy rate and the L2
+    read rate measured in this run.  The FP64 accumulation (32 bytes per
+    finished path) is counted per path."""
+    import numpy as np
+    import torch
+    import raccoongpurender_gb300 as rg
+    from raccoongpurender_gb300 import scenes
+    mesh, env, camd = scenes.mixed_scene(level=8, seed=3)
+    sm = rg.SceneManager()
+    sm.addMesh(mesh)
+    sm.setEnvmap(env)
+    sm.buildBVH(max_leaf_size=4)
+    cam = rg.camera_look_at(camd["eye"], camd["target"], camd["up"], camd["vfov"], camd["w"], camd["h"])
+    lane = rg.WavefrontLane(dev_index, 1 << 22)
+    lane.setup(sm)
+    lane.initialize(cam, rg.render_config(spp=64, max_depth=8, dof=0.0045))
+    lane.step(3)
+    lane.synchronize()
+    sl = lane.debug_slots()
+    live = np.asarray(sl["queue"]) >= 0
+    ro = np.asarray(sl["ro"])[live].astype(np.float32)
+    rd = np.asarray(sl["rd"])[live].astype(np.float32)
+    n = int(ro.shape[0])
+    dev = torch.device("cuda", dev_index)
+    soa = [torch.from_numpy(np.ascontiguousarray(x)).to(dev) for x in (ro[:, 0], ro[:, 1], ro[:, 2], rd[:, 0],
+                                                                        rd[:, 1], rd[:, 2])]
+    soa.append(torch.full((n,), 3.4028234663852886e38, dtype=torch.float32, device=dev))
+    prim = torch.empty(n, dtype=torch.int32, device=dev)
+    t = torch.empty(n, dtype=torch.float32, device=dev)
+    nodes = torch.empty(n, dtype=torch.int32, device=dev)
+    prims = torch.empty(n, dtype=torch.int32, device=dev)
+    lane.trace_closest_counts_device([a.data_ptr() for a in soa], n, prim.data_ptr(), t.data_ptr(), nodes.data_ptr(),
+                                     prims.data_ptr())
+    lane.synchronize()
+    nv, pt = float(nodes.double().mean()), float(prims.double().mean())
+    trav = 64.0 * nv + 48.0 * pt
+    seg = mrays_s * 1e6
+    state_gbs = (seg * RENDER_STATE_BYTES + mpaths_s * 1e6 * 32) / 1e9
+    trav_gbs = seg * trav / 1e9
+    return {"rays_sampled": n, "nodes_per_ray": round(nv, 2), "prims_per_ray": round(pt, 2),
+            "state_bytes_per_segment": RENDER_STATE_BYTES, "traversal_bytes_per_segment": round(trav, 1),
+            "state_gbs": round(state_gbs, 1), "state_frac_of_hbm": round(state_gbs / hbm_gbs, 4),
+            "traversal_gbs": round(trav_gbs, 1), "traversal_frac_of_l2": round(trav_gbs / l2_gbs, 4),
+            "time_frac_of_bound": round((state_gbs / hbm_gbs + trav_gbs / l2_gbs), 4),
+            "note": "time_frac_of_bound = state/HBM + traversal/L2: the share of the render's time that the two "
+                    "streams would need at their measured peaks if they did not overlap"}
+
+
 def batch_bench(dev_index: int, n: int = 32) -> dict:
     """Batched uneven requests: n requests (square side log-uniform 64..1024,
     spp log-uniform 1..256, 1k..2M triangles, full-render material mix and
@@ -257,12 +322,15 @@ def bvh_bench(dev_index: int, mesh, sets, stream: int, sah_build_s: float) -> di
 
 
 def guide_kernels_bench(dev_index: int, inference_kernel: int | None = None) -> dict:
-    """The guiding network's kernels on 2^18 random samples: one training
-    iteration (forward + loss + backward on the tensor cores, gradient flush,
-    Adam) and inference (the guide's default inference kernel, or
-    `inference_kernel`), timed with CUDA events on the stream they run on.
+    """The guiding network's kernels on 2^18 random samples, timed with CUDA
+    events on the stream they run on: inference (the guide's default kernel,
+    or `inference_kernel`) and one training iteration (forward + loss +
+    backward + weight gradients, the gradient reduction, Adam, the iteration
+    bookkeeping) for each training kernel, iterations enqueued back to back.
     FLOPs are the network's own (36-64-64-64-64-40: 34,304 per sample forward,
-    2x that backward), not the zero padding the kernels also multiply."""
+    2x that backward), not the zero padding the kernels also multiply; the
+    tcgen05 training kernel issues 75 MMAs of 128x64x16 per 128 samples
+    (forward 19, input gradients 16, weight and bias gradients 40)."""
     import numpy as np
     import torch
     import raccoongpurender_gb300 as rg
@@ -277,31 +345,41 @@ def guide_kernels_bench(dev_index: int, inference_kernel: int | None = None) -> 
         v = rng.normal(size=(n, 3))
         rows[:, c:c + 3] = v / np.linalg.norm(v, axis=1, keepdims=True)
     rows[:, 12] = rng.uniform(0.1, 2.0, n)
+    rows[:, 13] = np.maximum((rows[:, 3:6] * rows[:, 9:12]).sum(axis=1), 0.0) / np.pi  # a cosine BSDF pdf
     s = torch.from_numpy(rows).cuda(dev_index)
-    out = torch.empty((n, 40), dtype=torch.float32, device=s.device)
+    out = torch.empty((n, 48), dtype=torch.float32, device=s.device)
     st = torch.cuda.Stream(device=s.device)
     sp = st.cuda_stream
     for _ in range(3):
-        g.train_device(s.data_ptr(), n, weight_scale=1.0 / n, apply_adam=True, stream=sp)
         g.infer_device(s.data_ptr(), n, out.data_ptr(), stream=sp)
     torch.cuda.synchronize()
     reps = 20
-    with torch.cuda.stream(st):
-        e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+
+    def timed(fn) -> float:
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(st)
         for _ in range(reps):
-            g.infer_device(s.data_ptr(), n, out.data_ptr(), stream=sp)
+            fn()
         e1.record(st)
-    torch.cuda.synchronize()
-    infer_ms = e0.elapsed_time(e1) / reps
-    t0 = time.perf_counter()
-    for _ in range(reps):
-        g.train_device(s.data_ptr(), n, weight_scale=1.0 / n, apply_adam=True, stream=sp)  # synchronous
-    train_ms = (time.perf_counter() - t0) * 1e3 / reps
+        e1.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    infer_ms = timed(lambda: g.infer_device(s.data_ptr(), n, out.data_ptr(), stream=sp))
+    train = {}
+    for name, kernel in (("tcgen05", rg.GUIDE_TCGEN05), ("mma_sync", rg.GUIDE_MMA_SYNC)):
+        gt = rg.Guide(dev_index, training_kernel=kernel)
+        gt.set_bounds((-1, -1, -1), (1, 1, 1))
+        for _ in range(3):
+            gt.train_device_async(s.data_ptr(), n, weight_scale=1.0 / n, stream=sp)
+        torch.cuda.synchronize()
+        ms = timed(lambda: gt.train_device_async(s.data_ptr(), n, weight_scale=1.0 / n, stream=sp))
+        gt.check()
+        train[name] = {"iteration_ms": round(ms, 4), "network_tflops": round(3 * n * fwd / ms / 1e9, 1)}
+    train["tcgen05"]["mma_tflops"] = round(75 * (n / 128) * 2 * 128 * 64 * 16 / train["tcgen05"]["iteration_ms"] / 1e9, 1)
     return {"samples": n, "infer_ms": round(infer_ms, 4), "infer_tflops": round(n * fwd / infer_ms / 1e9, 1),
-            "train_iteration_ms": round(train_ms, 4),
-            "train_tflops": round(3 * n * fwd / train_ms / 1e9, 1),
-            "note": "train time is host wall time of a synchronous call (includes launch and sync overhead)"}
+            "train_iteration_ms": train["tcgen05"]["iteration_ms"],
+            "train_tflops": train["tcgen05"]["network_tflops"], "train_by_kernel": train,
+            "note": "CUDA events around 20 iterations enqueued back to back on one stream"}
 
 
 def guiding_bench(dev_index: int, w: int = 960, h: int = 540, spp: int = 256, ref_spp: int = 16384) -> dict:
@@ -311,7 +389,7 @@ def guiding_bench(dev_index: int, w: int = 960, h: int = 540, spp: int = 256, re
     online on the render's own samples for its first 120 iterations, then is
     frozen; inference and training inside the time) and "warm" (a guide
     trained online by an earlier 1024-spp render of the same view, frozen; in
-    the room also by a 4096-spp render).  Medians over 3 seeds.  Scenes: the full-render glossy/volume scene (the 1.31M-triangle
+    the room also by a 4096-spp render).  8 seeds: medians, means and ranges.  Scenes: the full-render glossy/volume scene (the 1.31M-triangle
     sphere, ground, volume box, sky + sun) and the sky-lit room."""
     import raccoongpurender_gb300 as rg
     from raccoongpurender_gb300 import guiding, scenes
@@ -614,7 +692,14 @@ def main() -> None:
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
 
+    # the roof of the closest-hit kernel, measured before any traversal has marked
+    # the tree's lines evict-last in L2: the L2 read bandwidth over a buffer the
+    # size of the tree, and the same probe over 4 GiB (HBM)
     mesh, sm, coherent, incoherent, build_s = build_workload()
+    info0 = sm.info()
+    ws_bytes = int(info0.num_inner_nodes) * 64 + int(mesh.ntris) * 48
+    l2_gbs = rg.probe_read_bandwidth(local, ws_bytes, reps=5)
+    hbm_read_gbs = rg.probe_read_bandwidth(local, 4 << 30, reps=3)
     n_each = len(coherent)
     lane = rg.WavefrontLane(local, 1024)
     lane.setup(sm)
@@ -730,12 +815,8 @@ def main() -> None:
     inc_bytes = bytes_per_ray[1] * n_each
     achieved = (coh_bytes + inc_bytes) / ((coh_ms + inc_ms) * 1e-3) / 1e9
     # the roof: the tree (inner nodes + primitive records) is L2-resident, so the
-    # denominator is the L2 read bandwidth measured now over a buffer of its size;
-    # an HBM-sized read of the same probe and the measured HBM copy rate beside it
-    info0 = sm.info()
-    ws_bytes = int(info0.num_inner_nodes) * 64 + int(mesh.ntris) * 48
-    l2_gbs = rg.probe_read_bandwidth(local, ws_bytes, reps=50)
-    hbm_read_gbs = rg.probe_read_bandwidth(local, 4 << 30, reps=10)
+    # denominator is the L2 read bandwidth over a buffer of its size (measured at
+    # the start); the HBM read probe and the measured HBM copy rate beside it
     traffic = args.traffic_bytes
     roof = {"bound": "l2", "achieved": round(achieved, 1), "peak": round(l2_gbs, 1), "unit": "GB/s",
             "frac": round(achieved / l2_gbs, 4), "traffic": traffic,
@@ -766,6 +847,9 @@ def main() -> None:
                   "scene_load_alembic": scene_load_bench(),
                   "image_error_vs_fp64_reference": {"cornell_256_4spp": image_error(local, "cornell", 4096),
                                                     "mixed_1080p_64spp": image_error(local, "mixed", 1024)}}
+        mx = render["mixed_1080p_64spp"]
+        render["mixed_1080p_64spp"]["roofline"] = render_roofline(local, mx["mrays_s"], mx["mpaths_s"], l2_gbs,
+                                                                  measured_peaks()["hbm_gbs"])
     bvh = bvh_bench(local, mesh, [([a.data_ptr() for a in soa], n, prim.data_ptr(), t.data_ptr())
                                   for soa, prim, t, n in sets], sptr, build_s) if not args.no_render else None
     guide = None

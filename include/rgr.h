@@ -362,7 +362,8 @@ typedef struct rgr_guide_config {
     float epsilon;           /* Adam (1e-8) */
     uint32_t batch_samples;  /* training samples per iteration (2^18); while rendering, an iteration
                                 waits (over several bounces if need be) for 1/16 of it */
-    float guide_fraction;    /* share of the non-envmap selection probability given to the guide (0.5) */
+    float guide_fraction;    /* share of the non-envmap selection probability given to the guide when
+                                learn_fraction is 0 (0.5) */
     int32_t train;           /* train online while rendering (1), or keep the weights fixed (0) */
     int32_t guide_volumes;   /* guide in-volume scattering too (0: the isotropic phase function and
                                 envmap sampling stay; guiding it doubles the largest per-vertex weight) */
@@ -372,10 +373,18 @@ typedef struct rgr_guide_config {
                                  activations, MMA-issuing warps apart from the row threads, five
                                  128-row tiles in flight per SM (2x faster than mma.sync);
                                  RGR_GUIDE_MMA_SYNC: warp-level mma.sync with the whole network in
-                                 register fragments.  Training always runs on mma.sync kernels. */
+                                 register fragments. */
     uint32_t max_depth;      /* guide only the first max_depth vertices of a path (0: every vertex); the
                                 others use BSDF and envmap sampling alone and cost no inference */
     uint64_t seed;           /* weight initialisation (1) */
+    int32_t training_kernel; /* RGR_GUIDE_TCGEN05 (default): forward, backward and the weight gradients
+                                as tcgen05.mma from shared memory into TMEM accumulators, two 128-sample
+                                tiles in flight per SM, per-SM gradient slots summed in a fixed order;
+                                RGR_GUIDE_MMA_SYNC: warp-level mma.sync with a shared-memory gradient
+                                accumulator per CTA */
+    int32_t learn_fraction;  /* 1 (default): the guide's share of the non-envmap selection probability is a
+                                network output per vertex, in [0.05, 0.95], trained on the KL divergence of
+                                the guide-BSDF mixture (Mueller et al. 2019); 0: guide_fraction everywhere */
 } rgr_guide_config;
 typedef struct rgr_guide_stats {
     uint64_t iterations;     /* Adam steps taken */
@@ -402,16 +411,22 @@ int rgr_guide_set_weights(rgr_guide* g, const float* w, const float* b);
 /* Use the guide in the context's next rgr_render_begin (NULL: plain rendering).
    The guide must live on the context's device and outlive its renders. */
 int rgr_context_set_guide(rgr_context* c, rgr_guide* g);
-/* Raw network outputs, 40 floats per row, of rows of 16 floats whose first 9
-   are (position, normal, outgoing direction); device pointers, on `stream`. */
+/* Raw network outputs, 48 floats per row (the mixture's 40, field-major; the selection
+   logit; 7 zeros), of rows of 16 floats whose first 9 are (position, normal, outgoing
+   direction); device pointers, on `stream`. */
 int rgr_guide_infer_device(rgr_guide* g, const float* rows, uint32_t n, float* out, void* stream);
 /* One training step on n samples of 16 floats (position, normal, outgoing,
-   incident direction, weight, 3 unused), each weight multiplied by
+   incident direction, weight, BSDF pdf of the incident direction (0: none, no
+   selection-probability term), 2 unused), each weight multiplied by
    weight_scale.  grads (device, may be NULL) receives the gradient of the
    loss, weights then biases (5*64*64 + 5*64 floats); *loss (host, may be NULL)
    the loss.  apply_adam = 0 leaves the network unchanged. Synchronous. */
 int rgr_guide_train_device(rgr_guide* g, const float* samples, uint32_t n, float weight_scale, int32_t apply_adam,
                            float* grads, float* loss, void* stream);
+/* The same training step with Adam, enqueued on `stream` without waiting for it (the
+   loss is in rgr_guide_loss_history once the stream has run it): for timing
+   iterations back to back.  samples must stay valid until the stream has run it. */
+int rgr_guide_train_device_async(rgr_guide* g, const float* samples, uint32_t n, float weight_scale, void* stream);
 int rgr_guide_stats_get(rgr_guide* g, rgr_guide_stats* st);
 /* RGR_OK, or RGR_E_CUDA when a tensor-core wait of the guide's kernels timed out since the
    last check (each wait gives up after about a second; the kernel then stops, frees its
@@ -431,7 +446,9 @@ int rgr_guide_last_batch(rgr_guide* g, float* out, uint32_t max, uint32_t* count
 /* Read bandwidth of `device` over a buffer of `bytes` (no reference counterpart: the
    denominator of the closest-hit roofline).  Streams the buffer with 16-byte loads that
    bypass L1 after a warm-up pass, so a buffer smaller than L2 measures L2 read bandwidth
-   and a larger one HBM; *gbs = bytes * reps / time.  Allocates its own buffer. */
+   and a larger one HBM; each of the `reps` timed launches reads the buffer as many times
+   as make 1 GiB; *gbs = bytes read / time.  Allocates its own buffer.  Lines another
+   kernel marked evict-last stay in L2 and shrink what the buffer can use. */
 int rgr_probe_read_bandwidth(int32_t device, uint64_t bytes, int32_t reps, double* gbs);
 const char* rgr_status_string(int status);
 const char* rgr_last_error(void);

@@ -12,7 +12,7 @@ CUDA kernels implement:
   and direction mapped by (c + 1) / 2) and octaves k = 0, 1:
   sin(2^k pi v), cos(2^k pi v)  ->  36 inputs (the lowest period is 2, so
   that opposite directions, v = 0 and v = 1, encode differently);
-* an MLP 36 -> 64 -> 64 -> 64 -> 64 -> 40 with ReLU, stored as five
+* an MLP 36 -> 64 -> 64 -> 64 -> 64 -> 41 with ReLU, stored as five
   zero-padded 64 x 64 matrices W[l][in][out] and biases b[l][64];
 * an 8-lobe von Mises-Fisher mixture read from the 40 outputs, field-major
   (output 8 f + i is field f of lobe i; per lobe: mean
@@ -25,6 +25,12 @@ CUDA kernels implement:
   (Mueller et al., "Neural Importance Sampling", ACM TOG 2019), plus
   w * 0.01 * sum over lobes of (|o| - 1)^2, which keeps the direction
   outputs' length near 1;
+* the learned selection probability of the same paper: output 40 is the logit
+  z of the guide's share a = A_MIN + (A_MAX - A_MIN) sigmoid(z) of the
+  non-envmap sampling probability, trained on the KL divergence of the
+  one-sample mixture a q(d) + (1 - a) p_bsdf(d): the term
+  -w log(a q + (1 - a) p_bsdf) of a sample that carries its BSDF pdf
+  (p_bsdf > 0), with q held fixed (its gradient reaches z only);
 * Adam (Kingma and Ba, ICLR 2015) with bias correction.
 
 With ``bf16=True`` the oracle rounds the values the kernels round to BF16
@@ -40,11 +46,15 @@ from __future__ import annotations
 import numpy as np
 
 LAYERS, WIDTH, INPUTS, OUTPUTS, LOBES = 5, 64, 36, 40, 8
+SEL = 40              # output index of the selection-probability logit
+NET_OUTPUTS = 41      # the mixture's 40 outputs and the selection logit
+ROW_OUTPUTS = 48      # raw outputs per row as the inference entry point writes them
+A_MIN, A_MAX = 0.05, 0.95  # range of the guide's share of the non-envmap probability
 KAPPA_MAX = 5000.0
 LOGIT_BOUND = 5.0     # lobe weight logits are LOGIT_BOUND * tanh(o / LOGIT_BOUND)
 NORM_PENALTY = 0.01   # weight of (|o| - 1)^2 per lobe direction output
 FAN_IN = [INPUTS, WIDTH, WIDTH, WIDTH, WIDTH]
-FAN_OUT = [WIDTH, WIDTH, WIDTH, WIDTH, OUTPUTS]
+FAN_OUT = [WIDTH, WIDTH, WIDTH, WIDTH, NET_OUTPUTS]
 
 
 def bf16(x) -> np.ndarray:
@@ -76,7 +86,7 @@ def encode(x9: np.ndarray, lo, inv_ext) -> np.ndarray:
 
 
 def forward(W: np.ndarray, b: np.ndarray, feats: np.ndarray, bf16_round: bool = True):
-    """Raw outputs (n, 40) and each layer's input (for backward)."""
+    """Raw outputs (n, 41) and each layer's input (for backward)."""
     W = np.asarray(W, np.float64)
     b = np.asarray(b, np.float64)
     Wq = bf16(W) if bf16_round else W
@@ -91,7 +101,7 @@ def forward(W: np.ndarray, b: np.ndarray, feats: np.ndarray, bf16_round: bool = 
             h = bf16(z) if bf16_round else z
         else:
             h = z
-    return h[:, :OUTPUTS], acts
+    return h[:, :NET_OUTPUTS], acts
 
 
 def softplus(x):
@@ -99,9 +109,15 @@ def softplus(x):
 
 
 def lobes(raw: np.ndarray) -> np.ndarray:
-    """Raw outputs (n, 40), field-major (output 8 f + i is field f of lobe i),
-    as (n, lobe, field)."""
-    return raw.reshape(-1, 5, LOBES).transpose(0, 2, 1)
+    """The mixture's raw outputs (the first 40 of a row), field-major (output
+    8 f + i is field f of lobe i), as (n, lobe, field)."""
+    return np.ascontiguousarray(raw[:, :OUTPUTS]).reshape(-1, 5, LOBES).transpose(0, 2, 1)
+
+
+def alpha(raw: np.ndarray) -> np.ndarray:
+    """The guide's share of the non-envmap sampling probability per row."""
+    z = np.asarray(raw, np.float64)[:, SEL]
+    return A_MIN + (A_MAX - A_MIN) / (1.0 + np.exp(-z))
 
 
 def mixture(raw: np.ndarray):
@@ -134,9 +150,21 @@ def penalty(raw: np.ndarray, w: np.ndarray) -> np.ndarray:
     return w * NORM_PENALTY * ((nrm - 1.0) ** 2).sum(axis=1)
 
 
-def loss_and_grad(raw: np.ndarray, d: np.ndarray, w: np.ndarray):
-    """Per-sample loss -w log q(d), and the gradient of -w log q(d) + penalty
-    with respect to the raw outputs (n, 40), analytic."""
+def selection_loss(raw: np.ndarray, d: np.ndarray, w: np.ndarray, pb: np.ndarray, q_fixed=None) -> np.ndarray:
+    """Per-sample -w log(a q + (1 - a) p_bsdf) for samples with p_bsdf > 0 (else 0),
+    with q the mixture density (or `q_fixed`, the density the gradient treats as
+    a constant)."""
+    q = mixture_pdf(raw, d) if q_fixed is None else q_fixed
+    a = alpha(raw)
+    live = pb > 0.0
+    mix = np.where(live, a * q + (1.0 - a) * pb, 1.0)
+    return np.where(live, -w * np.log(np.maximum(mix, 1e-30)), 0.0)
+
+
+def loss_and_grad(raw: np.ndarray, d: np.ndarray, w: np.ndarray, pb: np.ndarray | None = None):
+    """Per-sample loss -w log q(d), and the gradient with respect to the raw
+    outputs (n, 41), analytic, of -w log q(d) + penalty + the selection term
+    -w log(a q(d) + (1 - a) p_bsdf) (samples with p_bsdf > 0; q held fixed)."""
     o = lobes(raw)
     mu, kappa, pi, nrm, th = mixture(raw)
     c = np.einsum("nkc,nc->nk", mu, d)
@@ -152,7 +180,17 @@ def loss_and_grad(raw: np.ndarray, d: np.ndarray, w: np.ndarray):
     gmu = (-W * r * kappa)[:, :, None] * d[:, None, :]
     gm = (gmu * mu).sum(axis=2, keepdims=True)
     g[:, :, 0:3] = (gmu - gm * mu) / nrm[:, :, None] + (2.0 * W * NORM_PENALTY * (nrm - 1.0))[:, :, None] * mu
-    return -w * np.log(q), g.transpose(0, 2, 1).reshape(-1, OUTPUTS)
+    gout = np.zeros((raw.shape[0], NET_OUTPUTS))
+    gout[:, :OUTPUTS] = g.transpose(0, 2, 1).reshape(-1, OUTPUTS)
+    if pb is not None and raw.shape[1] > SEL:
+        pb = np.asarray(pb, np.float64)
+        z = np.asarray(raw, np.float64)[:, SEL]
+        sg = 1.0 / (1.0 + np.exp(-z))
+        a = A_MIN + (A_MAX - A_MIN) * sg
+        live = pb > 0.0
+        mix = np.maximum(a * q + (1.0 - a) * pb, 1e-30)
+        gout[:, SEL] = np.where(live, -w * (q - pb) / mix * (A_MAX - A_MIN) * sg * (1.0 - sg), 0.0)
+    return -w * np.log(q), gout
 
 
 def backward(W: np.ndarray, acts, dy_out: np.ndarray, bf16_round: bool = True):
@@ -160,7 +198,7 @@ def backward(W: np.ndarray, acts, dy_out: np.ndarray, bf16_round: bool = True):
     W = np.asarray(W, np.float64)
     Wq = bf16(W) if bf16_round else W
     dy = np.zeros((dy_out.shape[0], WIDTH))
-    dy[:, :OUTPUTS] = dy_out
+    dy[:, :dy_out.shape[1]] = dy_out
     if bf16_round:
         dy = bf16(dy)
     dW = np.zeros((LAYERS, WIDTH, WIDTH))
@@ -176,26 +214,40 @@ def backward(W: np.ndarray, acts, dy_out: np.ndarray, bf16_round: bool = True):
 
 
 def gradients(W, b, samples: np.ndarray, lo, inv_ext, weight_scale: float = 1.0, bf16_round: bool = True):
-    """(loss, dW, db) of a batch of samples (n, 16): x, n, wo, wi, weight."""
+    """(loss, dW, db) of a batch of samples (n, 16): x, n, wo, wi, weight,
+    BSDF pdf of wi (0: none).  The loss is the sum of -w log q(d); the
+    gradients include the selection term."""
     s = np.asarray(samples, np.float32)
     feats = encode(s[:, 0:9], lo, inv_ext)
     raw, acts = forward(W, b, feats, bf16_round)
     w = s[:, 12].astype(np.float64) * weight_scale
-    loss, g = loss_and_grad(raw, s[:, 9:12].astype(np.float64), w)
+    loss, g = loss_and_grad(raw, s[:, 9:12].astype(np.float64), w, s[:, 13].astype(np.float64))
     g[w <= 0.0] = 0.0
     loss[w <= 0.0] = 0.0
     dW, db = backward(W, acts, g, bf16_round)
     return float(loss.sum()), dW, db
 
 
-def objective(W, b, samples: np.ndarray, lo, inv_ext, weight_scale: float = 1.0, bf16_round: bool = False) -> float:
-    """The function the gradients differentiate: sum of -w log q(d) + penalty."""
+def objective(W, b, samples: np.ndarray, lo, inv_ext, weight_scale: float = 1.0, bf16_round: bool = False,
+              q_fixed=None) -> float:
+    """The function the gradients differentiate: sum of -w log q(d) + penalty
+    + the selection term, in which q is `q_fixed` (the mixture density at the
+    point of differentiation: the gradient treats it as a constant)."""
     s = np.asarray(samples, np.float32)
     raw, _ = forward(W, b, encode(s[:, 0:9], lo, inv_ext), bf16_round)
     w = s[:, 12].astype(np.float64) * weight_scale
-    loss, _ = loss_and_grad(raw, s[:, 9:12].astype(np.float64), w)
+    d = s[:, 9:12].astype(np.float64)
+    loss, _ = loss_and_grad(raw, d, w)
+    sel = selection_loss(raw, d, w, s[:, 13].astype(np.float64), q_fixed)
     keep = w > 0.0
-    return float(loss[keep].sum() + penalty(raw, w)[keep].sum())
+    return float(loss[keep].sum() + penalty(raw, w)[keep].sum() + sel[keep].sum())
+
+
+def mixture_density(W, b, samples: np.ndarray, lo, inv_ext, bf16_round: bool = False) -> np.ndarray:
+    """q(d) of each sample's direction under the network (W, b)."""
+    s = np.asarray(samples, np.float32)
+    raw, _ = forward(W, b, encode(s[:, 0:9], lo, inv_ext), bf16_round)
+    return mixture_pdf(raw, s[:, 9:12].astype(np.float64))
 
 
 def adam(p, g, m, v, t: int, lr=1e-3, beta1=0.9, beta2=0.999, eps=1e-8):
@@ -244,4 +296,7 @@ def random_samples(n: int, seed: int, lo=(-1, -1, -1), hi=(1, 1, 1)) -> np.ndarr
     s[:, 6:9] = wo
     s[:, 9:12] = unit(n)
     s[:, 12] = 0.1 + 1.9 * rng.random(n)
+    # the BSDF pdf of wi: a cosine lobe around the normal (0 below it), none for every 8th
+    c = (s[:, 9:12] * nrm).sum(axis=1)
+    s[:, 13] = np.where(np.arange(n) % 8 == 7, 0.0, np.maximum(c, 0.0) / np.pi)
     return s

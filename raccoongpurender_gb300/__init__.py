@@ -90,10 +90,11 @@ class rgr_guide_config(C.Structure):
     _fields_ = [("learning_rate", C.c_float), ("beta1", C.c_float), ("beta2", C.c_float), ("epsilon", C.c_float),
                 ("batch_samples", C.c_uint32), ("guide_fraction", C.c_float), ("train", C.c_int32),
                 ("guide_volumes", C.c_int32), ("train_interval", C.c_uint32), ("max_iterations", C.c_uint32),
-                ("inference_kernel", C.c_int32), ("max_depth", C.c_uint32), ("seed", C.c_uint64)]
+                ("inference_kernel", C.c_int32), ("max_depth", C.c_uint32), ("seed", C.c_uint64),
+                ("training_kernel", C.c_int32), ("learn_fraction", C.c_int32)]
 
 
-GUIDE_TCGEN05, GUIDE_MMA_SYNC = 0, 1  # rgr_guide_config.inference_kernel
+GUIDE_TCGEN05, GUIDE_MMA_SYNC = 0, 1  # rgr_guide_config.inference_kernel and .training_kernel
 TRACE_HOST_AUTO, TRACE_HOST_COPY = 0, 1  # rgr_set_trace_host_mode
 
 
@@ -190,6 +191,7 @@ _SIGS = {
     "rgr_guide_infer_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p]),
     "rgr_guide_train_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_float, C.c_int32, C.c_void_p,
                                          C.c_void_p, C.c_void_p]),
+    "rgr_guide_train_device_async": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_float, C.c_void_p]),
     "rgr_guide_stats_get": (C.c_int, [C.c_void_p, C.c_void_p]),
     "rgr_guide_loss_history": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p]),
     "rgr_guide_last_batch": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p]),
@@ -627,6 +629,7 @@ class Guide:
     cores, trained online by Adam while a WavefrontLane renders with it."""
 
     LAYERS, WIDTH, INPUTS, OUTPUTS, LOBES = 5, 64, 36, 40, 8
+    SEL, ROW_OUTPUTS = 40, 48  # the selection logit's output index; raw outputs per row of infer_device
     N_WEIGHTS = LAYERS * WIDTH * WIDTH
     N_PARAMS = N_WEIGHTS + LAYERS * WIDTH
 
@@ -679,7 +682,8 @@ class Guide:
         _check(self._lib.rgr_guide_set_weights(self._h, _ptr(w), _ptr(b)), "rgr_guide_set_weights")
 
     def infer_device(self, rows_ptr: int, n: int, out_ptr: int, stream: int = 0) -> None:
-        """Raw outputs (40 floats per row) of device rows of 16 floats (x, n, wo, ...)."""
+        """Raw outputs (48 floats per row: the mixture's 40, the selection logit, zeros)
+        of device rows of 16 floats (x, n, wo, ...)."""
         _check(self._lib.rgr_guide_infer_device(self._h, rows_ptr, n, out_ptr, stream or None),
                "rgr_guide_infer_device")
 
@@ -691,6 +695,12 @@ class Guide:
                                                 grads_ptr or None, C.byref(loss), stream or None),
                "rgr_guide_train_device")
         return loss.value
+
+    def train_device_async(self, samples_ptr: int, n: int, weight_scale: float = 1.0, stream: int = 0) -> None:
+        """One training step with Adam on n device samples, enqueued on `stream`
+        without waiting (rgr_guide_train_device_async)."""
+        _check(self._lib.rgr_guide_train_device_async(self._h, samples_ptr, n, weight_scale, stream or None),
+               "rgr_guide_train_device_async")
 
     def check(self) -> None:
         """Raise if a tensor-core wait of the guide's kernels timed out since the last check."""

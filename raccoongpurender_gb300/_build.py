@@ -25,7 +25,7 @@ BUILD = ROOT / "_build" / "rgr"
 LIB_DIR = PKG / "_lib"
 LIB = LIB_DIR / "librgr.so"
 
-CUDA_SOURCES = ["kernels/trace.cu", "kernels/wavefront.cu", "kernels/guide_mlp.cu", "kernels/guide_tc.cu",
+CUDA_SOURCES = ["kernels/trace.cu", "kernels/wavefront.cu", "kernels/guide_mlp.cu", "kernels/guide_tc.cu", "kernels/guide_train_tc.cu",
                 "kernels/envmap_gpu.cu", "kernels/bvh_gpu.cu",
                 "host/context.cu", "host/noalloc.cu", "host/guide.cu", "host/probe.cu"]
 CXX_SOURCES = ["host/scene.cpp", "host/bvh_build.cpp", "host/envmap_tables.cpp", "host/alembic.cpp"]

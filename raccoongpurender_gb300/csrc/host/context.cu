@@ -340,6 +340,7 @@ struct rgr_context {
         gd.nrec = gnrec.as<uint8_t>();
         gd.train = guide->train;
         gd.guide_frac = guide->cfg.guide_fraction;
+        gd.learn_frac = guide->cfg.learn_fraction != 0 ? 1 : 0;
         gd.volumes = guide->cfg.guide_volumes ? 1 : 0;
         gd.record = guide->cfg.train ? 1 : 0;
         gd.max_depth = guide->cfg.max_depth;

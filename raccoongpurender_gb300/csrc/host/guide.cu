@@ -3,6 +3,7 @@
 // and the per-bounce training launches of a guided render.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <new>
@@ -40,9 +41,17 @@ uint16_t to_bf16(float f) {
 
 // The network's real shape inside the zero-padded 64 x 64 layers.
 int fan_in(int l) { return l == 0 ? kGuideInputs : kGuideWidth; }
-int fan_out(int l) { return l == kGuideLayers - 1 ? kGuideOutputs : kGuideWidth; }
+int fan_out(int l) { return l == kGuideLayers - 1 ? kGuideNetOutputs : kGuideWidth; }
 // samples an online iteration waits for before it trains: 1/16 of the batch
 uint32_t min_batch(const rgr_guide_config& c) { return std::max<uint32_t>(1u, c.batch_samples / 16u); }
+
+// the training grid for n samples on the host-side entry points: the mma.sync
+// kernel takes 64-sample chunks, the tcgen05 one 128-sample tiles two at a time,
+// at most one CTA per SM
+int train_grid(const rgr_guide& g, uint32_t n) {
+    const uint32_t per_cta = g.cfg.training_kernel == RGR_GUIDE_TCGEN05 ? 256u : 64u;
+    return (int)std::min<uint32_t>(std::max<uint32_t>((n + per_cta - 1) / per_cta, 1u), (uint32_t)g.num_sms);
+}
 
 bool check_padding(const float* w, const float* b) {
     for (int l = 0; l < kGuideLayers; ++l)
@@ -79,6 +88,7 @@ int rgr_guide::init(const rgr_guide_config& c) {
     AL(counters, kCtrBytes);
     AL(loss_hist, 4 * kLossHist);
     AL(wtsw, kGuideWtBytes);
+    AL(gpart, 4 * (size_t)kGuidePartStride * (size_t)num_sms);
 #undef AL
     GuideView& g = view;
     g.w = w.as<float>();
@@ -113,13 +123,15 @@ int rgr_guide::init(const rgr_guide_config& c) {
     train.max_iter = cfg.max_iterations;
     train.min_count = min_batch(cfg);
     // He-uniform initialisation of the real part of each layer (the output layer
-    // scaled by 1/4 so that the first mixtures are broad), zero biases and padding
+    // scaled by 1/4 so that the first mixtures are broad), zero biases and padding;
+    // the selection logit's column starts at zero (the guide's share starts at
+    // 0.5 everywhere)
     std::vector<float> hw(kGuideWeights, 0.0f), hb(kGuideBiases, 0.0f);
     uint64_t s = cfg.seed;
     for (int l = 0; l < kGuideLayers; ++l) {
         const float lim = std::sqrt(6.0f / (float)fan_in(l)) * (l == kGuideLayers - 1 ? 0.25f : 1.0f);
         for (int i = 0; i < fan_in(l); ++i)
-            for (int o = 0; o < fan_out(l); ++o) {
+            for (int o = 0; o < (l == kGuideLayers - 1 ? kGuideOutputs : fan_out(l)); ++o) {
                 const double u = (double)(splitmix64(s) >> 11) * (1.0 / 9007199254740992.0);
                 hw[(l * kGuideWidth + i) * kGuideWidth + o] = (float)((2.0 * u - 1.0) * lim);
             }
@@ -146,10 +158,20 @@ void rgr_guide::infer_paths(const PathsView& p, const QueueView& q, const GuideR
         launch_guide_infer_paths(view, p, q, gd, guide_infer_grid(num_sms), st);
 }
 
+void rgr_guide::gradient_launches(const float* smp, const uint32_t* count, uint32_t cap, uint32_t min_count,
+                                  const float* wsum, float weight_scale, int grid, cudaStream_t st) {
+    if (cfg.training_kernel == RGR_GUIDE_TCGEN05) {
+        launch_guide_train_tc(view, smp, count, cap, min_count, wsum, weight_scale, grid, gpart.as<float>(),
+                              error_word(), st);
+        launch_guide_grad_reduce(view, gpart.as<float>(), (uint32_t)grid, count, min_count, st);
+    } else {
+        launch_guide_train(view, smp, count, cap, min_count, wsum, weight_scale, grid, st);
+    }
+}
+
 int rgr_guide::train_launches(cudaStream_t st) {
     if (cfg.train) {
-        launch_guide_train(view, train.samples, train.count, train.cap, train.min_count, train.wsum, 1.0f, num_sms,
-                           st);
+        gradient_launches(train.samples, train.count, train.cap, train.min_count, train.wsum, 1.0f, num_sms, st);
         launch_guide_adam(view, train.count, train.min_count, train.iter, cfg.learning_rate, cfg.beta1, cfg.beta2,
                           cfg.epsilon, st);
     }
@@ -175,6 +197,8 @@ void rgr_guide_config_default(rgr_guide_config* c) {
     c->inference_kernel = RGR_GUIDE_TCGEN05;
     c->max_depth = 0;
     c->seed = 1;
+    c->training_kernel = RGR_GUIDE_TCGEN05;
+    c->learn_fraction = 1;
 }
 
 static bool valid_config(const rgr_guide_config& c) {
@@ -182,7 +206,8 @@ static bool valid_config(const rgr_guide_config& c) {
            c.beta2 >= 0.0f && c.beta2 < 1.0f && c.epsilon > 0.0f && c.batch_samples >= 64 &&
            c.batch_samples <= (1u << 24) && c.guide_fraction >= 0.0f && c.guide_fraction <= 1.0f &&
            c.train_interval >= 1 && c.train_interval <= 64 &&
-           (c.inference_kernel == RGR_GUIDE_TCGEN05 || c.inference_kernel == RGR_GUIDE_MMA_SYNC);
+           (c.inference_kernel == RGR_GUIDE_TCGEN05 || c.inference_kernel == RGR_GUIDE_MMA_SYNC) &&
+           (c.training_kernel == RGR_GUIDE_TCGEN05 || c.training_kernel == RGR_GUIDE_MMA_SYNC);
 }
 
 int rgr_guide_create(rgr_guide** out, int32_t device, const rgr_guide_config* cfg) {
@@ -202,10 +227,14 @@ int rgr_guide_create(rgr_guide** out, int32_t device, const rgr_guide_config* cf
     RGR_CUDA(cudaSetDevice(device));
     RGR_CUDA((cudaError_t)guide_kernel_attributes());
     RGR_CUDA((cudaError_t)guide_tc_attributes());
+    RGR_CUDA((cudaError_t)guide_train_tc_attributes());
     rgr_guide* g = new (std::nothrow) rgr_guide();
     if (!g) return RGR_E_OOM;
     g->device = device;
-    cudaDeviceGetAttribute(&g->num_sms, cudaDevAttrMultiProcessorCount, device);
+    if (cudaDeviceGetAttribute(&g->num_sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) {
+        delete g;
+        return RGR_E_CUDA;
+    }
     int r = g->init(c);
     if (r != RGR_OK) {
         delete g;
@@ -318,8 +347,7 @@ int rgr_guide_train_device(rgr_guide* g, const float* samples, uint32_t n, float
     cudaStream_t st = (cudaStream_t)stream;
     RGR_CUDA(cudaMemcpyAsync(g->test.count, &n, 4, cudaMemcpyHostToDevice, st));
     RGR_CUDA(cudaMemsetAsync(g->loss.p, 0, 4, st));
-    const int grid = (int)std::min<uint32_t>(std::max<uint32_t>((n + 63) / 64, 1u), (uint32_t)g->num_sms);
-    launch_guide_train(g->view, samples, g->test.count, n, 0u, nullptr, weight_scale, grid, st);
+    g->gradient_launches(samples, g->test.count, n, 0u, nullptr, weight_scale, train_grid(*g, n), st);
     RGR_CUDA(cudaGetLastError());
     if (grads) {
         RGR_CUDA(cudaMemcpyAsync(grads, g->gW.p, 4 * kGuideWeights, cudaMemcpyDeviceToDevice, st));
@@ -339,6 +367,23 @@ int rgr_guide_train_device(rgr_guide* g, const float* samples, uint32_t n, float
     }
     RGR_CUDA(cudaStreamSynchronize(st));
     if (loss) *loss = hl;
+    return RGR_OK;
+}
+
+int rgr_guide_train_device_async(rgr_guide* g, const float* samples, uint32_t n, float weight_scale, void* stream) {
+    RGR_NVTX_RANGE("rgr_guide_train_device_async");
+    if (!g || (n && !samples) || !std::isfinite(weight_scale)) return RGR_E_INVALID;
+    if (n == 0) return RGR_OK;
+    RGR_CUDA(cudaSetDevice(g->device));
+    cudaStream_t st = (cudaStream_t)stream;
+    // n reaches the test stream's count word by a kernel, in stream order
+    RGR_CUDA(cudaMemsetAsync(g->loss.p, 0, 4, st));
+    launch_guide_set_count(g->test.count, n, st);
+    g->gradient_launches(samples, g->test.count, n, 0u, nullptr, weight_scale, train_grid(*g, n), st);
+    launch_guide_adam(g->view, g->test.count, 0u, g->test.iter, g->cfg.learning_rate, g->cfg.beta1, g->cfg.beta2,
+                      g->cfg.epsilon, st);
+    launch_guide_finish(g->view, g->test, st);
+    RGR_CUDA(cudaGetLastError());
     return RGR_OK;
 }
 

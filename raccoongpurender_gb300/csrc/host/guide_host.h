@@ -13,6 +13,7 @@ struct rgr_guide {
     rgr::DevBuf w, b, wbf, gW, gb, m, v, loss;
     // training stream: samples, counters, loss history
     rgr::DevBuf samples, counters, loss_hist, wtsw;
+    rgr::DevBuf gpart;  // the tcgen05 training kernel's per-CTA gradient slots (num_sms x kGuidePartStride)
     rgr::dev::GuideView view{};
     rgr::dev::GuideTrainD train{};  // the render's stream (counter bytes 0..27)
     rgr::dev::GuideTrainD test{};   // rgr_guide_train_device's (bytes 32..59; shares iter)
@@ -27,4 +28,8 @@ struct rgr_guide {
     // the launches that follow the trace/logic kernel of a guided render on the
     // bounces that end a training interval: train, Adam, reset the stream
     int train_launches(cudaStream_t st);
+    // one iteration's gradient launches (the configured training kernel) over
+    // min(*count, cap) samples, into gW, gb and the loss; `grid` CTAs
+    void gradient_launches(const float* samples, const uint32_t* count, uint32_t cap, uint32_t min_count,
+                           const float* wsum, float weight_scale, int grid, cudaStream_t st);
 };

@@ -5,12 +5,14 @@
 // roof that bounds the traversal is the L2 read bandwidth, not HBM.  This
 // probe measures it: a grid of 256-thread blocks (a multiple of the SM count)
 // streams a buffer of the chosen size with 16-byte loads that bypass L1
-// (ld.global.cg), four loads in flight per thread; the first launch brings
-// the buffer into L2, the timed launches read it from there.  A buffer larger
+// (ld.global.cg), four loads in flight per thread, the buffer read several
+// times per launch (at least 1 GiB); the first launch brings the buffer into
+// L2, the timed launches read it from there.  A buffer larger
 // than L2 measures HBM instead.  Diagnostic entry point: it allocates its own
 // buffer and changes no device setting.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <string>
 
 #include "../rgr_internal.h"
@@ -25,18 +27,23 @@ __device__ __forceinline__ uint4 ld_cg(const uint4* p) {
     return v;
 }
 
-__global__ void __launch_bounds__(256) k_read_probe(const uint4* __restrict__ buf, uint64_t n16, uint32_t* sink) {
+// `passes` reads of the whole buffer per launch, so that launch overhead does not
+// count against a buffer that L2 serves in a few microseconds
+__global__ void __launch_bounds__(256) k_read_probe(const uint4* __restrict__ buf, uint64_t n16, uint32_t passes,
+                                                    uint32_t* sink) {
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-    uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     uint32_t acc = 0;
-    for (; i + 3 * stride < n16; i += 4 * stride) {
-        uint4 a = ld_cg(buf + i), b = ld_cg(buf + i + stride), c = ld_cg(buf + i + 2 * stride),
-              d = ld_cg(buf + i + 3 * stride);
-        acc ^= a.x ^ a.y ^ a.z ^ a.w ^ b.x ^ b.y ^ b.z ^ b.w ^ c.x ^ c.y ^ c.z ^ c.w ^ d.x ^ d.y ^ d.z ^ d.w;
-    }
-    for (; i < n16; i += stride) {
-        uint4 a = ld_cg(buf + i);
-        acc ^= a.x ^ a.y ^ a.z ^ a.w;
+    for (uint32_t p = 0; p < passes; ++p) {
+        uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+        for (; i + 3 * stride < n16; i += 4 * stride) {
+            uint4 a = ld_cg(buf + i), b = ld_cg(buf + i + stride), c = ld_cg(buf + i + 2 * stride),
+                  d = ld_cg(buf + i + 3 * stride);
+            acc ^= a.x ^ a.y ^ a.z ^ a.w ^ b.x ^ b.y ^ b.z ^ b.w ^ c.x ^ c.y ^ c.z ^ c.w ^ d.x ^ d.y ^ d.z ^ d.w;
+        }
+        for (; i < n16; i += stride) {
+            uint4 a = ld_cg(buf + i);
+            acc ^= a.x ^ a.y ^ a.z ^ a.w;
+        }
     }
     if (acc == 0x9e3779b9u) *sink = acc;  // keeps the loads; the buffer is zero, so never taken
 }
@@ -69,11 +76,13 @@ extern "C" int rgr_probe_read_bandwidth(int32_t device, uint64_t bytes, int32_t 
     if (e == cudaSuccess) e = cudaEventCreate(&e1);
     if (e == cudaSuccess) e = cudaMemsetAsync(buf, 0, n16 * 16, st);
     float ms = 0.0f;
+    // at least 1 GiB read per launch
+    const uint32_t passes = (uint32_t)std::max<uint64_t>(1, (1ull << 30) / (n16 * 16));
     if (e == cudaSuccess) {
         const int grid = sms * 8;  // 8 resident 256-thread blocks per SM
-        for (int w = 0; w < 3; ++w) k_read_probe<<<grid, 256, 0, st>>>((const uint4*)buf, n16, sink);
+        for (int w = 0; w < 3; ++w) k_read_probe<<<grid, 256, 0, st>>>((const uint4*)buf, n16, 1u, sink);
         cudaEventRecord(e0, st);
-        for (int r = 0; r < reps; ++r) k_read_probe<<<grid, 256, 0, st>>>((const uint4*)buf, n16, sink);
+        for (int r = 0; r < reps; ++r) k_read_probe<<<grid, 256, 0, st>>>((const uint4*)buf, n16, passes, sink);
         cudaEventRecord(e1, st);
         e = cudaEventSynchronize(e1);
         if (e == cudaSuccess) e = cudaGetLastError();
@@ -89,6 +98,6 @@ extern "C" int rgr_probe_read_bandwidth(int32_t device, uint64_t bytes, int32_t 
         rgr::set_error(std::string("rgr_probe_read_bandwidth: ") + cudaGetErrorString(e));
         return e == cudaErrorMemoryAllocation ? RGR_E_OOM : RGR_E_CUDA;
     }
-    *gbs = (double)(n16 * 16) * reps / (ms * 1e-3) / 1e9;
+    *gbs = (double)(n16 * 16) * passes * reps / (ms * 1e-3) / 1e9;
     return RGR_OK;
 }

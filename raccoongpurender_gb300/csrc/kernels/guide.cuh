@@ -26,9 +26,18 @@ constexpr int kGuideBiases = kGuideLayers * kGuideWidth;
 constexpr int kGuideParams = kGuideWeights + kGuideBiases;
 constexpr int kGuideInputs = 36;   // 9 coordinates x 2 octaves x (sin, cos)
 constexpr int kGuideOutputs = 40;  // field-major: output 8 f + i is field f (mean xyz, concentration, weight) of lobe i
+constexpr int kGuideSelOutput = 40;  // the logit z of the guide's share of the non-envmap sampling probability
+constexpr int kGuideNetOutputs = 41; // the mixture's outputs and the selection logit
+constexpr int kGuideRowOutputs = 48; // raw outputs per row written by the inference entry point (41 and 7 zeros)
+// the guide's share a = kGuideAlphaMin + (kGuideAlphaMax - kGuideAlphaMin) sigmoid(z): the
+// BSDF always keeps at least 5 % of the non-envmap probability, and the guide as much
+constexpr float kGuideAlphaMin = 0.05f, kGuideAlphaMax = 0.95f;
 constexpr float kGuideKappaMax = 5000.0f;
 constexpr float kGuideLogitBound = 5.0f;    // lobe weight logits lie in (-5, 5)
 constexpr float kGuideNormPenalty = 0.01f;  // pull of each direction output's length toward 1
+// one CTA's slot in the tcgen05 training kernel's partials buffer: its weight
+// gradient, bias gradient and loss (kGuideParams + 1 floats), padded to 128 bytes
+constexpr uint32_t kGuidePartStride = kGuideParams + 32;
 
 // position normalisation of the input encoding (scene bounds)
 struct GuideParams {
@@ -95,12 +104,60 @@ __host__ __device__ __forceinline__ bool wt_is_bias_slot(uint32_t l, uint32_t in
 __device__ __forceinline__ float vmf_pdf(float kappa, float c) {
     return kappa / (6.283185307179586f * -expm1f(-2.0f * kappa)) * expf(kappa * (c - 1.0f));
 }
+__device__ __forceinline__ float softplus(float x) { return x > 20.0f ? x : log1pf(expf(x)); }
+__device__ __forceinline__ float sigmoid(float x) { return 1.0f / (1.0f + expf(-x)); }
+
+// One lobe of the mixture from its five raw outputs (the training kernels):
+//   mean = o / |o|, kappa = min(softplus(o_3) + 0.01, kGuideKappaMax),
+//   logit = kGuideLogitBound tanh(o_4 / kGuideLogitBound)
+// (bounded so that no lobe's weight can saturate to zero and stop learning).
+struct LobeOut {
+    float mx, my, mz, kappa, norm, th, logit;
+};
+__device__ __forceinline__ LobeOut lobe_of(float o0, float o1, float o2, float o3, float o4) {
+    LobeOut L;
+    L.norm = fmaxf(sqrtf(o0 * o0 + o1 * o1 + o2 * o2), 1.0e-12f);
+    L.mx = o0 / L.norm;
+    L.my = o1 / L.norm;
+    L.mz = o2 / L.norm;
+    L.kappa = fminf(softplus(o3) + 0.01f, kGuideKappaMax);
+    L.th = tanhf(o4 * (1.0f / kGuideLogitBound));
+    L.logit = kGuideLogitBound * L.th;
+    return L;
+}
+// The gradient, with respect to the raw outputs of one lobe (g[0..4] = mean xyz,
+// concentration, weight logit), of -wt log q(d) + wt kGuideNormPenalty (|o| - 1)^2,
+// given the lobe L, its mixture weight pi and its responsibility r = pi f / q
+// for the sample direction d; raw_k is the lobe's raw concentration output.  The
+// second term holds the length of each direction output near 1 (the direction
+// o / |o| does not depend on it, and the first term's gradient shrinks as 1 / |o|).
+__device__ __forceinline__ void lobe_grad(const LobeOut& L, float pi, float r, float raw_k, float dx, float dy,
+                                          float dz, float wt, float* g) {
+    // weight logit: d(-log q)/d l = -(r - pi), through l = B tanh(o / B)
+    g[4] = -wt * (r - pi) * (1.0f - L.th * L.th);
+    // concentration: d log f / d kappa = 1/kappa - 2 e^{-2k} / (1 - e^{-2k}) + (mu.d - 1)
+    const float k = L.kappa;
+    const float md = L.mx * dx + L.my * dy + L.mz * dz;
+    const float dlogf = 1.0f / k - 2.0f * expf(-2.0f * k) / -expm1f(-2.0f * k) + (md - 1.0f);
+    const float dk = (softplus(raw_k) + 0.01f < kGuideKappaMax) ? sigmoid(raw_k) : 0.0f;
+    g[3] = -wt * r * dlogf * dk;
+    // mean: d log f / d mu = kappa d, through mu = o / |o|: (I - mu mu^T) / |o|;
+    // plus the length penalty 2 wt c (|o| - 1) mu
+    const float gx = -wt * r * k * dx, gy = -wt * r * k * dy, gz = -wt * r * k * dz;
+    const float gm = gx * L.mx + gy * L.my + gz * L.mz;
+    const float pen = 2.0f * wt * kGuideNormPenalty * (L.norm - 1.0f);
+    g[0] = (gx - gm * L.mx) / L.norm + pen * L.mx;
+    g[1] = (gy - gm * L.my) / L.norm + pen * L.my;
+    g[2] = (gz - gm * L.mz) / L.norm + pen * L.mz;
+}
 
 // The inferred mixture of one guided vertex as the shading kernel reads it,
 // kGuideMixVecs 16-byte words in global memory (FP16): lobe i's mean xyz and
-// kappa in halves 4i..4i+3, the eight weights in halves 32..39.  Sampling and
-// the pdf decode it the same way (means and weights normalised after the
-// FP16 rounding), so the density evaluated is exactly the one sampled.
+// kappa in halves 4i..4i+3, the eight weights in halves 32..39, scaled so that
+// they sum to the guide's share a of the non-envmap sampling probability at
+// the vertex.  Sampling and the pdf decode it the same way (means and weights
+// normalised after the FP16 rounding, a = the sum of the stored weights), so
+// the density evaluated and the share used are exactly the ones sampled with.
 __device__ __forceinline__ uint32_t half2_bits(float lo, float hi) {
     const __half2 h = __floats2half2_rn(lo, hi);
     return *reinterpret_cast<const uint32_t*>(&h);
@@ -114,6 +171,26 @@ __device__ __forceinline__ float4 mixture_lobe(const uint4* p, int i) {
     const float2 xy = half2_float2(q.x), zk = half2_float2(q.y);
     const float inv = 1.0f / sqrtf(fmaxf(xy.x * xy.x + xy.y * xy.y + zk.x * zk.x, 1.0e-30f));
     return make_float4(xy.x * inv, xy.y * inv, zk.x * inv, zk.y);
+}
+// the guide's share of the non-envmap probability at the vertex: the sum of the stored weights
+__device__ __forceinline__ float mixture_alpha(const uint4* p) {
+    const uint4 q = __ldg(p + 4);
+    const float2 a = half2_float2(q.x), b = half2_float2(q.y), c = half2_float2(q.z), d = half2_float2(q.w);
+    return ((a.x + a.y) + (b.x + b.y)) + ((c.x + c.y) + (d.x + d.y));
+}
+__device__ __forceinline__ float alpha_of(float z) {
+    return kGuideAlphaMin + (kGuideAlphaMax - kGuideAlphaMin) / (1.0f + __expf(-z));
+}
+// The gradient, with respect to the selection logit z, of the selection term
+// -wt log(a q + (1 - a) pb), a = alpha_of(z), with the mixture density q held
+// fixed; zero for a sample without a BSDF pdf (pb = 0).  Accurate functions:
+// the training kernels use it.
+__device__ __forceinline__ float selection_grad(float z, float q, float pb, float wt) {
+    if (!(pb > 0.0f)) return 0.0f;
+    const float sg = 1.0f / (1.0f + expf(-z));
+    const float a = kGuideAlphaMin + (kGuideAlphaMax - kGuideAlphaMin) * sg;
+    const float mix = fmaxf(a * q + (1.0f - a) * pb, 1.0e-30f);
+    return -wt * (q - pb) / mix * (kGuideAlphaMax - kGuideAlphaMin) * sg * (1.0f - sg);
 }
 // the eight weights of the record, normalised
 __device__ __forceinline__ void mixture_weights(const uint4* p, float* w) {
@@ -179,7 +256,8 @@ size_t guide_train_smem();
 int guide_kernel_attributes();
 // persistent grid of the inference kernels (resident CTAs)
 int guide_infer_grid(int num_sms);
-// raw network outputs (40 floats per row) of rows of 16 floats (x, n, wo in the first 9)
+// raw network outputs (kGuideRowOutputs floats per row: the 40 mixture outputs, the
+// selection logit, zeros) of rows of 16 floats (x, n, wo in the first 9)
 void launch_guide_infer(const GuideView& g, const float* rows, uint32_t n, float* out, int grid, cudaStream_t st);
 // mixtures of this bounce's guided queue items (Lambertian, Ward, in-volume when enabled)
 void launch_guide_infer_paths(const GuideView& g, const PathsView& p, const QueueView& q, const GuideRenderD& gd,
@@ -191,8 +269,22 @@ void launch_guide_train(const GuideView& g, const float* samples, const uint32_t
 // Adam on the accumulated gradients when *count > 0 and >= min_count; iteration number from *iter + 1
 void launch_guide_adam(const GuideView& g, const uint32_t* count, uint32_t min_count, const uint32_t* iter,
                        float lr, float beta1, float beta2, float eps, cudaStream_t st);
+// *count = n, in stream order (the sample count of an iteration enqueued from the host)
+void launch_guide_set_count(uint32_t* count, uint32_t n, cudaStream_t st);
 // after an iteration: advance *iter, log the loss, retune the acceptance, reset counters
 void launch_guide_finish(const GuideView& g, const GuideTrainD& t, cudaStream_t st);
+
+// tcgen05 / TMEM training (guide_train_tc.cu): one iteration over min(*count, cap)
+// samples into the CTAs' slots of `part` (grid x kGuidePartStride floats), nothing
+// while fewer than min_count samples are in; then launch_guide_grad_reduce sums
+// the grid's slots into gW, gb and the loss.  A timed-out wait sets bit 1 of *err.
+size_t guide_train_tc_smem();
+int guide_train_tc_attributes();  // cudaError_t of opting the kernel into its shared memory
+void launch_guide_train_tc(const GuideView& g, const float* samples, const uint32_t* count, uint32_t cap,
+                           uint32_t min_count, const float* wsum, float weight_scale, int grid, float* part,
+                           uint32_t* err, cudaStream_t st);
+void launch_guide_grad_reduce(const GuideView& g, const float* part, uint32_t nparts, const uint32_t* count,
+                              uint32_t min_count, cudaStream_t st);
 
 // tcgen05 / TMEM inference (guide_tc.cu): same results as the mma.sync kernels up
 // to FP32 accumulation order; a timed-out tensor-core wait sets bit 0 of *err

@@ -45,7 +45,8 @@ constexpr int kStride = 72;      // shared-memory row stride of bf16 tiles (elem
 constexpr int kTrainWarps = 4;   // warps per training CTA
 constexpr int kRows = 16 * kTrainWarps;
 constexpr int kInferWarps = 8;   // warps per inference CTA
-constexpr int kOutTiles = 5;     // n tiles (of 8) holding the 40 outputs
+constexpr int kOutTiles = 5;     // n tiles (of 8) holding the mixture's 40 outputs
+constexpr int kNetTiles = 6;     // and the selection logit (output 40, tile 5)
 
 __device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
     __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
@@ -172,7 +173,7 @@ __device__ __forceinline__ void activate(uint32_t a[4][4], float acc[8][4], cons
 // field f of lobe 2q + s of row g + 8h (bias added).  With keep != nullptr the
 // inputs of layers 1..4 are also stored there (training).
 __device__ __forceinline__ void forward_frag(uint32_t a[4][4], const __nv_bfloat16 (*W)[kH][kStride],
-                                             const float (*b)[kH], int lane, float o[kOutTiles][2][2],
+                                             const float (*b)[kH], int lane, float o[kNetTiles][2][2],
                                              __nv_bfloat16 (*keep)[kRows][kStride]) {
     float acc[8][4];
     for (int l = 0; l + 1 < kLayers; ++l) {
@@ -182,7 +183,7 @@ __device__ __forceinline__ void forward_frag(uint32_t a[4][4], const __nv_bfloat
     }
     layer_fwd<3>(acc, a, W[kLayers - 1], lane);
     const int q = lane & 3;
-    for (int f = 0; f < kOutTiles; ++f) {
+    for (int f = 0; f < kNetTiles; ++f) {
         const float b0 = b[kLayers - 1][8 * f + 2 * q], b1 = b[kLayers - 1][8 * f + 2 * q + 1];
         o[f][0][0] = acc[f][0] + b0;
         o[f][0][1] = acc[f][1] + b1;
@@ -192,8 +193,6 @@ __device__ __forceinline__ void forward_frag(uint32_t a[4][4], const __nv_bfloat
 }
 
 // ---------------------------------------------------------------- vMF mixture
-__device__ __forceinline__ float softplus(float x) { return x > 20.0f ? x : log1pf(expf(x)); }
-__device__ __forceinline__ float sigmoid(float x) { return 1.0f / (1.0f + expf(-x)); }
 __device__ __forceinline__ float quad_max(float x) {
     x = fmaxf(x, __shfl_xor_sync(0xffffffffu, x, 1));
     return fmaxf(x, __shfl_xor_sync(0xffffffffu, x, 2));
@@ -203,28 +202,10 @@ __device__ __forceinline__ float quad_sum(float x) {
     return x + __shfl_xor_sync(0xffffffffu, x, 2);
 }
 
-// One lobe of the mixture from its five raw outputs:
-//   mean = o / |o|, kappa = min(softplus(o_3) + 0.01, kGuideKappaMax),
-//   logit = kGuideLogitBound tanh(o_4 / kGuideLogitBound)
-// (bounded so that no lobe's weight can saturate to zero and stop learning).
-struct LobeOut {
-    float mx, my, mz, kappa, norm, th, logit;
-};
-__device__ __forceinline__ LobeOut lobe_of(float o0, float o1, float o2, float o3, float o4) {
-    LobeOut L;
-    L.norm = fmaxf(sqrtf(o0 * o0 + o1 * o1 + o2 * o2), 1.0e-12f);
-    L.mx = o0 / L.norm;
-    L.my = o1 / L.norm;
-    L.mz = o2 / L.norm;
-    L.kappa = fminf(softplus(o3) + 0.01f, kGuideKappaMax);
-    L.th = tanhf(o4 * (1.0f / kGuideLogitBound));
-    L.logit = kGuideLogitBound * L.th;
-    return L;
-}
 
 // The mixture of row h of this lane (its lobes 2q, 2q + 1; weights by softmax
 // across the quad).  All 32 lanes must call it.
-__device__ __forceinline__ void mixture_quad(const float o[kOutTiles][2][2], int h, LobeOut L[2], float w[2]) {
+__device__ __forceinline__ void mixture_quad(const float o[kNetTiles][2][2], int h, LobeOut L[2], float w[2]) {
     for (int s = 0; s < 2; ++s) L[s] = lobe_of(o[0][h][s], o[1][h][s], o[2][h][s], o[3][h][s], o[4][h][s]);
     const float mx = quad_max(fmaxf(L[0].logit, L[1].logit));
     w[0] = expf(L[0].logit - mx);
@@ -239,9 +220,12 @@ __device__ __forceinline__ void mixture_quad(const float o[kOutTiles][2][2], int
 // -wt log q(d) + wt kGuideNormPenalty sum_i (|o_i| - 1)^2; the second term
 // holds the length of each lobe's direction output near 1 (the direction
 // o / |o| does not depend on it, and the gradient of the first term shrinks
-// as 1 / |o|).  All 32 lanes must call it.
-__device__ __forceinline__ float loss_grad_quad(const float o[kOutTiles][2][2], int h, float dx, float dy, float dz,
-                                                float wt, float g[kOutTiles][2]) {
+// as 1 / |o|).  Tile 5 (lane q = 0, column 0: output 40) gets the gradient of
+// the selection term -wt log(a q + (1 - a) pb) with respect to the selection
+// logit, q held fixed (pb = the sample's BSDF pdf; none when 0).  All 32 lanes
+// must call it.
+__device__ __forceinline__ float loss_grad_quad(const float o[kNetTiles][2][2], int h, float dx, float dy, float dz,
+                                                float wt, float pb, float g[kNetTiles][2]) {
     LobeOut L[2];
     float pi[2];
     mixture_quad(o, h, L, pi);
@@ -250,24 +234,13 @@ __device__ __forceinline__ float loss_grad_quad(const float o[kOutTiles][2][2], 
     const float q = fmaxf(quad_sum(pi[0] * f[0] + pi[1] * f[1]), 1.0e-30f);
     for (int s = 0; s < 2; ++s) {
         const float r = pi[s] * f[s] / q;  // responsibility of the lobe
-        // weight logit: d(-log q)/d l = -(r - pi), through l = B tanh(o / B)
-        g[4][s] = -wt * (r - pi[s]) * (1.0f - L[s].th * L[s].th);
-        // concentration: d log f / d kappa = 1/kappa - 2 e^{-2k} / (1 - e^{-2k}) + (mu.d - 1)
-        const float k = L[s].kappa;
-        const float md = L[s].mx * dx + L[s].my * dy + L[s].mz * dz;
-        const float dlogf = 1.0f / k - 2.0f * expf(-2.0f * k) / -expm1f(-2.0f * k) + (md - 1.0f);
-        const float raw_k = o[3][h][s];
-        const float dk = (softplus(raw_k) + 0.01f < kGuideKappaMax) ? sigmoid(raw_k) : 0.0f;
-        g[3][s] = -wt * r * dlogf * dk;
-        // mean: d log f / d mu = kappa d, through mu = o / |o|: (I - mu mu^T) / |o|;
-        // plus the length penalty 2 wt c (|o| - 1) mu
-        const float gx = -wt * r * k * dx, gy = -wt * r * k * dy, gz = -wt * r * k * dz;
-        const float gm = gx * L[s].mx + gy * L[s].my + gz * L[s].mz;
-        const float pen = 2.0f * wt * kGuideNormPenalty * (L[s].norm - 1.0f);
-        g[0][s] = (gx - gm * L[s].mx) / L[s].norm + pen * L[s].mx;
-        g[1][s] = (gy - gm * L[s].my) / L[s].norm + pen * L[s].my;
-        g[2][s] = (gz - gm * L[s].mz) / L[s].norm + pen * L[s].mz;
+        float gl[5];
+        lobe_grad(L[s], pi[s], r, o[3][h][s], dx, dy, dz, wt, gl);
+        for (int k = 0; k < 5; ++k) g[k][s] = gl[k];
     }
+    const float z = __shfl_sync(0xffffffffu, o[5][h][0], (threadIdx.x & 31u) & ~3u);  // output 40, held by q = 0
+    g[5][0] = ((threadIdx.x & 3u) == 0u) ? selection_grad(z, q, pb, wt) : 0.0f;
+    g[5][1] = 0.0f;
     return -wt * logf(q);
 }
 
@@ -277,7 +250,7 @@ struct SmemFwd {
     float b[kLayers][kH];
 };
 
-// rows: 16 floats each (x, n, wo in the first 9); out: 40 raw floats per row
+// rows: 16 floats each (x, n, wo in the first 9); out: kGuideRowOutputs raw floats per row
 __global__ void __launch_bounds__(32 * kInferWarps, 4) k_guide_infer(GuideView gv, const float* __restrict__ rows,
                                                                       uint32_t n, float* __restrict__ out) {
     __shared__ SmemFwd S;
@@ -295,13 +268,13 @@ __global__ void __launch_bounds__(32 * kInferWarps, 4) k_guide_infer(GuideView g
         }
         uint32_t a[4][4];
         encode_frag(v[0], v[1], q, a);
-        float o[kOutTiles][2][2];
+        float o[kNetTiles][2][2];
         forward_frag(a, S.W, S.b, lane, o, nullptr);
         for (int h = 0; h < 2; ++h) {
             const uint32_t r = base + g + 8 * h;
             if (r >= n) continue;
-            for (int f = 0; f < kOutTiles; ++f)
-                *reinterpret_cast<float2*>(out + kGuideOutputs * (size_t)r + 8 * f + 2 * q) =
+            for (int f = 0; f < kNetTiles; ++f)
+                *reinterpret_cast<float2*>(out + kGuideRowOutputs * (size_t)r + 8 * f + 2 * q) =
                     make_float2(o[f][h][0], o[f][h][1]);
         }
     }
@@ -349,12 +322,17 @@ __global__ void __launch_bounds__(32 * kInferWarps, 4) k_guide_infer_paths(Guide
         }
         uint32_t a[4][4];
         encode_frag(v[0], v[1], q, a);
-        float o[kOutTiles][2][2];
+        float o[kNetTiles][2][2];
         forward_frag(a, S.W, S.b, lane, o, nullptr);
         for (int h = 0; h < 2; ++h) {
             LobeOut L[2];
             float w[2];
             mixture_quad(o, h, L, w);
+            // the weights carry the guide's share of the vertex (their sum)
+            const float z = __shfl_sync(0xffffffffu, o[5][h][0], lane & ~3);
+            const float alpha = gd.learn_frac ? alpha_of(z) : gd.guide_frac;
+            w[0] *= alpha;
+            w[1] *= alpha;
             const uint32_t r = base + g + 8 * h;
             if (r >= n) continue;
             uint4* dst = gd.lobes + (size_t)kGuideMixVecs * r;  // FP16 record (guide.cuh)
@@ -416,12 +394,13 @@ __global__ void __launch_bounds__(32 * kTrainWarps) k_guide_train(GuideView gv, 
     const int r0 = 16 * warp;  // this warp's rows within the chunk
     for (uint32_t chunk = blockIdx.x * (uint32_t)kRows; chunk < n; chunk += gridDim.x * (uint32_t)kRows) {
         // ---- forward, keeping each layer's input
-        float v[2][9], dir[2][3], wt[2];
+        float v[2][9], dir[2][3], wt[2], pb[2];
         for (int h = 0; h < 2; ++h) {
             const uint32_t r = chunk + r0 + gq + 8 * h;
             float x9[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
             dir[h][0] = dir[h][1] = dir[h][2] = 0.0f;
             wt[h] = 0.0f;
+            pb[h] = 0.0f;
             if (r < n) {
                 const float* s = samples + 16 * (size_t)r;
                 for (int c = 0; c < 9; ++c) x9[c] = s[c];
@@ -429,30 +408,31 @@ __global__ void __launch_bounds__(32 * kTrainWarps) k_guide_train(GuideView gv, 
                 dir[h][1] = s[10];
                 dir[h][2] = s[11];
                 wt[h] = s[12] * scale;
+                pb[h] = s[13];
             }
             coords(x9, gv.params, v[h]);
         }
         uint32_t a[4][4];
         encode_frag(v[0], v[1], q, a);
         store_a(&S.act[0][r0], a, lane);
-        float o[kOutTiles][2][2];
+        float o[kNetTiles][2][2];
         forward_frag(a, S.W, S.b, lane, o, reinterpret_cast<__nv_bfloat16(*)[kRows][kStride]>(&S.act[0][r0]));
         // ---- loss gradient at the output, in the fragment layout
         float lossv = 0.0f;
-        uint32_t gp[2][kOutTiles];  // the output gradient, packed bf16, per row half
+        uint32_t gp[2][kNetTiles];  // the output gradient, packed bf16, per row half
         for (int h = 0; h < 2; ++h) {
-            float gr[kOutTiles][2];
-            const float lh = loss_grad_quad(o, h, dir[h][0], dir[h][1], dir[h][2], wt[h], gr);
+            float gr[kNetTiles][2];
+            const float lh = loss_grad_quad(o, h, dir[h][0], dir[h][1], dir[h][2], wt[h], pb[h], gr);
             const bool live = wt[h] > 0.0f;
             if (live && q == 0) lossv += lh;
-            for (int f = 0; f < kOutTiles; ++f) {
+            for (int f = 0; f < kNetTiles; ++f) {
                 gp[h][f] = live ? pack_bf16(gr[f][0], gr[f][1]) : 0u;
                 *reinterpret_cast<uint32_t*>(&S.dy[r0 + gq + 8 * h][8 * f + 2 * q]) = gp[h][f];
             }
-            for (int f = kOutTiles; f < 8; ++f)
+            for (int f = kNetTiles; f < 8; ++f)
                 *reinterpret_cast<uint32_t*>(&S.dy[r0 + gq + 8 * h][8 * f + 2 * q]) = 0u;
         }
-        for (int f = 0; f < kOutTiles; ++f) add_colsums(S.gb[warp][kLayers - 1], 8 * f + 2 * q, gp[0][f], gp[1][f], lane);
+        for (int f = 0; f < kNetTiles; ++f) add_colsums(S.gb[warp][kLayers - 1], 8 * f + 2 * q, gp[0][f], gp[1][f], lane);
         for (int off = 16; off > 0; off >>= 1) lossv += __shfl_xor_sync(0xffffffffu, lossv, off);
         if (lane == 0) S.loss[warp] += lossv;
         __syncthreads();
@@ -592,9 +572,13 @@ __global__ void k_guide_finish(GuideView g, GuideTrainD t) {
     *g.loss = 0.0f;
 }
 
+__global__ void k_guide_set_count(uint32_t* count, uint32_t n) { *count = n; }
+
 }  // namespace
 
 size_t guide_infer_smem() { return sizeof(SmemFwd); }
+
+void launch_guide_set_count(uint32_t* count, uint32_t n, cudaStream_t st) { k_guide_set_count<<<1, 1, 0, st>>>(count, n); }
 size_t guide_train_smem() { return sizeof(SmemTrain); }
 
 int guide_kernel_attributes() {

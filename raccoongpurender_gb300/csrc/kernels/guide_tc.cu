@@ -26,7 +26,7 @@
 // tiles (other groups, or the group's other buffers) run their epilogues.  After the last layer each thread has its row's 40
 // outputs in registers and computes the mixture (or keeps the raw outputs)
 // without any exchange; the tile's results (80-byte FP16 mixture records, or
-// 160 bytes of raw outputs) are staged in shared memory and leave in one bulk
+// 192 bytes of raw outputs) are staged in shared memory and leave in one bulk
 // copy.  Weights and bias chunks are staged once
 // per CTA by one bulk copy.  Every wait is bounded: on a timeout the CTA
 // records an error, stops issuing and frees its TMEM.
@@ -77,7 +77,7 @@ constexpr uint32_t kErrTimeout = 1u;
 
 struct __align__(1024) SmemTc {
     unsigned char wt[kGuideWtBytes];                // the staged weights and bias chunks (50 x 1024 B)
-    unsigned char out[kTcGroups][128 * 160];        // a tile's output rows (80 or 160 bytes), stored by one bulk copy
+    unsigned char out[kTcGroups][128 * 4 * kGuideRowOutputs];  // a tile's output rows (80 or 192 bytes), one bulk copy
     unsigned long long wbar;                        // the weights' bulk copy
     unsigned long long a_full[kTcGroups][kBufs];    // the A tile of the next layer is written (128 arrivals)
     unsigned long long d_full[kTcGroups][kBufs];    // the layer's MMAs are done (one commit)
@@ -212,6 +212,9 @@ __device__ __forceinline__ void tmem_ld8(uint32_t taddr, uint32_t* r) {
                  : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
                  : "r"(taddr));
 }
+__device__ __forceinline__ void tmem_ld1(uint32_t taddr, uint32_t* r) {
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x1.b32 {%0}, [%1];\n" : "=r"(r[0]) : "r"(taddr));
+}
 __device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory"); }
 // 32 columns of this thread's TMEM lane from registers
 __device__ __forceinline__ void tmem_st32(uint32_t taddr, const uint32_t* r) {
@@ -288,8 +291,9 @@ __device__ __forceinline__ float softplus_fast(float x) { return x > 20.0f ? x :
 // The mixture of one row's 40 raw outputs (field-major) as the FP16 record
 // the shading kernel reads (guide.cuh), the functions of guide_mlp.cu's
 // lobe_of in hardware approximations: the mixture only has to be the one the
-// shading kernel samples and evaluates, which decodes it from here.
-__device__ __forceinline__ void row_mixture(const float* o, uint4* dst) {
+// shading kernel samples and evaluates, which decodes it from here.  The
+// weights are stored scaled by the guide's share `alpha` of the vertex.
+__device__ __forceinline__ void row_mixture(const float* o, float alpha, uint4* dst) {
     float w[kGuideLobes], mx = -3.0e38f;
 #pragma unroll
     for (int i = 0; i < kGuideLobes; ++i) {
@@ -307,7 +311,7 @@ __device__ __forceinline__ void row_mixture(const float* o, uint4* dst) {
         w[i] = __expf(w[i] - mx);
         den += w[i];
     }
-    const float r = 1.0f / den;
+    const float r = alpha / den;
 #pragma unroll
     for (int i = 0; i < 4; ++i) dst[i] = make_uint4(lobe[2 * i].x, lobe[2 * i].y, lobe[2 * i + 1].x, lobe[2 * i + 1].y);
     dst[4] = make_uint4(half2_bits(w[0] * r, w[1] * r), half2_bits(w[2] * r, w[3] * r), half2_bits(w[4] * r, w[5] * r),
@@ -539,9 +543,14 @@ __global__ void __launch_bounds__(kTcThreads, 1)
                         mbar_arrive(smem_u32(&S.a_full[g][j]));
                         continue;
                     }
-                    uint32_t o[40];
+                    uint32_t o[kGuideRowOutputs];
                     tmem_ld32(tm, o);
                     tmem_ld8(tm + 32u, o + 32);
+                    if (kPaths) {
+                        tmem_ld1(tm + 40u, o + 40);  // the selection logit only
+                    } else {
+                        tmem_ld8(tm + 40u, o + 40);
+                    }
                     tmem_wait_ld();
                     fence_before();
                     // the staging rows are free once the previous bulk copy has read them
@@ -550,22 +559,24 @@ __global__ void __launch_bounds__(kTcThreads, 1)
                         timed_out = true;
                         break;
                     }
-                    // the row's result (the 80-byte FP16 mixture record, or the 160
+                    // the row's result (the 80-byte FP16 mixture record, or the 192
                     // bytes of raw outputs), then the tile's rows to global memory
                     // in one bulk copy
-                    constexpr uint32_t kRowBytes = kPaths ? 16u * kGuideMixVecs : 4u * kGuideOutputs;
+                    constexpr uint32_t kRowBytes = kPaths ? 16u * kGuideMixVecs : 4u * kGuideRowOutputs;
                     unsigned char* row_out = S.out[g] + kRowBytes * lt;
                     if (r < n) {
-                        float of[40];
-#pragma unroll
-                        for (int q = 0; q < 40; ++q) of[q] = __uint_as_float(o[q]);
                         if (kPaths) {
-                            row_mixture(of, reinterpret_cast<uint4*>(row_out));
+                            float of[kGuideOutputs];
+#pragma unroll
+                            for (int q = 0; q < kGuideOutputs; ++q) of[q] = __uint_as_float(o[q]);
+                            const float alpha =
+                                gd.learn_frac ? alpha_of(__uint_as_float(o[kGuideSelOutput])) : gd.guide_frac;
+                            row_mixture(of, alpha, reinterpret_cast<uint4*>(row_out));
                         } else {
 #pragma unroll
-                            for (int q = 0; q < kGuideOutputs / 4; ++q)
-                                reinterpret_cast<float4*>(row_out)[q] =
-                                    make_float4(of[4 * q], of[4 * q + 1], of[4 * q + 2], of[4 * q + 3]);
+                            for (int q = 0; q < kGuideRowOutputs / 4; ++q)
+                                reinterpret_cast<uint4*>(row_out)[q] = make_uint4(o[4 * q], o[4 * q + 1], o[4 * q + 2],
+                                                                                  o[4 * q + 3]);
                         }
                     }
                     fence_async_smem();

@@ -224,15 +224,29 @@ template <bool kGuided>
 RGR_DEV void shade_slot(const RequestD& rq, const PathsView& P, int k, uint32_t slot, unsigned long long gpix,
                         const GuideRenderD& gd, uint32_t gi) {
     const SceneView& sc = rq.sc;
-    float4 ro4 = P.ro[slot], rd4 = P.rd[slot], T4 = P.T[slot], L4 = P.L[slot], ng4 = P.ng[slot];
-    int4 va = P.vols[2 * (size_t)slot], vb = P.vols[2 * (size_t)slot + 1];
+    // Path state is loaded only where this item uses it: a material queue is a
+    // sparse subset of the slots, so every 16-byte vector costs a DRAM sector of
+    // its own.  A new path (k = 0) replaces everything but its RNG state and the
+    // volume hit of the ended path; L is loaded (and stored) only when the stage
+    // changes it; the first half of the volume list only when the list is used.
+    const bool fresh = k == 0;
+    const float4 rd4 = P.rd[slot];
+    float4 ro4 = make_float4(0.0f, 0.0f, 0.0f, 0.0f), T4 = ro4, ng4 = ro4;
+    int4 va = make_int4(0, 0, 0, 0), vb = va;
+    if (!fresh) {
+        ro4 = P.ro[slot];
+        T4 = P.T[slot];
+        ng4 = P.ng[slot];
+        vb = P.vols[2 * (size_t)slot + 1];
+        if (k == kMatVolume || vb.w > 0) va = P.vols[2 * (size_t)slot];
+    }
     Rng rng = rng_load(P.rng, slot);
-    f3 ro = xyz(ro4), rd = xyz(rd4), T = xyz(T4), L = xyz(L4), Ng = xyz(ng4);
+    f3 ro = xyz(ro4), rd = xyz(rd4), T = xyz(T4), L = mk(0, 0, 0), Ng = xyz(ng4);
     float tmin = ro4.w;
     int32_t hv = __float_as_int(rd4.w);
     int32_t hs = __float_as_int(ng4.w);
     uint32_t pixel = __float_as_uint(T4.w);
-    uint32_t logic_i = __float_as_uint(L4.w);
+    uint32_t logic_i = 0;
     int vcount = vb.w;
 
     if (k == 0) {  // new_path (new_path.cl:17-83)
@@ -291,8 +305,11 @@ RGR_DEV void shade_slot(const RequestD& rq, const PathsView& P, int k, uint32_t 
             is.sel0 = bxdf_p;
             is.sel1 = 1.0f - bxdf_p;
         }
-        if (kGuided && gi != ~0u) {  // the guide takes its share of the non-envmap probability
-            is.sel2 = is.sel0 * gd.guide_frac;
+        if (kGuided && gi != ~0u) {
+            // the guide takes its share of the non-envmap probability: the sum of the
+            // record's stored weights (the network's selection output, or the fixed
+            // fraction), decoded identically wherever the record is read
+            is.sel2 = is.sel0 * mixture_alpha(gd.lobes + (size_t)kGuideMixVecs * gi);
             is.sel0 = is.sel0 - is.sel2;
         }
         float u = rng.uniform();
@@ -515,7 +532,17 @@ RGR_DEV void shade_slot(const RequestD& rq, const PathsView& P, int k, uint32_t 
         ro = ro + rd * tmin + wi * 1.0e-5f;
         rd = wi;
     }
-    // logic.cl:31-33, applied here: the stage that made the shading result consumes it
+    // logic.cl:31-33, applied here: the stage that made the shading result consumes it.
+    // L + T * shLe leaves L's bits unchanged when shLe is zero and T finite (L is
+    // never -0), so L is read and written only otherwise, for new paths and in
+    // guided renders (the training records carry it).
+    const bool touch_L = fresh || kGuided || shLe.x != 0.0f || shLe.y != 0.0f || shLe.z != 0.0f ||
+                         !is_finite(T.x) || !is_finite(T.y) || !is_finite(T.z);
+    if (touch_L && !fresh) {
+        const float4 L4 = P.L[slot];
+        L = xyz(L4);
+        logic_i = __float_as_uint(L4.w);
+    }
     L = L + T * shLe;
     T = T * shT;
     if (kGuided && is.sel2 != 0.0f && gd.record && guide_training_open(gd.train)) {
@@ -531,7 +558,7 @@ RGR_DEV void shade_slot(const RequestD& rq, const PathsView& P, int k, uint32_t 
             rec[1] = make_float4(gn.y, gn.z, wo_in.x, wo_in.y);
             rec[2] = make_float4(wo_in.z, is.wi.x, is.wi.y, is.wi.z);
             rec[3] = make_float4(L.x, L.y, L.z, T.x);
-            rec[4] = make_float4(T.y, T.z, cp, 0.0f);
+            rec[4] = make_float4(T.y, T.z, cp, is.pdf0);  // pdf0: the BSDF (phase) pdf of wi
             gd.nrec[slot] = (uint8_t)(r + 1);
         }
     }
@@ -555,12 +582,14 @@ RGR_DEV void shade_slot(const RequestD& rq, const PathsView& P, int k, uint32_t 
     P.ro[slot] = f4(ro, tmin);
     P.rd[slot] = f4(rd, __int_as_float(hv));
     P.T[slot] = f4(T, __uint_as_float(pixel));
-    P.L[slot] = f4(L, __uint_as_float(logic_i));
+    if (touch_L) P.L[slot] = f4(L, __uint_as_float(logic_i));
     P.ng[slot] = f4(Ng, __int_as_float(hs));
-    if (k == 0 || k == kMatVolume) {
+    if (k == kMatVolume) {
         vb.w = vcount;
         P.vols[2 * (size_t)slot] = va;
         P.vols[2 * (size_t)slot + 1] = vb;
+    } else if (fresh) {
+        reinterpret_cast<int*>(P.vols + 2 * (size_t)slot + 1)[3] = 0;  // an empty list; the stale entries stay
     }
     rng_store(P.rng, slot, rng);
 }
@@ -826,7 +855,7 @@ RGR_DEV void guide_emit_samples(const GuideRenderD& gd, uint32_t slot, f3 L, boo
             dst[0] = rec[0];  // x, n.x
             dst[1] = rec[1];  // n.yz, wo.xy
             dst[2] = rec[2];  // wo.z, wi
-            dst[3] = make_float4(w[r], 0.0f, 0.0f, 0.0f);
+            dst[3] = make_float4(w[r], rec[4].w, 0.0f, 0.0f);  // weight, BSDF pdf of wi
             wsum += w[r];
         }
         ++idx;

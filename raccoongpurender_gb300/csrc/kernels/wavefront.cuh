@@ -132,7 +132,8 @@ struct GuideRenderD {
     float4* records;      // per slot kGuideRecords x 5 float4
     uint8_t* nrec;        // records written on the slot's current path
     GuideTrainD train;
-    float guide_frac;     // share of the non-envmap selection probability given to the guide
+    float guide_frac;     // share of the non-envmap selection probability given to the guide (learn_frac = 0)
+    int32_t learn_frac;   // 1: that share is the network's selection output, per vertex
     int32_t volumes;      // guide in-volume vertices too
     int32_t record;       // record training samples
     uint32_t max_depth;   // guide vertices 1..max_depth of a path only (0: all); then, per bounce:

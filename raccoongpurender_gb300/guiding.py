@@ -55,12 +55,20 @@ def render_mean(rg, scene, cam, spp: int, seed_offset: int, path_count: int = 1 
     return mean_image(acc)
 
 
+def spread(errs) -> dict:
+    """mean, median, min and max of per-seed relMSE values."""
+    e = np.asarray(errs, np.float64)
+    return {"mean": float(e.mean()), "median": float(np.median(e)), "min": float(e.min()), "max": float(e.max())}
+
+
 def equal_time(rg, scene, cam, ref: np.ndarray, spp_plain: int, path_count: int = 1 << 22, seed_offset: int = 1,
-               guide_kw: dict | None = None, repeats: int = 3, warm_spp: int | None = None,
+               guide_kw: dict | None = None, repeats: int = 8, warm_spp: int | None = None,
                longer_warm_spp: tuple = ()) -> dict:
     """Plain rendering at spp_plain against guided rendering given the same
-    wall time, relMSE against `ref` (medians over `repeats` seeds: single
-    sun-caustic samples of radiance ~1e4 dominate individual runs).
+    wall time, relMSE against `ref` over `repeats` seeds (medians, with mean,
+    min and max: single sun-caustic samples of radiance ~1e4 dominate
+    individual runs).  The ratios are plain's relMSE over guided's, of the
+    medians and of the means.
       cold: the guide starts untrained and trains online on the render's own
             samples (`guide_kw`), inference and training inside the time;
       warm: a guide trained online, without an iteration limit, by an earlier
@@ -85,13 +93,14 @@ def equal_time(rg, scene, cam, ref: np.ndarray, spp_plain: int, path_count: int 
     tp = float(np.median(plain_t))
     ep = float(np.median(plain_e))
     # cold: calibrate the cost per spp, then render at the spp that fits
-    same_e, iters = [], []
+    same_e, iters, same_t = [], [], []
     for sd in seeds:
         g = rg.Guide(0, **guide_kw)
         _, acc, tg = render(rg, scene, cam, spp_plain, sd, lane=lane, guide=g)
+        same_t.append(tg)
         same_e.append(relmse(mean_image(acc), ref))
         iters.append(g.stats()["iterations"])
-    spp_cold = max(1, int(spp_plain * tp / tg))
+    spp_cold = max(1, int(spp_plain * tp / float(np.median(same_t))))
     cold_t, cold_e = [], []
     for sd in seeds:
         _, acc, t = render(rg, scene, cam, spp_cold, sd, lane=lane, guide=rg.Guide(0, **guide_kw))
@@ -117,18 +126,21 @@ def equal_time(rg, scene, cam, ref: np.ndarray, spp_plain: int, path_count: int 
         ew = float(np.median(warm_e))
         return {"spp": spp_warm, "time_s": round(float(np.median(warm_t)), 4), "relmse": ew,
                 "trained_by": f"{train_spp} spp render, {warm_iters} iterations",
-                "relmse_runs": [round(e, 6) for e in warm_e],
+                "relmse_runs": [round(e, 6) for e in warm_e], "relmse_spread": spread(warm_e),
                 "relmse_ratio_equal_time": round(ep / ew, 3) if ew > 0 else None,
+                "relmse_ratio_of_means": round(float(np.mean(plain_e) / np.mean(warm_e)), 3),
                 "relmse_same_spp": float(np.median(warm_same))}
 
     ec = float(np.median(cold_e))
     out = {
-        "spp_plain": spp_plain, "time_plain_s": round(tp, 4), "relmse_plain": ep,
-        "relmse_plain_runs": [round(e, 6) for e in plain_e],
+        "seeds": repeats, "spp_plain": spp_plain, "time_plain_s": round(tp, 4), "relmse_plain": ep,
+        "relmse_plain_runs": [round(e, 6) for e in plain_e], "relmse_plain_spread": spread(plain_e),
         "cold": {"spp": spp_cold, "time_s": round(float(np.median(cold_t)), 4), "relmse": ec,
-                 "relmse_runs": [round(e, 6) for e in cold_e],
+                 "relmse_runs": [round(e, 6) for e in cold_e], "relmse_spread": spread(cold_e),
                  "relmse_ratio_equal_time": round(ep / ec, 3) if ec > 0 else None,
-                 "relmse_same_spp": float(np.median(same_e)), "training_iterations": int(np.median(iters))},
+                 "relmse_ratio_of_means": round(float(np.mean(plain_e) / np.mean(cold_e)), 3),
+                 "relmse_same_spp": float(np.median(same_e)), "relmse_same_spp_spread": spread(same_e),
+                 "training_iterations": int(np.median(iters))},
         "warm": warm(warm_spp or 4 * spp_plain),
     }
     for n in longer_warm_spp:

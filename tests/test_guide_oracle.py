@@ -23,24 +23,27 @@ def test_bf16_rounding():
 def test_loss_gradient_finite_differences():
     rng = np.random.default_rng(1)
     n = 16
-    raw = rng.normal(size=(n, go.OUTPUTS))
+    raw = rng.normal(size=(n, go.NET_OUTPUTS))
     raw[:, 3 * go.LOBES:4 * go.LOBES] = rng.uniform(-2.0, 3.0, (n, go.LOBES))  # concentrations
     d = rng.normal(size=(n, 3))
     d /= np.linalg.norm(d, axis=1, keepdims=True)
     w = rng.uniform(0.1, 2.0, n)
-    _, g = go.loss_and_grad(raw, d, w)
+    pb = np.where(np.arange(n) % 4 == 3, 0.0, rng.uniform(0.01, 2.0, n))  # every 4th without a BSDF pdf
+    _, g = go.loss_and_grad(raw, d, w, pb)
+    q0 = go.mixture_pdf(raw, d)  # the selection term's gradient holds the mixture density fixed
 
     def total(r):
-        return go.loss_and_grad(r, d, w)[0] + go.penalty(r, w)
+        return go.loss_and_grad(r, d, w)[0] + go.penalty(r, w) + go.selection_loss(r, d, w, pb, q0)
 
     h = 1e-6
     num = np.zeros_like(raw)
-    for j in range(go.OUTPUTS):
+    for j in range(go.NET_OUTPUTS):
         e = np.zeros_like(raw)
         e[:, j] = h
         num[:, j] = (total(raw + e) - total(raw - e)) / (2 * h)
     err = np.abs(num - g).max() / np.abs(g).max()
     assert err < 1e-6, err
+    assert np.abs(g[:, go.SEL]).max() > 0 and (g[pb == 0, go.SEL] == 0).all()
 
 
 def test_network_gradient_finite_differences():
@@ -50,9 +53,10 @@ def test_network_gradient_finite_differences():
     loss, dW, db = go.gradients(W, b, s, lo, ie, bf16_round=False)
     rng = np.random.default_rng(5)
     h = 1e-6
+    q0 = go.mixture_density(W, b, s, lo, ie)
 
     def L(W2, b2):
-        return go.objective(W2, b2, s, lo, ie)
+        return go.objective(W2, b2, s, lo, ie, q_fixed=q0)
 
     W64, b64 = W.astype(np.float64), b.astype(np.float64)
     checked = 0
@@ -73,6 +77,14 @@ def test_network_gradient_finite_differences():
         num = (L(W64, bp) - L(W64, bm)) / (2 * h)
         assert abs(num - db[l, o]) <= 1e-5 * max(1.0, abs(num)), (l, o, num, db[l, o])
     assert checked == 30
+    # the selection logit (output 40 of the last layer) is trained
+    for i in (0, 7, 33):
+        Wp, Wm = W64.copy(), W64.copy()
+        Wp[4, i, go.SEL] += h
+        Wm[4, i, go.SEL] -= h
+        num = (L(Wp, b64) - L(Wm, b64)) / (2 * h)
+        assert abs(num - dW[4, i, go.SEL]) <= 1e-5 * max(1.0, abs(num))
+    assert dW[4, :, go.SEL].any() and db[4, go.SEL] != 0.0
     # padding receives no gradient
     for l in range(go.LAYERS):
         assert not dW[l, go.FAN_IN[l]:, :].any()

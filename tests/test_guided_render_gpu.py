@@ -101,3 +101,28 @@ def test_depth_limited_guide_is_unbiased(rg):
     g.check()
     assert g.stats()["iterations"] > 20
     assert abs(guided.mean() / plain.mean() - 1.0) < 0.02
+
+
+def test_learned_selection_share(rg):
+    """The guide's share of the non-envmap sampling probability is a network
+    output trained on the guide-BSDF mixture: after training in the room it
+    differs between vertices and stays inside [0.05, 0.95]; with the share
+    fixed instead (learn_fraction = 0) the render is unbiased too."""
+    import torch
+    sm, cam = _scene(rg, "room")
+    g = _pretrained(rg, sm, cam, 300)
+    batch = g.last_batch()
+    assert len(batch) > 1000 and (batch[:, 13] > 0).mean() > 0.5  # samples carry their BSDF pdf
+    rows = torch.from_numpy(np.ascontiguousarray(batch)).cuda()
+    out = torch.zeros((len(batch), rg.Guide.ROW_OUTPUTS), dtype=torch.float32, device="cuda")
+    g.infer_device(rows.data_ptr(), len(batch), out.data_ptr())
+    torch.cuda.synchronize()
+    z = out.cpu().numpy()[:, rg.Guide.SEL].astype(np.float64)
+    alpha = 0.05 + 0.9 / (1.0 + np.exp(-z))
+    print(f"learned share: mean {alpha.mean():.3f} std {alpha.std():.3f} min {alpha.min():.3f} max {alpha.max():.3f}")
+    assert alpha.std() > 0.01 and abs(alpha.mean() - 0.5) > 0.01
+    plain = guiding.render_mean(rg, sm, cam, spp=512, seed_offset=1, path_count=1 << 18)
+    fixed = rg.Guide(0, learn_fraction=0, guide_fraction=0.5)
+    guided = guiding.render_mean(rg, sm, cam, spp=512, seed_offset=1, path_count=1 << 18, guide=fixed)
+    fixed.check()
+    assert abs(guided.mean() / plain.mean() - 1.0) < 0.02
