@@ -246,7 +246,7 @@ def batch_bench(dev_index: int, n: int = 32) -> dict:
     spp log-uniform 1..256, 1k..2M triangles, full-render material mix and
     envmap, half with a volume box) rendered to completion in one shared path
     pool, shortest request first, bounce loop replayed from a CUDA graph;
-    pool size, graph length and shade grid from the autotuner."""
+    pool size, graph length, shade grid and trace refill from the autotuner."""
     import numpy as np
     import raccoongpurender_gb300 as rg
     from raccoongpurender_gb300 import autotune, scenes
@@ -266,6 +266,7 @@ def batch_bench(dev_index: int, n: int = 32) -> dict:
     tuned = autotune.tune_batch(built, device=dev_index, log=lambda *_: None)
     b = rg.Batch(dev_index, tuned["path_count"])
     b.set_render_tuning(tuned["shade_blocks"], tuned["graph_steps"])
+    b.set_render_trace(tuned.get("render_refill", 12))
     ids = [b.add(sm, cam, cfg) for sm, cam, cfg in built]
     b.run(order=rg.ORDER_SHORTEST_FIRST, steps_per_launch=tuned["graph_steps"], max_steps=200)  # warm
     t0 = time.perf_counter()

@@ -328,7 +328,7 @@ int rgr_set_trace_tuning(rgr_context* c, int32_t refill, int32_t blocks_per_sm);
 
 /* How a bounce casts its extension rays: persistent = 1 runs a persistent
    closest-hit kernel over the slots just shaded whose warps take new slots
-   when at least `refill` (1..32, default 24) lanes are idle, then the logic
+   when at least `refill` (1..32, default 12) lanes are idle, then the logic
    kernel; persistent = 0 traces and runs the logic in one kernel, one thread
    per slot; persistent = -1 (default) picks 1 for scenes of at least 4096
    inner BVH nodes.  Results are identical.  Takes effect at the next

@@ -594,7 +594,7 @@ class WavefrontLane:
     def set_trace_tuning(self, refill: int = 16, blocks_per_sm: int = 0) -> None:
         _check(self._lib.rgr_set_trace_tuning(self._h, refill, blocks_per_sm), "rgr_set_trace_tuning")
 
-    def set_render_trace(self, persistent=-1, refill: int = 24) -> None:
+    def set_render_trace(self, persistent=-1, refill: int = 12) -> None:
         """Extension rays of a bounce: persistent refilling kernel + logic (True),
         fused (False), or by scene size (-1, the default)."""
         mode = persistent if isinstance(persistent, int) and not isinstance(persistent, bool) else int(bool(persistent))
@@ -804,6 +804,12 @@ class Batch:
     def set_render_tuning(self, shade_blocks_per_sm: int = 8, graph_steps: int = 8) -> None:
         _check(self._lib.rgr_set_render_tuning(self._lib.rgr_batch_context(self._h), shade_blocks_per_sm,
                                                graph_steps), "rgr_set_render_tuning")
+
+    def set_render_trace(self, refill: int = 12) -> None:
+        """Refill threshold of the bounce's persistent closest-hit kernel (the
+        kernel is chosen by scene size, as for a single render)."""
+        _check(self._lib.rgr_set_render_trace(self._lib.rgr_batch_context(self._h), -1, refill),
+               "rgr_set_render_trace")
 
     def request_stats(self, rid: int) -> rgr_request_stats:
         st = rgr_request_stats()

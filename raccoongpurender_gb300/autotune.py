@@ -4,6 +4,8 @@ Knobs (all results are bit-identical across knob values; only speed changes):
   * path_count     — resident paths in the pool (queue capacities follow it);
   * graph_steps    — bounces per replayed CUDA graph;
   * shade_blocks   — resident 256-thread blocks per SM of the shade kernel;
+  * render_refill  — refill a warp of the bounce's persistent trace kernel
+                     when this many lanes are idle;
   * trace_refill   — refill a closest-hit warp with new rays when this many
                      lanes are idle;
   * trace_stage    — top BVH nodes each closest-hit CTA stages in shared
@@ -23,8 +25,9 @@ import os
 import time
 from pathlib import Path
 
-DEFAULTS = dict(path_count=1 << 22, graph_steps=8, shade_blocks=8)
-CANDIDATES = dict(path_count=[1 << 20, 1 << 21, 1 << 22, 1 << 23, 1 << 24], graph_steps=[4, 8, 16], shade_blocks=[4, 8, 16])
+DEFAULTS = dict(path_count=1 << 22, graph_steps=8, shade_blocks=8, render_refill=12)
+CANDIDATES = dict(path_count=[1 << 20, 1 << 21, 1 << 22, 1 << 23, 1 << 24], graph_steps=[4, 8, 16], shade_blocks=[4, 8, 16],
+                  render_refill=[8, 16, 24])
 TRACE_DEFAULTS = dict(trace_refill=24, trace_stage=0)
 TRACE_CANDIDATES = dict(trace_refill=[8, 16, 24, 32], trace_stage=[0, 64, 256, 1024])
 
@@ -102,6 +105,7 @@ def tune_batch(scenes_and_requests, device: int = 0, spp_cap: int = 4, use_cache
     def trial(p):
         b = rg.Batch(device, p["path_count"])
         b.set_render_tuning(p["shade_blocks"], p["graph_steps"])
+        b.set_render_trace(p["render_refill"])
         for s, c, f in scenes_and_requests:
             g = rg.render_config(dof=f.dof, rr_depth=f.rr_depth, radiance_clamp=f.radiance_clamp,
                                  env_select_prob=f.env_select_prob, max_depth=f.max_depth,

@@ -194,7 +194,9 @@ struct rgr_context {
     int trace_refill = 24;   // refill a warp when this many lanes are idle (measured best of 1..32)
     int trace_blocks = 0;    // resident blocks per SM asked for (0: as many as fit)
     // extension rays of a bounce: persistent refilling kernel, then logic (or fused)
-    TraceShape render_trace{true, 24, 0, nullptr};
+    // refill 12: the mixed 1080p render at 2^24 paths runs 1047.7 / 1066.6 / 1067.6 / 1066.5 /
+    // 1059.5 Mpaths/s with a warp refilled at 24 / 8 / 12 / 16 / 20 idle lanes
+    TraceShape render_trace{true, 12, 0, nullptr};
     int render_trace_mode = -1;  // 1 persistent, 0 fused, -1 by scene size at render begin
     uint32_t trace_stage = 0;  // top BVH nodes staged in shared memory per CTA
     // learned path guiding: the attached network and this render's per-slot buffers
