@@ -169,8 +169,17 @@ __device__ __forceinline__ float2 half2_float2(uint32_t v) {
 __device__ __forceinline__ float4 mixture_lobe(const uint4* p, int i) {
     const uint2 q = __ldg(reinterpret_cast<const uint2*>(p) + i);
     const float2 xy = half2_float2(q.x), zk = half2_float2(q.y);
-    const float inv = 1.0f / sqrtf(fmaxf(xy.x * xy.x + xy.y * xy.y + zk.x * zk.x, 1.0e-30f));
+    const float inv = rsqrtf(fmaxf(xy.x * xy.x + xy.y * xy.y + zk.x * zk.x, 1.0e-30f));
     return make_float4(xy.x * inv, xy.y * inv, zk.x * inv, zk.y);
+}
+// The vMF density as the shading kernel evaluates it: the SFU's exponential and
+// reciprocal.  Sampling (mixture_sample) and evaluation (mixture_pdf) decode the
+// record with the same functions, so the pdf a sample is weighted with is the
+// density it was drawn from up to the SFU's relative error (about 2^-21); the
+// compiler's IEEE division and square root, which the path arithmetic needs for
+// parity with the reference, are not used here.
+__device__ __forceinline__ float vmf_pdf_fast(float kappa, float c) {
+    return __fdividef(kappa, 6.283185307179586f * (1.0f - __expf(-2.0f * kappa))) * __expf(kappa * (c - 1.0f));
 }
 // the guide's share of the non-envmap probability at the vertex: the sum of the stored weights
 __device__ __forceinline__ float mixture_alpha(const uint4* p) {
@@ -200,7 +209,7 @@ __device__ __forceinline__ void mixture_weights(const uint4* p, float* w) {
     float sum = 0.0f;
 #pragma unroll
     for (int i = 0; i < kGuideLobes; ++i) sum += w[i];
-    const float inv = 1.0f / fmaxf(sum, 1.0e-30f);
+    const float inv = __fdividef(1.0f, fmaxf(sum, 1.0e-30f));
 #pragma unroll
     for (int i = 0; i < kGuideLobes; ++i) w[i] *= inv;
 }
@@ -211,7 +220,7 @@ __device__ __forceinline__ float mixture_pdf(const uint4* p, float dx, float dy,
 #pragma unroll
     for (int i = 0; i < kGuideLobes; ++i) {
         const float4 L = mixture_lobe(p, i);
-        pdf += w[i] * vmf_pdf(L.w, L.x * dx + L.y * dy + L.z * dz);
+        pdf += w[i] * vmf_pdf_fast(L.w, L.x * dx + L.y * dy + L.z * dz);
     }
     return pdf;
 }
@@ -230,23 +239,23 @@ __device__ __forceinline__ void mixture_sample(const uint4* p, float u0, float u
     }
     const float4 L = mixture_lobe(p, k);
     const float kappa = L.w;
-    float wc = 1.0f + logf(u1 + (1.0f - u1) * expf(-2.0f * kappa)) / kappa;
+    float wc = 1.0f + __fdividef(__logf(u1 + (1.0f - u1) * __expf(-2.0f * kappa)), kappa);
     wc = fminf(fmaxf(wc, -1.0f), 1.0f);
     const float s = sqrtf(fmaxf(0.0f, 1.0f - wc * wc));
     float sp, cp;
-    sincospif(2.0f * u2, &sp, &cp);
+    __sincosf(6.283185307179586f * u2, &sp, &cp);
     const float sign = L.z >= 0.0f ? 1.0f : -1.0f;
-    const float a = -1.0f / (sign + L.z);
+    const float a = __fdividef(-1.0f, sign + L.z);  // |sign + z| >= 1
     const float bb = L.x * L.y * a;
     const float tx = 1.0f + sign * L.x * L.x * a, ty = sign * bb, tz = -sign * L.x;
     const float bx = bb, by = sign + L.y * L.y * a, bz = -L.y;
     float x = wc * L.x + s * (cp * tx + sp * bx);
     float y = wc * L.y + s * (cp * ty + sp * by);
     float z = wc * L.z + s * (cp * tz + sp * bz);
-    const float n = sqrtf(x * x + y * y + z * z);
-    d[0] = x / n;
-    d[1] = y / n;
-    d[2] = z / n;
+    const float n = rsqrtf(x * x + y * y + z * z);
+    d[0] = x * n;
+    d[1] = y * n;
+    d[2] = z * n;
 }
 
 // ------------------------------------------------------------ launchers (guide_mlp.cu)
