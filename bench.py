@@ -123,6 +123,28 @@ def build_workload(level: int = 8, res: int = 2048):
     return mesh, sm, coherent, incoherent, build_s
 
 
+def closest_hit_once(dev_index: int = 0) -> None:
+    """One launch of the closest-hit kernel per ray set of the workload above
+    (coherent, then incoherent) with the library's default launch shape, rays
+    in device memory: the command the kernel's ncu captures run."""
+    import torch
+
+    import raccoongpurender_gb300 as rg
+    mesh, sm, coherent, incoherent, _ = build_workload()
+    lane = rg.WavefrontLane(dev_index, 1024)
+    lane.setup(sm)
+    dev = torch.device("cuda", dev_index)
+    stream = torch.cuda.Stream(dev)
+    for rays in (coherent, incoherent):
+        soa = [torch.from_numpy(a).to(dev) for a in rays.soa()]
+        prim = torch.empty(len(rays), dtype=torch.int32, device=dev)
+        t = torch.empty(len(rays), dtype=torch.float32, device=dev)
+        torch.cuda.synchronize(dev)
+        lane.trace_closest_device([a.data_ptr() for a in soa], len(rays), prim.data_ptr(), t.data_ptr(), 0,
+                                  stream.cuda_stream)
+        stream.synchronize()
+
+
 def render_bench(dev_index: int, which: str, repeats: int = 2, pools=(1 << 22,)) -> dict:
     """Full wavefront renders at a fixed sample budget, timed with CUDA events
     on the context stream (host waits only at the end).
@@ -267,6 +289,7 @@ def batch_bench(dev_index: int, n: int = 32) -> dict:
     b = rg.Batch(dev_index, tuned["path_count"])
     b.set_render_tuning(tuned["shade_blocks"], tuned["graph_steps"])
     b.set_render_trace(tuned.get("render_refill", 12))
+    b.set_trace_search(tuned.get("render_search", 8))
     ids = [b.add(sm, cam, cfg) for sm, cam, cfg in built]
     b.run(order=rg.ORDER_SHORTEST_FIRST, steps_per_launch=tuned["graph_steps"], max_steps=200)  # warm
     t0 = time.perf_counter()

@@ -335,6 +335,16 @@ int rgr_set_trace_tuning(rgr_context* c, int32_t refill, int32_t blocks_per_sm);
    rgr_render_begin. */
 int rgr_set_render_trace(rgr_context* c, int32_t persistent, int32_t refill);
 
+/* Leaf batching of the persistent traversal kernels: within a round a warp's
+   lanes take node steps while at least `search` (1..32) of them still search
+   for their next leaf; the lanes that reached one wait there, then all of
+   them intersect their leaves together (1 = every lane waits for the last
+   one).  `closest` sets the closest-hit kernel (rgr_trace_closest*),
+   `render` the extension rays of a render's bounces (takes effect at the
+   next rgr_render_begin); 0 leaves that one unchanged.  Results are
+   identical for every value.  Default 8 and 8; chosen by the autotuner. */
+int rgr_set_trace_search(rgr_context* c, int32_t closest, int32_t render);
+
 /* Shared-memory staging of the closest-hit kernel: each CTA copies the first
    staged_nodes (0..1024) inner nodes — the top levels of the tree, which the
    builder stores first in breadth-first order — into shared memory and reads

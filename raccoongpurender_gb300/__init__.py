@@ -169,6 +169,7 @@ _SIGS = {
     "rgr_set_trace_staging": (C.c_int, [C.c_void_p, C.c_uint32]),
     "rgr_set_trace_host_mode": (C.c_int, [C.c_void_p, C.c_int32]),
     "rgr_set_render_trace": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32]),
+    "rgr_set_trace_search": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32]),
     "rgr_set_render_tuning": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32]),
     "rgr_batch_create": (C.c_int, [C.c_void_p, C.c_int32, C.c_uint32]),
     "rgr_batch_destroy": (None, [C.c_void_p]),
@@ -600,6 +601,13 @@ class WavefrontLane:
         mode = persistent if isinstance(persistent, int) and not isinstance(persistent, bool) else int(bool(persistent))
         _check(self._lib.rgr_set_render_trace(self._h, mode, refill), "rgr_set_render_trace")
 
+    def set_trace_search(self, closest: int = 8, render: int = 8) -> None:
+        """Leaf batching of the persistent traversal kernels: a warp takes node
+        steps while at least this many of its lanes still search for their next
+        leaf (closest-hit kernel / a render's extension rays; 0 leaves one
+        unchanged).  Results are identical for every value."""
+        _check(self._lib.rgr_set_trace_search(self._h, closest, render), "rgr_set_trace_search")
+
     def set_trace_host_mode(self, mode: int) -> None:
         """rgr_trace_closest with host arrays: TRACE_HOST_AUTO (zero copy where the
         GPU can address them) or TRACE_HOST_COPY (chunked copies)."""
@@ -810,6 +818,11 @@ class Batch:
         kernel is chosen by scene size, as for a single render)."""
         _check(self._lib.rgr_set_render_trace(self._lib.rgr_batch_context(self._h), -1, refill),
                "rgr_set_render_trace")
+
+    def set_trace_search(self, render: int = 8) -> None:
+        """Leaf batching of the bounce's persistent closest-hit kernel."""
+        _check(self._lib.rgr_set_trace_search(self._lib.rgr_batch_context(self._h), 0, render),
+               "rgr_set_trace_search")
 
     def request_stats(self, rid: int) -> rgr_request_stats:
         st = rgr_request_stats()

@@ -6,8 +6,11 @@ Knobs (all results are bit-identical across knob values; only speed changes):
   * shade_blocks   — resident 256-thread blocks per SM of the shade kernel;
   * render_refill  — refill a warp of the bounce's persistent trace kernel
                      when this many lanes are idle;
+  * render_search  — that kernel's warps take node steps while this many
+                     lanes still search for their next leaf;
   * trace_refill   — refill a closest-hit warp with new rays when this many
                      lanes are idle;
+  * trace_search   — the same leaf batching for the closest-hit kernel;
   * trace_stage    — top BVH nodes each closest-hit CTA stages in shared
                      memory (the "BVH staging depth": 64 nodes = 6 levels).
 Coordinate descent from a default point: each knob in turn is swept over its
@@ -25,11 +28,11 @@ import os
 import time
 from pathlib import Path
 
-DEFAULTS = dict(path_count=1 << 22, graph_steps=8, shade_blocks=8, render_refill=12)
+DEFAULTS = dict(path_count=1 << 22, graph_steps=8, shade_blocks=8, render_refill=12, render_search=8)
 CANDIDATES = dict(path_count=[1 << 20, 1 << 21, 1 << 22, 1 << 23, 1 << 24], graph_steps=[4, 8, 16], shade_blocks=[4, 8, 16],
-                  render_refill=[8, 16, 24])
-TRACE_DEFAULTS = dict(trace_refill=24, trace_stage=0)
-TRACE_CANDIDATES = dict(trace_refill=[8, 16, 24, 32], trace_stage=[0, 64, 256, 1024])
+                  render_refill=[8, 16, 24], render_search=[4, 12, 16])
+TRACE_DEFAULTS = dict(trace_refill=24, trace_search=8, trace_stage=0)
+TRACE_CANDIDATES = dict(trace_refill=[8, 16, 32], trace_search=[4, 12, 16], trace_stage=[0, 64, 256, 1024])
 
 
 def _gpu_name(device: int) -> str:
@@ -106,6 +109,7 @@ def tune_batch(scenes_and_requests, device: int = 0, spp_cap: int = 4, use_cache
         b = rg.Batch(device, p["path_count"])
         b.set_render_tuning(p["shade_blocks"], p["graph_steps"])
         b.set_render_trace(p["render_refill"])
+        b.set_trace_search(p["render_search"])
         for s, c, f in scenes_and_requests:
             g = rg.render_config(dof=f.dof, rr_depth=f.rr_depth, radiance_clamp=f.radiance_clamp,
                                  env_select_prob=f.env_select_prob, max_depth=f.max_depth,
@@ -132,6 +136,7 @@ def tune_trace(lane, ray_sets, stream: int, device: int = 0, reps: int = 3, use_
     def run(p):
         lane.set_trace_staging(p["trace_stage"])
         lane.set_trace_tuning(p["trace_refill"], 0)
+        lane.set_trace_search(p["trace_search"], 0)
         for ptrs, n, pp, tp in ray_sets:  # warm
             lane.trace_closest_device(ptrs, n, pp, tp, 0, stream)
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -147,4 +152,5 @@ def tune_trace(lane, ray_sets, stream: int, device: int = 0, reps: int = 3, use_
     best = tuner.tune(sig, run, use_cache=use_cache, defaults=TRACE_DEFAULTS, candidates=TRACE_CANDIDATES)
     lane.set_trace_staging(best["trace_stage"])
     lane.set_trace_tuning(best["trace_refill"], 0)
+    lane.set_trace_search(best["trace_search"], 0)
     return best, tuner.trials

@@ -193,10 +193,14 @@ struct rgr_context {
     int trace_grid = 0;      // persistent traversal grid (SMs x resident blocks)
     int trace_refill = 24;   // refill a warp when this many lanes are idle (measured best of 1..32)
     int trace_blocks = 0;    // resident blocks per SM asked for (0: as many as fit)
+    // node steps while this many lanes of a warp search for a leaf: 8 measured best of
+    // 1..24 with refill 24 (3702 Mrays/s, 3319 with every lane waiting for the last)
+    int trace_search = 8;
     // extension rays of a bounce: persistent refilling kernel, then logic (or fused)
     // refill 12: the mixed 1080p render at 2^24 paths runs 1047.7 / 1066.6 / 1067.6 / 1066.5 /
     // 1059.5 Mpaths/s with a warp refilled at 24 / 8 / 12 / 16 / 20 idle lanes
-    TraceShape render_trace{true, 12, 0, nullptr};
+    // search 8: 1114.8 Mpaths/s against 1032.8 with every lane waiting for the last
+    TraceShape render_trace{true, 12, 8, 0, nullptr};
     int render_trace_mode = -1;  // 1 persistent, 0 fused, -1 by scene size at render begin
     uint32_t trace_stage = 0;  // top BVH nodes staged in shared memory per CTA
     // learned path guiding: the attached network and this render's per-slot buffers
@@ -770,8 +774,8 @@ int rgr_trace_closest_device(rgr_context* c, const rgr_ray_soa* rays, uint64_t n
     if (r != RGR_OK) return r;
     if ((r = c->tcounter.alloc(8)) != RGR_OK) return r;
     launch_trace_rays(c->scene.sv, rays->ox, rays->oy, rays->oz, rays->dx, rays->dy, rays->dz, rays->tmax, n, prim, t, ng_xyz,
-                      c->err.as<uint32_t>(), c->tcounter.as<unsigned long long>(), c->trace_refill, c->trace_grid,
-                      c->trace_stage, st);
+                      c->err.as<uint32_t>(), c->tcounter.as<unsigned long long>(), c->trace_refill, c->trace_search,
+                      c->trace_grid, c->trace_stage, st);
     RGR_CUDA(cudaGetLastError());
     return RGR_OK;
 }
@@ -812,6 +816,17 @@ int rgr_set_render_trace(rgr_context* c, int32_t persistent, int32_t refill) {
     c->render_trace.refill = refill;
     c->begun = false;  // takes effect at the next render begin
     c->drop_graph();
+    return RGR_OK;
+}
+
+int rgr_set_trace_search(rgr_context* c, int32_t closest, int32_t render) {
+    if (!c || closest < 0 || closest > 32 || render < 0 || render > 32) return RGR_E_INVALID;
+    if (closest > 0) c->trace_search = closest;
+    if (render > 0 && render != c->render_trace.search) {
+        c->render_trace.search = render;
+        c->begun = false;  // takes effect at the next render begin
+        c->drop_graph();
+    }
     return RGR_OK;
 }
 
@@ -899,7 +914,7 @@ int rgr_trace_closest(rgr_context* c, const rgr_ray_soa* rays, uint64_t n, int32
             // 2905 with the threshold tuned for rays in device memory)
             launch_trace_rays(c->scene.sv, dsrc[0], dsrc[1], dsrc[2], dsrc[3], dsrc[4], dsrc[5], dsrc[6], n, dprim, dt,
                               nullptr, ts.err.as<uint32_t>(), ts.counter.as<unsigned long long>(), kZeroCopyRefill,
-                              c->trace_grid, c->trace_stage, st);
+                              c->trace_search, c->trace_grid, c->trace_stage, st);
             RGR_CUDA(cudaGetLastError());
             uint32_t err = 0;
             RGR_CUDA(cudaMemcpyAsync(&err, ts.err.p, 4, cudaMemcpyDeviceToHost, st));
@@ -937,8 +952,8 @@ int rgr_trace_closest(rgr_context* c, const rgr_ray_soa* rays, uint64_t n, int32
         launch_trace_rays(c->scene.sv, ts.rays[0].as<float>(), ts.rays[1].as<float>(), ts.rays[2].as<float>(),
                           ts.rays[3].as<float>(), ts.rays[4].as<float>(), ts.rays[5].as<float>(),
                           ts.rays[6].as<float>(), m, ts.prim.as<int32_t>(), ts.t.as<float>(), nullptr,
-                          ts.err.as<uint32_t>(), ts.counter.as<unsigned long long>(), c->trace_refill, c->trace_grid,
-                          c->trace_stage, st);
+                          ts.err.as<uint32_t>(), ts.counter.as<unsigned long long>(), c->trace_refill,
+                          c->trace_search, c->trace_grid, c->trace_stage, st);
         RGR_CUDA(cudaGetLastError());
         RGR_CUDA(cudaMemcpyAsync(prim + off, ts.prim.p, 4 * m, cudaMemcpyDeviceToHost, st));
         RGR_CUDA(cudaMemcpyAsync(t + off, ts.t.p, 4 * m, cudaMemcpyDeviceToHost, st));

@@ -200,8 +200,8 @@ extern "C" int rgr_render_noalloc(rgr_context* c, const rgr_camera* cam, const r
         return RGR_E_CUDA;
     launch_init(p, q, k.seed_offset, st);
     if (!ok(cudaGetLastError(), "kernel launch")) return RGR_E_CUDA;
-    const TraceShape ts{true, 24, sms * (trace_paths_max_blocks_per_sm() > 0 ? trace_paths_max_blocks_per_sm() : 1),
-                        scal + 3};
+    const TraceShape ts{true, 24, 8,
+                        sms * (trace_paths_max_blocks_per_sm() > 0 ? trace_paths_max_blocks_per_sm() : 1), scal + 3};
     for (int32_t i = 0; i < steps; ++i) {
         launch_compact_new(p, q, st);
         launch_shade(p, q, rp, sms * 8, st);

@@ -7,8 +7,10 @@
 //
 // Persistent warps: each warp keeps 32 rays in flight and, between traversal
 // rounds, hands finished lanes new rays from a global counter (one atomic per
-// refill per warp).  Rays are read and results written with streaming
-// (evict-first) cache hints; the tree is read with an L2 evict-last policy.
+// refill per warp).  Within a round the lanes take node steps while at least
+// `search` of them still search for their next leaf; the others wait at
+// theirs.  Rays are read and results written with streaming (evict-first)
+// cache hints; the tree is read with an L2 evict-last policy.
 // Each ray's traversal is unchanged, so results do not depend on the
 // schedule.
 #include "wavefront.cuh"
@@ -33,6 +35,7 @@ struct RayBatch {
     uint32_t* err;
     unsigned long long* next;    // work counter, zero at launch
     int refill;                  // refill when at least this many lanes are idle
+    int search;                  // node steps while at least this many lanes search
     uint32_t stage;              // inner nodes copied to shared memory (kStaged)
 };
 
@@ -78,23 +81,22 @@ __global__ void __launch_bounds__(256, RGR_TRACE_MIN_BLOCKS) k_trace_rays(SceneV
             if (exhausted) break;
             continue;
         }
-        if (ray != ~0ull) {
-            if (s.link != kDone) trace_round<kCount, kStaged, kSmemStack>(sc, s, &cnt, err, pol, stn);
-            if (s.link == kDone) {
-                __stcs(b.prim + ray, s.prim);
-                __stcs(b.t + ray, s.tmin);
-                if (b.ng) {
-                    f3 n = s.prim >= 0 ? hit_normal(sc, s.prim, s.ro, s.rd, s.tmin) : mk(0.0f, 0.0f, 0.0f);
-                    b.ng[3 * ray + 0] = n.x;
-                    b.ng[3 * ray + 1] = n.y;
-                    b.ng[3 * ray + 2] = n.z;
-                }
-                if (kCount) {
-                    b.nodes[ray] = cnt.nodes;
-                    b.prims[ray] = cnt.prims;
-                }
-                ray = ~0ull;
+        trace_warp_round<kCount, kStaged, kSmemStack>(sc, s, ray != ~0ull && s.link != kDone, b.search, &cnt, err, pol,
+                                                      stn);
+        if (ray != ~0ull && s.link == kDone) {
+            __stcs(b.prim + ray, s.prim);
+            __stcs(b.t + ray, s.tmin);
+            if (b.ng) {
+                f3 n = s.prim >= 0 ? hit_normal(sc, s.prim, s.ro, s.rd, s.tmin) : mk(0.0f, 0.0f, 0.0f);
+                b.ng[3 * ray + 0] = n.x;
+                b.ng[3 * ray + 1] = n.y;
+                b.ng[3 * ray + 2] = n.z;
             }
+            if (kCount) {
+                b.nodes[ray] = cnt.nodes;
+                b.prims[ray] = cnt.prims;
+            }
+            ray = ~0ull;
         }
     }
     if (err) atomicOr(b.err, err);
@@ -104,10 +106,10 @@ __global__ void __launch_bounds__(256, RGR_TRACE_MIN_BLOCKS) k_trace_rays(SceneV
 
 void launch_trace_rays(const SceneView& sc, const float* ox, const float* oy, const float* oz, const float* dx,
                        const float* dy, const float* dz, const float* tmax, uint64_t n, int32_t* prim, float* t,
-                       float* ng, uint32_t* err, unsigned long long* counter, int refill, int grid, uint32_t stage,
-                       cudaStream_t st) {
+                       float* ng, uint32_t* err, unsigned long long* counter, int refill, int search, int grid,
+                       uint32_t stage, cudaStream_t st) {
     if (n == 0) return;
-    RayBatch b{ox, oy, oz, dx, dy, dz, tmax, n, prim, t, ng, nullptr, nullptr, err, counter, refill, stage};
+    RayBatch b{ox, oy, oz, dx, dy, dz, tmax, n, prim, t, ng, nullptr, nullptr, err, counter, refill, search, stage};
     cudaMemsetAsync(counter, 0, sizeof(unsigned long long), st);
     if (stage > 0)
         k_trace_rays<false, true><<<grid, kStackThreads, 64 * (size_t)stage, st>>>(sc, b);
@@ -120,7 +122,7 @@ void launch_trace_rays_counts(const SceneView& sc, const float* ox, const float*
                               float* t, uint32_t* nodes, uint32_t* prims, uint32_t* err, unsigned long long* counter,
                               int grid, cudaStream_t st) {
     if (n == 0) return;
-    RayBatch b{ox, oy, oz, dx, dy, dz, tmax, n, prim, t, nullptr, nodes, prims, err, counter, 16, 0u};
+    RayBatch b{ox, oy, oz, dx, dy, dz, tmax, n, prim, t, nullptr, nodes, prims, err, counter, 16, 1, 0u};
     cudaMemsetAsync(counter, 0, sizeof(unsigned long long), st);
     k_trace_rays<true, false><<<grid, kStackThreads, 0, st>>>(sc, b);
 }

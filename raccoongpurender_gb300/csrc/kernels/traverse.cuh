@@ -12,13 +12,16 @@
 //     far child of the deepest pending "both hit" node, without re-testing
 //     its box; a short stack of those far links does the same thing.
 // Layout: 64-byte inner nodes holding both child boxes (one 64-byte line,
-// four 16-byte read-only loads), leaves encoded in the parent's link, and
+// two 32-byte read-only loads), leaves encoded in the parent's link, and
 // primitives pre-gathered in leaf order as 48-byte records (v0, v1-v0, v2-v0:
 // the edge subtraction is done once on the host and is bit-identical).
 //
 // The state of one ray lives in TraceState so that a warp can run rounds
 // (inner nodes down to one leaf, then that leaf) and refill finished lanes
 // with new rays between rounds; the visit order of each ray is unchanged.
+// trace_warp_round lets the lanes that found their leaf wait while enough
+// others still search, instead of waiting for the last one (exact: each lane
+// still intersects its leaves in its own order).
 // BVH loads carry an L2 evict-last policy so that streaming ray data does not
 // push the tree out of L2.
 #pragma once
@@ -53,6 +56,16 @@ RGR_DEV float4 ld_keep(const float4* ptr, uint64_t pol) {
         : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
         : "l"(ptr), "l"(pol));
     return v;
+}
+
+// 32-byte read-only load (sm_100 and later) into two float4, same policy; the
+// address must be 32-byte aligned.  A warp's divergent lanes cost the L1 one
+// request per lane per load instruction, so a 64-byte node in two of these
+// costs half of what four 16-byte loads do.
+RGR_DEV void ld_keep8(const float4* ptr, uint64_t pol, float4& a, float4& b) {
+    asm("ld.global.nc.L2::cache_hint.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8], %9;"
+        : "=f"(a.x), "=f"(a.y), "=f"(a.z), "=f"(a.w), "=f"(b.x), "=f"(b.y), "=f"(b.z), "=f"(b.w)
+        : "l"(ptr), "l"(pol));
 }
 
 // slabs_with_hit (extension_ray_cast_stackless.cl:35-50).  fminf/fmaxf have
@@ -190,70 +203,81 @@ struct StagedNodes {
     uint32_t n;
 };
 
+// One inner node: both child boxes slab-tested against the current tmin
+// (extension_ray_cast_stackless.cl:81-200); returns the next link (the
+// nearer hit child, the only hit child, or the newest pending far link).
+template <bool kNanCheck, bool kCount, bool kStaged, int kSm>
+RGR_DEV uint32_t node_step(const SceneView& sc, TraceState& s, uint32_t link, TraceCounters* cnt, uint32_t& err,
+                           uint64_t pol, StagedNodes st) {
+    float4 q0, q1, q2, q3;
+    if (kStaged && link < st.n) {
+        const float4* np = st.smem + 4 * link;
+        q0 = np[0];
+        q1 = np[1];
+        q2 = np[2];
+        q3 = np[3];
+    } else {
+        const float4* np = sc.nodes + 4 * (size_t)link;  // 64-byte aligned
+        ld_keep8(np, pol, q0, q1);
+        ld_keep8(np + 2, pol, q2, q3);
+    }
+    if (kCount) cnt->nodes++;
+    float L0, L1, R0, R1;
+    const bool L = slab<kNanCheck>(q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, s.ro, s.inv, s.tmin, L0, L1);
+    const bool R = slab<kNanCheck>(q1.z, q1.w, q2.x, q2.y, q2.z, q2.w, s.ro, s.inv, s.tmin, R0, R1);
+    const uint32_t cl = __float_as_uint(q3.x), cr = __float_as_uint(q3.y);
+    if (L && R) {
+        const bool left_first = (L0 == R0) ? (L1 < R1) : (L0 < R0);
+        if (s.sp < kStackSize) {  // push the far child
+            if (s.sp > 0) stack_put<kSm>(s, s.sp - 1, s.top);
+            s.top = left_first ? cr : cl;
+            s.sp++;
+        } else {
+            err |= kErrStackOverflow;  // unreachable: tree depth <= 63
+        }
+        return left_first ? cl : cr;
+    }
+    if (L) return cl;
+    if (R) return cr;
+    return pop<kSm>(s);
+}
+
+// The primitives of the leaf `link` in the reference primitive_ids order;
+// returns the newest pending far link.
+template <bool kCount, int kSm>
+RGR_DEV uint32_t leaf_step(const SceneView& sc, TraceState& s, uint32_t link, TraceCounters* cnt, uint64_t pol) {
+    const float4* __restrict__ prims = sc.prims;
+    const uint32_t first = link & 0x0fffffffu;
+    const uint32_t count = ((link >> 28) & 7u) + 1u;
+    for (uint32_t k = 0; k < count; ++k) {
+        // a 48-byte record starts on a 32-byte boundary when its index is even:
+        // (a, b) in one 32-byte load and c in a 16-byte one; when it is odd, a in
+        // a 16-byte load and (b, c) in a 32-byte one
+        const uint32_t rec = first + k;
+        const float4* pp = prims + 3 * (size_t)rec;
+        const bool even = (rec & 1u) == 0u;
+        float4 w0, w1;
+        ld_keep8(even ? pp : pp + 1, pol, w0, w1);
+        const float4 w2 = ld_keep(even ? pp + 2 : pp, pol);
+        const float4 a = even ? w0 : w2, b = even ? w1 : w0, c = even ? w2 : w1;
+        if (kCount) cnt->prims++;
+        if (__float_as_uint(b.w) == 0u) {
+            if (tri_test(s.ro, s.rd, xyz(a), xyz(b), xyz(c), s.tmin)) s.prim = (int32_t)__float_as_uint(a.w);
+        } else {
+            if (sphere_test(s.ro, s.rd, xyz(a), b.x, s.tmin)) s.prim = (int32_t)__float_as_uint(a.w);
+        }
+    }
+    return pop<kSm>(s);
+}
+
 // One round: inner nodes down to the next leaf, then that leaf.  On return
 // s.link is the next link to visit, or kDone.
 template <bool kNanCheck, bool kCount, bool kStaged, int kSm>
 RGR_DEV void trace_round_t(const SceneView& sc, TraceState& s, TraceCounters* cnt, uint32_t& err, uint64_t pol,
                            StagedNodes st) {
-    const float4* __restrict__ nodes = sc.nodes;
     uint32_t link = s.link;
-    while (!(link & kLeafFlag)) {
-        float4 q0, q1, q2, q3;
-        if (kStaged && link < st.n) {
-            const float4* np = st.smem + 4 * link;
-            q0 = np[0];
-            q1 = np[1];
-            q2 = np[2];
-            q3 = np[3];
-        } else {
-            const float4* np = nodes + 4 * (size_t)link;
-            q0 = ld_keep(np + 0, pol);
-            q1 = ld_keep(np + 1, pol);
-            q2 = ld_keep(np + 2, pol);
-            q3 = ld_keep(np + 3, pol);
-        }
-        if (kCount) cnt->nodes++;
-        float L0, L1, R0, R1;
-        bool L = slab<kNanCheck>(q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, s.ro, s.inv, s.tmin, L0, L1);
-        bool R = slab<kNanCheck>(q1.z, q1.w, q2.x, q2.y, q2.z, q2.w, s.ro, s.inv, s.tmin, R0, R1);
-        const uint32_t cl = __float_as_uint(q3.x), cr = __float_as_uint(q3.y);
-        if (L && R) {
-            bool left_first = (L0 == R0) ? (L1 < R1) : (L0 < R0);
-            if (s.sp < kStackSize) {  // push the far child
-                if (s.sp > 0) stack_put<kSm>(s, s.sp - 1, s.top);
-                s.top = left_first ? cr : cl;
-                s.sp++;
-            } else {
-                err |= kErrStackOverflow;  // unreachable: tree depth <= 63
-            }
-            link = left_first ? cl : cr;
-        } else if (L) {
-            link = cl;
-        } else if (R) {
-            link = cr;
-        } else {
-            link = pop<kSm>(s);
-        }
-    }
-    if (link != kDone) {
-        // leaf: primitives in the reference primitive_ids order
-        const float4* __restrict__ prims = sc.prims;
-        const uint32_t first = link & 0x0fffffffu;
-        const uint32_t count = ((link >> 28) & 7u) + 1u;
-        for (uint32_t k = 0; k < count; ++k) {
-            const float4* pp = prims + 3 * (size_t)(first + k);
-            const float4 a = ld_keep(pp + 0, pol);
-            const float4 b = ld_keep(pp + 1, pol);
-            if (kCount) cnt->prims++;
-            if (__float_as_uint(b.w) == 0u) {
-                const float4 c = ld_keep(pp + 2, pol);
-                if (tri_test(s.ro, s.rd, xyz(a), xyz(b), xyz(c), s.tmin)) s.prim = (int32_t)__float_as_uint(a.w);
-            } else {
-                if (sphere_test(s.ro, s.rd, xyz(a), b.x, s.tmin)) s.prim = (int32_t)__float_as_uint(a.w);
-            }
-        }
-        link = pop<kSm>(s);
-    }
+    while (!(link & kLeafFlag)) link = node_step<kNanCheck, kCount, kStaged, kSm>(sc, s, link, cnt, err, pol, st);
+    if (link != kDone) link = leaf_step<kCount, kSm>(sc, s, link, cnt, pol);
     s.link = link;
 }
 
@@ -266,6 +290,41 @@ RGR_DEV void trace_round(const SceneView& sc, TraceState& s, TraceCounters* cnt,
     } else {
         trace_round_t<true, kCount, kStaged, kSm>(sc, s, cnt, err, pol, st);
     }
+}
+
+// A round of the whole warp; all 32 lanes call it, `active` on the lanes
+// whose ray is not finished (s.link != kDone).  The active lanes take node
+// steps while at least `min_search` of them are still searching for their
+// next leaf (lanes that reached a leaf, or the end, wait; with min_search =
+// 1 all of them wait for the last), then the lanes at a leaf intersect it.
+// The warp votes once per two node steps (measured: 3702 against 3591
+// Mrays/s with a vote per step on the 1.31M-triangle closest-hit workload).
+// A lane still searching keeps its place and goes on in the next round, so
+// each ray visits the same nodes and leaves in the same order as in
+// trace_round.  `sc` must be a valid scene on every lane.
+template <bool kCount, bool kStaged, int kSm>
+RGR_DEV void trace_warp_round(const SceneView& sc, TraceState& s, bool active, int min_search, TraceCounters* cnt,
+                              uint32_t& err, uint64_t pol, StagedNodes st = StagedNodes{nullptr, 0u}) {
+    const unsigned full = 0xffffffffu;
+    const unsigned act = __ballot_sync(full, active);
+    const bool all_nan_free = __all_sync(full, !active || s.nan_free);
+    uint32_t link = active ? s.link : kDone;
+    for (;;) {
+        const bool searching = !(link & kLeafFlag);  // kDone carries the leaf flag
+        const unsigned sm = __ballot_sync(full, searching);
+        if (sm == 0u || (sm != act && (int)__popc(sm) < min_search)) break;
+        if (searching) {
+            if (all_nan_free) {
+                link = node_step<false, kCount, kStaged, kSm>(sc, s, link, cnt, err, pol, st);
+                if (!(link & kLeafFlag)) link = node_step<false, kCount, kStaged, kSm>(sc, s, link, cnt, err, pol, st);
+            } else {
+                link = s.nan_free ? node_step<false, kCount, kStaged, kSm>(sc, s, link, cnt, err, pol, st)
+                                  : node_step<true, kCount, kStaged, kSm>(sc, s, link, cnt, err, pol, st);
+            }
+        }
+    }
+    if (link != kDone && (link & kLeafFlag)) link = leaf_step<kCount, kSm>(sc, s, link, cnt, pol);
+    if (active) s.link = link;
 }
 
 // Closest hit of one ray.  tmin in: the ray's far clip (ExtensionResult.tmin);

@@ -880,7 +880,7 @@ RGR_DEV void guide_emit_samples(const GuideRenderD& gd, uint32_t slot, f3 L, boo
 // miss leaves P.ng.w at the -1 the shading stage wrote.  Each slot may belong
 // to another request (scene).
 __global__ void __launch_bounds__(256, 5) k_trace_paths(PathsView P, QueueView Q, RenderParams rp,
-                                                         unsigned long long* next, int refill) {
+                                                         unsigned long long* next, int refill, int search) {
     const unsigned full = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     const unsigned lt = (1u << lane) - 1u;
@@ -893,7 +893,7 @@ __global__ void __launch_bounds__(256, 5) k_trace_paths(PathsView P, QueueView Q
     __shared__ uint32_t s_stack[kSmemStack > 0 ? kSmemStack * kStackThreads : 1];
     TraceState s;
     s.sstk = s_stack + threadIdx.x;
-    const SceneView* scp = nullptr;
+    const SceneView* scp = &rp.reqs[0].sc;  // a valid scene on idle lanes too
     uint32_t slot = ~0u;  // ~0: idle
     bool exhausted = false;
     uint32_t err = 0;
@@ -925,17 +925,16 @@ __global__ void __launch_bounds__(256, 5) k_trace_paths(PathsView P, QueueView Q
             if (exhausted) break;
             continue;
         }
-        if (slot != ~0u) {
-            if (s.link != kDone) trace_round<false, false, kSmemStack>(*scp, s, nullptr, err, pol);
-            if (s.link == kDone) {
-                if (s.prim >= 0) {
-                    const f3 ng = hit_normal(*scp, s.prim, s.ro, s.rd, s.tmin);
-                    P.ng[slot] = f4(ng, __int_as_float(s.prim));
-                    P.ro[slot] = f4(s.ro, s.tmin);
-                    P.rd[slot] = f4(s.rd, __int_as_float(-1));
-                }
-                slot = ~0u;
+        trace_warp_round<false, false, kSmemStack>(*scp, s, slot != ~0u && s.link != kDone, search, nullptr, err,
+                                                   pol);
+        if (slot != ~0u && s.link == kDone) {
+            if (s.prim >= 0) {
+                const f3 ng = hit_normal(*scp, s.prim, s.ro, s.rd, s.tmin);
+                P.ng[slot] = f4(ng, __int_as_float(s.prim));
+                P.ro[slot] = f4(s.ro, s.tmin);
+                P.rd[slot] = f4(s.rd, __int_as_float(-1));
             }
+            slot = ~0u;
         }
     }
     if (err) atomicOr(rp.err, err);
@@ -1193,7 +1192,7 @@ cudaError_t launch_trace_paths(const PathsView& p, const QueueView& q, const Ren
     if (!ts.persistent) return cudaSuccess;
     const cudaError_t e = cudaMemsetAsync(ts.counter, 0, sizeof(unsigned long long), st);
     if (e != cudaSuccess) return e;
-    k_trace_paths<<<ts.grid, kStackThreads, 0, st>>>(p, q, rp, ts.counter, ts.refill);
+    k_trace_paths<<<ts.grid, kStackThreads, 0, st>>>(p, q, rp, ts.counter, ts.refill, ts.search);
     return cudaSuccess;
 }
 

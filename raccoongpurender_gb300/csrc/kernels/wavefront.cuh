@@ -178,13 +178,16 @@ void launch_shade(const PathsView& p, const QueueView& q, const RenderParams& rp
 // the guided items at vertices 1..gd.max_depth of their paths (gd.sel / remap / nsel; *nsel zeroed first)
 void launch_guide_select(const PathsView& p, const QueueView& q, const GuideRenderD& gd, int grid, cudaStream_t st);
 // How a bounce casts its extension rays: persistent = a separate persistent
-// closest-hit kernel over the slots just shaded (refilling warps, `grid`
-// CTAs, `counter` a device word it may use; launch_trace_paths, between the
-// shading kernel and the queue resets), then the logic kernel; otherwise one
-// kernel traces and runs the logic per slot (launch_trace_paths does nothing).
+// closest-hit kernel over the slots just shaded (warps refilled when `refill`
+// lanes are idle, node steps while `search` lanes still search for a leaf,
+// `grid` CTAs, `counter` a device word it may use; launch_trace_paths, between
+// the shading kernel and the queue resets), then the logic kernel; otherwise
+// one kernel traces and runs the logic per slot (launch_trace_paths does
+// nothing).
 struct TraceShape {
     bool persistent;
     int refill;
+    int search;
     int grid;
     unsigned long long* counter;
 };
@@ -205,8 +208,8 @@ void launch_merge_intermediate(void* a, const void* b, uint32_t n, cudaStream_t 
 constexpr uint32_t kMaxStagedNodes = 1024;
 void launch_trace_rays(const SceneView& sc, const float* ox, const float* oy, const float* oz, const float* dx,
                        const float* dy, const float* dz, const float* tmax, uint64_t n, int32_t* prim, float* t,
-                       float* ng, uint32_t* err, unsigned long long* counter, int refill, int grid, uint32_t stage,
-                       cudaStream_t st);
+                       float* ng, uint32_t* err, unsigned long long* counter, int refill, int search, int grid,
+                       uint32_t stage, cudaStream_t st);
 void launch_trace_rays_counts(const SceneView& sc, const float* ox, const float* oy, const float* oz, const float* dx,
                               const float* dy, const float* dz, const float* tmax, uint64_t n, int32_t* prim,
                               float* t, uint32_t* nodes, uint32_t* prims, uint32_t* err, unsigned long long* counter,

@@ -32,7 +32,7 @@ struct VolumeD {  // kernels/types.cl:99-102: R.xyz, C
 };
 
 // ---------------------------------------------------------------- BVH
-// Device layout of one inner node: 64 bytes, fetched as four 16-byte loads.
+// Device layout of one inner node: 64 bytes, fetched as two 32-byte loads.
 //   q0 = (L.lo.x, L.lo.y, L.lo.z, L.hi.x)
 //   q1 = (L.hi.y, L.hi.z, R.lo.x, R.lo.y)
 //   q2 = (R.lo.z, R.hi.x, R.hi.y, R.hi.z)

@@ -125,6 +125,29 @@ def test_persistent_and_fused_trace_agree(rg, po):
     np.testing.assert_allclose(out[0][1], out[1][1], rtol=1e-12, atol=1e-300)
 
 
+def test_render_leaf_batching_agrees(rg, po):
+    """The bounce's persistent trace kernel leaves bit-identical slot state
+    and accumulation for every leaf-batching value (1 = every lane waits for
+    the last, 32 = lanes wait only when all are at a leaf)."""
+    mesh, env, camd = scenes.mixed_scene(level=4, seed=3)
+    sm, _ = build(mesh, env=env)
+    cam = camera(camd, 96, 54)
+    out = []
+    for search in (1, 8, 32):
+        lane = rg.WavefrontLane(0, 1 << 14)
+        lane.set_render_trace(True, 12)
+        lane.set_trace_search(0, search)
+        lane.setup(sm)
+        lane.initialize(cam, rg.render_config())
+        lane.step(20)
+        lane.synchronize()
+        out.append((lane.debug_slots(), lane.accumulation()))
+    for o in out[1:]:
+        for k in out[0][0]:
+            assert (np.asarray(out[0][0][k]).view(np.uint32) == np.asarray(o[0][k]).view(np.uint32)).all(), k
+        assert (out[0][1].view(np.uint64) == o[1].view(np.uint64)).all()
+
+
 def test_envmap_tables_on_gpu(rg):
     """FP64 selection weights and normalisation on the GPU: the pdf tables agree
     with the host builder (the reference's) to FP64 rounding, and each alias

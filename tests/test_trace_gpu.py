@@ -80,6 +80,40 @@ def test_empty_scene(rg):
     assert (bits(t) == bits(rays.tmax)).all()
 
 
+@pytest.mark.parametrize("search,refill", [(1, 1), (1, 32), (3, 24), (8, 16), (32, 8), (32, 32)])
+def test_leaf_batching(rg, po, search, refill):
+    """A warp's lanes that reached a leaf wait while at least `search` others
+    still search (1: all wait for the last); every value gives the same hits,
+    on rays in device memory and on host arrays."""
+    import torch
+    mesh = scenes.displaced_icosphere(6, seed=7)
+    sm, osc = build(mesh)
+    lane = rg.WavefrontLane(0, 1024)
+    lane.setup(sm)
+    lane.set_trace_tuning(refill, 0)
+    lane.set_trace_search(search, 0)
+    prim_rays, rnd = scenes.closest_hit_rays(mesh, res=128, n_random=32768, seed=6)
+    for rays in (prim_rays, rnd):
+        _check(lane, osc, rays)
+        dev = torch.device("cuda", 0)
+        soa = [torch.from_numpy(a).to(dev) for a in rays.soa()]
+        prim = torch.empty(len(rays), dtype=torch.int32, device=dev)
+        t = torch.empty(len(rays), dtype=torch.float32, device=dev)
+        lane.trace_closest_device([a.data_ptr() for a in soa], len(rays), prim.data_ptr(), t.data_ptr(), 0, 0)
+        lane.synchronize()
+        oprim, ot, _ = osc.trace(rays.packed8(), threads=16)
+        assert (prim.cpu().numpy() == oprim).all()
+        assert (bits(t.cpu().numpy()) == bits(ot)).all()
+
+
+def test_trace_search_range(rg):
+    lane = rg.WavefrontLane(0, 1024)
+    for bad in ((-1, 8), (33, 8), (8, 33), (8, -1)):
+        with pytest.raises(RuntimeError):
+            lane.set_trace_search(*bad)
+    lane.set_trace_search(0, 0)  # 0 leaves both unchanged
+
+
 @pytest.mark.parametrize("stage", [1, 100, 1024])
 def test_staged_top_levels(rg, po, stage):
     """Top BVH levels read from shared memory give the same hits."""
