@@ -162,7 +162,7 @@ struct rgr_context {
     uint32_t npaths = 0, ntiles = 0;
     DeviceScene scene;
     // paths
-    DevBuf ro, rd, T, L, ng, rng, vols, qid, req, queues[kNumQueues], counts, tile_new, scalars, accum, err;
+    DevBuf slots, qid, req, queues[kNumQueues], counts, tile_new, scalars, accum, err;
     DevBuf reqtab, done;  // request table and its per-request (done, done_ns) counters
     PathsView pv{};
     QueueView qv{};
@@ -221,13 +221,7 @@ struct rgr_context {
         int r;
 #define AL(buf, bytes) \
     if ((r = buf.alloc(bytes)) != RGR_OK) return r;
-        AL(ro, 16 * n);
-        AL(rd, 16 * n);
-        AL(T, 16 * n);
-        AL(L, 16 * n);
-        AL(ng, 16 * n);
-        AL(rng, 16 * n);
-        AL(vols, 32 * n);
+        AL(slots, kSlotBytes * n);
         AL(qid, n);
         AL(req, 2 * n);
         for (int q = 0; q < kNumQueues; ++q) AL(queues[q], 4 * n);
@@ -237,13 +231,7 @@ struct rgr_context {
         AL(err, 16);
 #undef AL
         PathsView& p = pv;
-        p.ro = ro.as<float4>();
-        p.rd = rd.as<float4>();
-        p.T = T.as<float4>();
-        p.L = L.as<float4>();
-        p.ng = ng.as<float4>();
-        p.rng = rng.as<uint4>();
-        p.vols = vols.as<int4>();
+        p.set_slots(slots.p);
         p.qid = qid.as<uint8_t>();
         p.req = req.as<uint16_t>();
         p.n = npaths;
@@ -609,10 +597,9 @@ struct StatePart {
 };
 std::vector<StatePart> render_state(rgr_context* c) {
     const size_t n = (size_t)c->ntiles * kTile;
-    std::vector<StatePart> v = {{&c->ro, 16 * n},   {&c->rd, 16 * n},  {&c->T, 16 * n},      {&c->L, 16 * n},
-                                {&c->ng, 16 * n},   {&c->rng, 16 * n}, {&c->vols, 32 * n},   {&c->qid, n},
-                                {&c->req, 2 * n},   {&c->counts, 32},  {&c->tile_new, 4 * (size_t)c->ntiles},
-                                {&c->scalars, 64},  {&c->err, 16},     {&c->accum, 32 * (size_t)c->npix},
+    std::vector<StatePart> v = {{&c->slots, kSlotBytes * n}, {&c->qid, n},     {&c->req, 2 * n},
+                                {&c->counts, 32},             {&c->tile_new, 4 * (size_t)c->ntiles},
+                                {&c->scalars, 64},            {&c->err, 16},   {&c->accum, 32 * (size_t)c->npix},
                                 {&c->done, 16}};
     for (int q = 0; q < kNumQueues; ++q) v.push_back({&c->queues[q], 4 * n});
     return v;

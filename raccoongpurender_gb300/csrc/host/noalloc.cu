@@ -48,14 +48,8 @@ static_assert(kNoAllocMaxPaths % kTile == 0, "whole tiles");
 // byte offsets inside the scratch array (every region 256-byte aligned)
 constexpr size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
 constexpr size_t kN = kNoAllocMaxPaths;
-constexpr size_t kOffRo = 0;
-constexpr size_t kOffRd = kOffRo + align256(16 * kN);
-constexpr size_t kOffT = kOffRd + align256(16 * kN);
-constexpr size_t kOffL = kOffT + align256(16 * kN);
-constexpr size_t kOffNg = kOffL + align256(16 * kN);
-constexpr size_t kOffRng = kOffNg + align256(16 * kN);
-constexpr size_t kOffVols = kOffRng + align256(16 * kN);
-constexpr size_t kOffQid = kOffVols + align256(32 * kN);
+constexpr size_t kOffSlots = 0;
+constexpr size_t kOffQid = kOffSlots + align256(kSlotBytes * kN);
 constexpr size_t kOffReq = kOffQid + align256(kN);
 constexpr size_t kOffQueues = kOffReq + align256(2 * kN);
 constexpr size_t kOffCounts = kOffQueues + align256(4 * kN) * kNumQueues;
@@ -139,13 +133,7 @@ extern "C" int rgr_render_noalloc(rgr_context* c, const rgr_camera* cam, const r
     const uint32_t ntiles = (path_count + kTile - 1) / kTile;
 
     PathsView p;
-    p.ro = reinterpret_cast<float4*>(base + kOffRo);
-    p.rd = reinterpret_cast<float4*>(base + kOffRd);
-    p.T = reinterpret_cast<float4*>(base + kOffT);
-    p.L = reinterpret_cast<float4*>(base + kOffL);
-    p.ng = reinterpret_cast<float4*>(base + kOffNg);
-    p.rng = reinterpret_cast<uint4*>(base + kOffRng);
-    p.vols = reinterpret_cast<int4*>(base + kOffVols);
+    p.set_slots(base + kOffSlots);
     p.qid = base + kOffQid;
     p.req = reinterpret_cast<uint16_t*>(base + kOffReq);
     p.n = path_count;

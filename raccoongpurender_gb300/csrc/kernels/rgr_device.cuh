@@ -61,11 +61,14 @@ struct Rng {
         return (a << 31) | b;
     }
 };
-RGR_DEV Rng rng_load(const uint4* p, uint32_t i) {
+// p: a uint4 array or a slot field of uint4
+template <class P>
+RGR_DEV Rng rng_load(const P& p, uint32_t i) {
     uint4 v = p[i];
     return Rng{v.x, v.y, v.z, v.w};
 }
-RGR_DEV void rng_store(uint4* p, uint32_t i, const Rng& r) { p[i] = make_uint4(r.s0, r.s1, r.s2, r.s3); }
+template <class P>
+RGR_DEV void rng_store(const P& p, uint32_t i, const Rng& r) { p[i] = make_uint4(r.s0, r.s1, r.s2, r.s3); }
 
 // ------------------------------------------------------------ scene view
 struct SceneView {

@@ -237,8 +237,8 @@ RGR_DEV void shade_slot(const RequestD& rq, const PathsView& P, int k, uint32_t 
         ro4 = P.ro[slot];
         T4 = P.T[slot];
         ng4 = P.ng[slot];
-        vb = P.vols[2 * (size_t)slot + 1];
-        if (k == kMatVolume || vb.w > 0) va = P.vols[2 * (size_t)slot];
+        vb = P.vb[slot];
+        if (k == kMatVolume || vb.w > 0) va = P.va[slot];
     }
     Rng rng = rng_load(P.rng, slot);
     f3 ro = xyz(ro4), rd = xyz(rd4), T = xyz(T4), L = mk(0, 0, 0), Ng = xyz(ng4);
@@ -586,10 +586,10 @@ RGR_DEV void shade_slot(const RequestD& rq, const PathsView& P, int k, uint32_t 
     P.ng[slot] = f4(Ng, __int_as_float(hs));
     if (k == kMatVolume) {
         vb.w = vcount;
-        P.vols[2 * (size_t)slot] = va;
-        P.vols[2 * (size_t)slot + 1] = vb;
+        P.va[slot] = va;
+        P.vb[slot] = vb;
     } else if (fresh) {
-        reinterpret_cast<int*>(P.vols + 2 * (size_t)slot + 1)[3] = 0;  // an empty list; the stale entries stay
+        reinterpret_cast<int*>(&P.vb[slot])[3] = 0;  // an empty list; the stale entries stay
     }
     rng_store(P.rng, slot, rng);
 }
@@ -623,8 +623,8 @@ __global__ void k_init(PathsView P, QueueView Q, uint32_t seed_offset) {
     P.T[i] = make_float4(0, 0, 0, 0);
     P.L[i] = make_float4(0, 0, 0, 0);
     P.ng[i] = make_float4(0, 0, 0, __int_as_float(-1));
-    P.vols[2 * (size_t)i] = make_int4(0, 0, 0, 0);
-    P.vols[2 * (size_t)i + 1] = make_int4(0, 0, 0, 0);
+    P.va[i] = make_int4(0, 0, 0, 0);
+    P.vb[i] = make_int4(0, 0, 0, 0);
     P.qid[i] = 0;  // initialize_all_as_new_path (new_path.cl:9-15)
     P.req[i] = 0;
 }
@@ -1144,7 +1144,7 @@ __global__ void k_debug_slots(PathsView P, uint32_t* out) {
     uint32_t* o = out + 34 * (size_t)i;
     float4 T = P.T[i], L = P.L[i], ro = P.ro[i], rd = P.rd[i], ng = P.ng[i];
     uint4 r = P.rng[i];
-    int4 va = P.vols[2 * (size_t)i], vb = P.vols[2 * (size_t)i + 1];
+    int4 va = P.va[i], vb = P.vb[i];
     const float f[12] = {T.x, T.y, T.z, L.x, L.y, L.z, ro.x, ro.y, ro.z, rd.x, rd.y, rd.z};
     for (int k = 0; k < 12; ++k) o[k] = __float_as_uint(f[k]);
     o[12] = __float_as_uint(L.w);

@@ -22,17 +22,38 @@ enum { kMatLambertian = 1, kMatSpecular = 2, kMatDielectric = 3, kMatWard = 4, k
 //   vols = InVolumeList as two int4: volumes[0..3], (volumes[4..6], count)
 // ShadingResult and IncidentSample never leave registers: the stage that
 // produces them also consumes them.
+// Path state of a slot: kSlotVecs 16-byte vectors, the slots' records one
+// after another (128 bytes per slot).  The fields a stage uses together share
+// a 32-byte sector: (ro, rd) for the closest hit, (T, L) and (ng, rng) for
+// the logic, the volume list (va, vb) when the path is in a volume.  A queue
+// holds a sparse subset of the slots, so a stage reading a queue item's state
+// pulls only sectors it uses (with one array per field each 16-byte vector
+// cost a 32-byte sector of its own).
+constexpr int kSlotVecs = 8;
+constexpr size_t kSlotBytes = 16 * kSlotVecs;
+template <class V, int kField>
+struct SlotField {
+    V* base;  // the first slot's record
+    __host__ __device__ __forceinline__ V& operator[](size_t i) const { return base[i * kSlotVecs + kField]; }
+};
 struct PathsView {
-    float4* ro;
-    float4* rd;
-    float4* T;
-    float4* L;
-    float4* ng;
-    uint4* rng;
-    int4* vols;
+    SlotField<float4, 0> ro;   // origin, tmin (t of the hit)
+    SlotField<float4, 1> rd;   // direction, volume hit
+    SlotField<float4, 2> T;    // throughput, pixel
+    SlotField<float4, 3> L;    // radiance, logic step
+    SlotField<float4, 4> ng;   // geometric normal, primitive
+    SlotField<uint4, 5> rng;   // xoshiro128** state
+    SlotField<int4, 6> va;     // volume list, entries 0..3
+    SlotField<int4, 7> vb;     // entries 4..6, count
     uint8_t* qid;    // queue of the next step, kQueueIdle when done
     uint16_t* req;   // request of the path in the slot
     uint32_t n;
+    // all fields over one buffer of n * kSlotBytes bytes
+    __host__ void set_slots(void* p) {
+        ro.base = rd.base = T.base = L.base = ng.base = static_cast<float4*>(p);
+        rng.base = static_cast<uint4*>(p);
+        va.base = vb.base = static_cast<int4*>(p);
+    }
 };
 
 struct QueueView {

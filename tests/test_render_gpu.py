@@ -126,9 +126,10 @@ def test_persistent_and_fused_trace_agree(rg, po):
 
 
 def test_render_leaf_batching_agrees(rg, po):
-    """The bounce's persistent trace kernel leaves bit-identical slot state
-    and accumulation for every leaf-batching value (1 = every lane waits for
-    the last, 32 = lanes wait only when all are at a leaf)."""
+    """The bounce's persistent trace kernel leaves bit-identical slot state for
+    every leaf-batching value (1 = every lane waits for the last, 32 = lanes
+    wait only when all are at a leaf); the FP64 sums agree to the rounding of
+    their atomic summation order."""
     mesh, env, camd = scenes.mixed_scene(level=4, seed=3)
     sm, _ = build(mesh, env=env)
     cam = camera(camd, 96, 54)
@@ -145,7 +146,7 @@ def test_render_leaf_batching_agrees(rg, po):
     for o in out[1:]:
         for k in out[0][0]:
             assert (np.asarray(out[0][0][k]).view(np.uint32) == np.asarray(o[0][k]).view(np.uint32)).all(), k
-        assert (out[0][1].view(np.uint64) == o[1].view(np.uint64)).all()
+        np.testing.assert_allclose(out[0][1], o[1], rtol=1e-12, atol=1e-300)
 
 
 def test_envmap_tables_on_gpu(rg):
