@@ -519,8 +519,9 @@ int rgr_render_begin(rgr_context* c, const rgr_camera* cam, const rgr_render_con
     RGR_CUDA(cudaMemsetAsync(c->accum.p, 0, 32 * (size_t)c->npix, c->stream));
     RGR_CUDA(cudaMemsetAsync(c->done.p, 0, 16, c->stream));
     const unsigned long long limit = k.spp ? (unsigned long long)k.spp * c->npix : 0ull;
-    RequestD q = request_d(c->scene.sv, *cam, k, c->accum.as<double>(), 0ull, limit ? limit : ~0ull,
-                           c->done.as<unsigned long long>());
+    // no completion counter: nothing reads a single render's completion time, and
+    // the counter cost every warp of the logic kernel an atomic on one address
+    RequestD q = request_d(c->scene.sv, *cam, k, c->accum.as<double>(), 0ull, limit ? limit : ~0ull, nullptr);
     if ((r = c->setup_guiding()) != RGR_OK) return r;
     if (c->guided) q.flags |= kFlagFixBacksideEnvPdf | kFlagTwoSidedLambertian;
     if ((r = c->start(&q, 1, limit, k.seed_offset)) != RGR_OK) return r;

@@ -940,14 +940,13 @@ __global__ void __launch_bounds__(256, 5) k_trace_paths(PathsView P, QueueView Q
     if (err) atomicOr(rp.err, err);
 }
 
-// kPreTraced: k_trace_paths has cast the extension rays of this bounce; the
-// kernel only runs the logic.  Otherwise each thread traces its slot first.
+// The logic of one live slot (logic.cl:27-190) after its extension ray;
+// returns the queue of its next step (0: a new path, counted per tile here;
+// a material queue: appended by the caller).  kPreTraced: k_trace_paths has
+// cast the extension rays of this bounce; otherwise the thread traces first.
 template <bool kGuided, bool kPreTraced>
-__global__ void __launch_bounds__(128) k_trace_logic(PathsView P, QueueView Q, RenderParams rp) {
-    const uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x;
-    const bool live = slot < P.n && P.qid[slot] != kQueueIdle;
-    const unsigned active = __ballot_sync(0xffffffffu, live);
-    if (!live) return;
+RGR_DEV int logic_slot(const PathsView& P, const QueueView& Q, const RenderParams& rp, uint32_t slot,
+                       unsigned active) {
     const int req = P.req[slot];
     const RequestD& rq = rp.reqs[req];
     const SceneView& sc = rq.sc;
@@ -1036,20 +1035,16 @@ __global__ void __launch_bounds__(128) k_trace_logic(PathsView P, QueueView Q, R
     }
     P.qid[slot] = (uint8_t)q;
     {
-        // new paths: count per tile for the ordered compaction; others: material queue
+        // new paths: count per tile for the ordered compaction
         const unsigned newmask = __ballot_sync(active, q == 0);
         if (q == 0) {
             unsigned tp = __match_any_sync(newmask, (int)(slot / kTile));
             int leader = __ffs(tp) - 1;
             if ((int)(threadIdx.x & 31) == leader) atomicAdd(Q.tile_new + slot / kTile, (uint32_t)__popc(tp));
-        } else {
-            enqueue(Q, q, slot, active & ~newmask);
         }
     }
     {
         int lane = threadIdx.x & 31;
-        int leader = __ffs(active) - 1;
-        if (lane == leader) atomicAdd(rp.rays, (unsigned long long)__popc(active));
         if (err) atomicOr(rp.err, err);
         // finished paths per request; the last one of a request stamps its completion time
         const unsigned donemask = __ballot_sync(active, newPath);
@@ -1066,6 +1061,43 @@ __global__ void __launch_bounds__(128) k_trace_logic(PathsView P, QueueView Q, R
             }
         }
     }
+    return q;
+}
+
+// The logic kernel, one thread per slot.  Material-queue appends are gathered
+// per block (shared-memory counts, then one global atomic per queue), and so
+// is the ray count: with one atomic per warp all warps of the launch queued on
+// the same few counters.
+constexpr int kLogicThreads = 256;
+template <bool kGuided, bool kPreTraced>
+__global__ void __launch_bounds__(kLogicThreads) k_trace_logic(PathsView P, QueueView Q, RenderParams rp) {
+    __shared__ uint32_t s_q[kNumQueues];  // items per queue, then the block's base in it
+    if (threadIdx.x < kNumQueues) s_q[threadIdx.x] = 0;
+    const int lane = threadIdx.x & 31;
+    const uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool live = slot < P.n && P.qid[slot] != kQueueIdle;
+    const unsigned active = __ballot_sync(0xffffffffu, live);
+    int q = 0;
+    if (live) q = logic_slot<kGuided, kPreTraced>(P, Q, rp, slot, active);
+    const bool mat = live && q != 0;
+    const unsigned matmask = __ballot_sync(0xffffffffu, mat);
+    __syncthreads();  // s_q cleared
+    uint32_t off = 0;
+    if (mat) {
+        const unsigned peers = __match_any_sync(matmask, q);
+        const int leader = __ffs(peers) - 1;
+        uint32_t base = 0;
+        if (lane == leader) base = atomicAdd(&s_q[q], (uint32_t)__popc(peers));
+        off = __shfl_sync(peers, base, leader) + __popc(peers & ((1u << lane) - 1u));
+    }
+    const int nlive = __syncthreads_count(live);
+    if (threadIdx.x < kNumQueues) {
+        const uint32_t n = s_q[threadIdx.x];
+        if (n) s_q[threadIdx.x] = atomicAdd(Q.counts + threadIdx.x, n);
+    }
+    if (threadIdx.x == 0 && nlive) atomicAdd(rp.rays, (unsigned long long)nlive);
+    __syncthreads();
+    if (mat) queue_items(Q, q)[s_q[q] + off] = slot;
 }
 
 // RGB16 intermediate (accumlation.cl:6-25) from FP64 sums: mean in double,
@@ -1198,19 +1230,19 @@ cudaError_t launch_trace_paths(const PathsView& p, const QueueView& q, const Ren
 
 void launch_trace_logic(const PathsView& p, const QueueView& q, const RenderParams& rp, const TraceShape& ts,
                         cudaStream_t st) {
-    const unsigned nb = (p.n + 127) / 128;
+    const unsigned nb = (p.n + kLogicThreads - 1) / kLogicThreads;
     // the guided variant differs only in recording training samples: a render
     // with a frozen guide runs the plain one (fewer registers)
     const bool recording = rp.gd.lobes && rp.gd.record;
     if (ts.persistent) {
         if (recording)
-            k_trace_logic<true, true><<<nb, 128, 0, st>>>(p, q, rp);
+            k_trace_logic<true, true><<<nb, kLogicThreads, 0, st>>>(p, q, rp);
         else
-            k_trace_logic<false, true><<<nb, 128, 0, st>>>(p, q, rp);
+            k_trace_logic<false, true><<<nb, kLogicThreads, 0, st>>>(p, q, rp);
     } else if (recording) {
-        k_trace_logic<true, false><<<nb, 128, 0, st>>>(p, q, rp);
+        k_trace_logic<true, false><<<nb, kLogicThreads, 0, st>>>(p, q, rp);
     } else {
-        k_trace_logic<false, false><<<nb, 128, 0, st>>>(p, q, rp);
+        k_trace_logic<false, false><<<nb, kLogicThreads, 0, st>>>(p, q, rp);
     }
 }
 
