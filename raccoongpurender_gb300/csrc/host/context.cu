@@ -292,6 +292,7 @@ struct rgr_context {
         RGR_CUDA(cudaMemsetAsync(qv.counts + 1, 0, sizeof(uint32_t) * (kNumQueues - 1), st));
         RGR_CUDA(cudaMemsetAsync(qv.tile_new, 0, sizeof(uint32_t) * ntiles, st));
         launch_trace_logic(pv, qv, rp, render_trace, st);
+        if (!single_render) launch_stamp_done(rp, st);  // batches: per-request completion times
         RGR_CUDA(cudaGetLastError());
         if (guided && train_now) return guide->train_launches(st);
         return RGR_OK;
@@ -401,6 +402,7 @@ struct rgr_context {
         add(&render_trace, sizeof(render_trace));
         add(&graph_steps, sizeof(graph_steps));
         add(&guided, sizeof(guided));
+        add(&single_render, sizeof(single_render));  // batches add the completion stamps
         if (guided) {
             add(&guide->view, sizeof(guide->view));
             add(&guide->cfg, sizeof(guide->cfg));

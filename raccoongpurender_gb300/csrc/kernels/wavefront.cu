@@ -1046,18 +1046,12 @@ RGR_DEV int logic_slot(const PathsView& P, const QueueView& Q, const RenderParam
     {
         int lane = threadIdx.x & 31;
         if (err) atomicOr(rp.err, err);
-        // finished paths per request; the last one of a request stamps its completion time
+        // finished paths per request (k_stamp_done stamps the completion times)
         const unsigned donemask = __ballot_sync(active, newPath);
         if (newPath && rq.done != nullptr) {
             unsigned peers = __match_any_sync(donemask, req);
             if (lane == __ffs(peers) - 1) {
-                const unsigned long long n = __popc(peers);
-                const unsigned long long old = atomicAdd(rq.done, n);
-                if (old + n == rq.sample_end - rq.sample_begin) {
-                    unsigned long long t;
-                    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-                    *rq.done_ns = t;
-                }
+                atomicAdd(rq.done, (unsigned long long)__popc(peers));
             }
         }
     }
@@ -1098,6 +1092,21 @@ __global__ void __launch_bounds__(kLogicThreads) k_trace_logic(PathsView P, Queu
     if (threadIdx.x == 0 && nlive) atomicAdd(rp.rays, (unsigned long long)nlive);
     __syncthreads();
     if (mat) queue_items(Q, q)[s_q[q] + off] = slot;
+}
+
+// The completion time of each request whose paths have all finished, stamped
+// once by the bounce in which its last path ended (after that bounce's logic
+// kernel, when its accumulation is complete).  The logic kernel only counts
+// finished paths: an atomic with a returned value per warp, to find the last
+// one, queued the warps on the requests' counters.
+__global__ void k_stamp_done(RenderParams rp) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= rp.nreq) return;
+    const RequestD& q = rp.reqs[r];
+    if (q.done == nullptr || *q.done_ns != 0ull || *q.done != q.sample_end - q.sample_begin) return;
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    *q.done_ns = t;
 }
 
 // RGB16 intermediate (accumlation.cl:6-25) from FP64 sums: mean in double,
@@ -1244,6 +1253,10 @@ void launch_trace_logic(const PathsView& p, const QueueView& q, const RenderPara
     } else {
         k_trace_logic<false, false><<<nb, kLogicThreads, 0, st>>>(p, q, rp);
     }
+}
+
+void launch_stamp_done(const RenderParams& rp, cudaStream_t st) {
+    if (rp.nreq > 0) k_stamp_done<<<(rp.nreq + 127) / 128, 128, 0, st>>>(rp);
 }
 
 int trace_paths_max_blocks_per_sm() {

@@ -106,7 +106,7 @@ struct RequestD {
     unsigned long long sample_begin;   // global sample indices [begin, end) are this request's
     unsigned long long sample_end;     // ~0: progressive, no end
     unsigned long long* done;          // paths of this request that finished (kept or discarded)
-    unsigned long long* done_ns;       // %globaltimer when the last one finished
+    unsigned long long* done_ns;       // %globaltimer after the bounce in which the last one finished
 };
 
 // RequestD.flags: evaluate the 6-axis envmap pdf of a BSDF-sampled direction
@@ -218,6 +218,8 @@ cudaError_t launch_trace_paths(const PathsView& p, const QueueView& q, const Ren
 void launch_trace_logic(const PathsView& p, const QueueView& q, const RenderParams& rp, const TraceShape& ts,
                         cudaStream_t st);
 int trace_paths_max_blocks_per_sm();
+// per-request completion stamps of a batch (after the logic kernel of a bounce)
+void launch_stamp_done(const RenderParams& rp, cudaStream_t st);
 void launch_readback(int fmt, const double* accum, uint32_t npix, void* dev_out, cudaStream_t st);
 void launch_sum_counts(const double* accum, uint32_t npix, unsigned long long* out, cudaStream_t st);
 void launch_debug_slots(const PathsView& p, uint32_t* out, cudaStream_t st);
