@@ -224,23 +224,26 @@ template <bool kGuided>
 RGR_DEV void shade_slot(const RequestD& rq, const PathsView& P, int k, uint32_t slot, unsigned long long gpix,
                         const GuideRenderD& gd, uint32_t gi) {
     const SceneView& sc = rq.sc;
-    // Path state is loaded only where this item uses it: a material queue is a
-    // sparse subset of the slots, so every 16-byte vector costs a DRAM sector of
-    // its own.  A new path (k = 0) replaces everything but its RNG state and the
-    // volume hit of the ended path; L is loaded (and stored) only when the stage
-    // changes it; the first half of the volume list only when the list is used.
+    // Path state moves by 32-byte sector of the slot record and only where this
+    // item uses it (a material queue is a sparse subset of the slots, so each
+    // sector touched costs a DRAM sector): a new path (k = 0) replaces everything
+    // but its RNG state and the volume hit of the ended path, so it skips the
+    // (T, L) sector and the volume list; L is stored only when the stage changes
+    // it; the first half of the volume list is loaded only when the list is used.
     const bool fresh = k == 0;
-    const float4 rd4 = P.rd[slot];
-    float4 ro4 = make_float4(0.0f, 0.0f, 0.0f, 0.0f), T4 = ro4, ng4 = ro4;
+    float4 ro4, rd4, ng4, rng4, T4 = make_float4(0.0f, 0.0f, 0.0f, 0.0f), L4 = T4;
     int4 va = make_int4(0, 0, 0, 0), vb = va;
+    // the ray's sector and the (ng, rng) sector, each in one access; (T, L) likewise
+    ld_sector<0>(P, slot, ro4, rd4);
+    ld_sector<2>(P, slot, ng4, rng4);
     if (!fresh) {
-        ro4 = P.ro[slot];
-        T4 = P.T[slot];
-        ng4 = P.ng[slot];
+        ld_sector<1>(P, slot, T4, L4);
         vb = P.vb[slot];
         if (k == kMatVolume || vb.w > 0) va = P.va[slot];
+    } else {
+        ro4 = ng4 = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     }
-    Rng rng = rng_load(P.rng, slot);
+    Rng rng = rng_of_bits(rng4);
     f3 ro = xyz(ro4), rd = xyz(rd4), T = xyz(T4), L = mk(0, 0, 0), Ng = xyz(ng4);
     float tmin = ro4.w;
     int32_t hv = __float_as_int(rd4.w);
@@ -539,7 +542,6 @@ RGR_DEV void shade_slot(const RequestD& rq, const PathsView& P, int k, uint32_t 
     const bool touch_L = fresh || kGuided || shLe.x != 0.0f || shLe.y != 0.0f || shLe.z != 0.0f ||
                          !is_finite(T.x) || !is_finite(T.y) || !is_finite(T.z);
     if (touch_L && !fresh) {
-        const float4 L4 = P.L[slot];
         L = xyz(L4);
         logic_i = __float_as_uint(L4.w);
     }
@@ -579,11 +581,11 @@ RGR_DEV void shade_slot(const RequestD& rq, const PathsView& P, int k, uint32_t 
         float u = rng.uniform();
         tmin = -1.0f / vol.w * log_(u);
     }
-    P.ro[slot] = f4(ro, tmin);
-    P.rd[slot] = f4(rd, __int_as_float(hv));
-    P.T[slot] = f4(T, __uint_as_float(pixel));
-    if (touch_L) P.L[slot] = f4(L, __uint_as_float(logic_i));
-    P.ng[slot] = f4(Ng, __int_as_float(hs));
+    st_sector<0>(P, slot, f4(ro, tmin), f4(rd, __int_as_float(hv)));
+    if (touch_L)
+        st_sector<1>(P, slot, f4(T, __uint_as_float(pixel)), f4(L, __uint_as_float(logic_i)));
+    else
+        P.T[slot] = f4(T, __uint_as_float(pixel));
     if (k == kMatVolume) {
         vb.w = vcount;
         P.va[slot] = va;
@@ -591,7 +593,7 @@ RGR_DEV void shade_slot(const RequestD& rq, const PathsView& P, int k, uint32_t 
     } else if (fresh) {
         reinterpret_cast<int*>(&P.vb[slot])[3] = 0;  // an empty list; the stale entries stay
     }
-    rng_store(P.rng, slot, rng);
+    st_sector<2>(P, slot, f4(Ng, __int_as_float(hs)), rng_bits(rng));
 }
 
 // ------------------------------------------------------------ kernels
@@ -797,7 +799,7 @@ RGR_DEV uint32_t mix32(uint32_t h) {  // murmur3 finaliser
     return h;
 }
 
-// A guided path ended with radiance L: turn its training records into samples.
+// A guided path ended with radiance L: its training records become samples.
 // Record r holds the vertex, the sampled wi, the (L, T) of the path just after
 // the vertex (its emission added, its throughput factor applied) and cos / pdf
 // of wi, so the radiance that arrived along wi is L_i = (L_end - L_r) / T_r
@@ -806,68 +808,55 @@ RGR_DEV uint32_t mix32(uint32_t h) {  // murmur3 finaliser
 // combines with the BSDF (the network does not see the material).
 // Records are offered with the acceptance probability the last iteration set
 // (a hash of slot, record and iteration, not the path's RNG, so rendering is
-// unchanged) until `cap` samples are in.  Every lane of `active` calls it
-// (ending = its path ended and it records); the warp takes one atomic for the
-// sample count, one for the weight sum and one for the offered count.
-RGR_DEV void guide_emit_samples(const GuideRenderD& gd, uint32_t slot, f3 L, bool ending, unsigned active) {
+// unchanged) until `cap` samples are in.  guide_offer decides a lane's records;
+// the logic kernel gathers the counts per block (one atomic for the block's
+// samples, one for its offered count) and guide_write stores them.
+struct GuideOffer {
+    uint32_t take = 0;     // bit r: record r is accepted
+    uint32_t offered = 0;  // records with a positive, finite weight
+    float w[kGuideRecords] = {};
+};
+RGR_DEV void guide_offer(const GuideRenderD& gd, uint32_t slot, f3 L, bool ending, GuideOffer& o) {
     const GuideTrainD& tr = gd.train;
-    const int lane = threadIdx.x & 31;
     const uint32_t nr = ending ? min((uint32_t)gd.nrec[slot], (uint32_t)kGuideRecords) : 0u;
-    float w[kGuideRecords];
-    uint32_t take = 0, offered = 0;  // take: bit r = record r is accepted
-    if (nr) {
-        const float accept = *tr.accept;
-        const uint32_t it = *tr.iter;
-        for (uint32_t r = 0; r < (uint32_t)kGuideRecords; ++r) {
-            w[r] = 0.0f;
-            if (r >= nr) continue;
-            const float4* rec = gd.records + ((size_t)slot * kGuideRecords + r) * 5;
-            const float4 d = rec[3], e = rec[4];
-            const float lx = d.w > 0.0f ? (L.x - d.x) / d.w : 0.0f;
-            const float ly = e.x > 0.0f ? (L.y - d.y) / e.x : 0.0f;
-            const float lz = e.y > 0.0f ? (L.z - d.z) / e.y : 0.0f;
-            const float wr = (0.2126f * lx + 0.7152f * ly + 0.0722f * lz) * e.z;
-            if (!(wr > 0.0f) || !is_finite(wr)) continue;
-            ++offered;
-            const uint32_t h = mix32(slot * 0x9e3779b1u ^ (r + 1u) * 0x85ebca77u ^ (it + 1u) * 0xc2b2ae3du);
-            if ((float)(h >> 8) * (1.0f / 16777216.0f) >= accept) continue;
-            w[r] = wr;
-            take |= 1u << r;
-        }
+    if (!nr) return;
+    const float accept = *tr.accept;
+    const uint32_t it = *tr.iter;
+    for (uint32_t r = 0; r < (uint32_t)kGuideRecords; ++r) {
+        if (r >= nr) continue;
+        const float4* rec = gd.records + ((size_t)slot * kGuideRecords + r) * 5;
+        const float4 d = rec[3], e = rec[4];
+        const float lx = d.w > 0.0f ? (L.x - d.x) / d.w : 0.0f;
+        const float ly = e.x > 0.0f ? (L.y - d.y) / e.x : 0.0f;
+        const float lz = e.y > 0.0f ? (L.z - d.z) / e.y : 0.0f;
+        const float wr = (0.2126f * lx + 0.7152f * ly + 0.0722f * lz) * e.z;
+        if (!(wr > 0.0f) || !is_finite(wr)) continue;
+        ++o.offered;
+        const uint32_t h = mix32(slot * 0x9e3779b1u ^ (r + 1u) * 0x85ebca77u ^ (it + 1u) * 0xc2b2ae3du);
+        if ((float)(h >> 8) * (1.0f / 16777216.0f) >= accept) continue;
+        o.w[r] = wr;
+        o.take |= 1u << r;
     }
-    // exclusive prefix of the accepted counts (0..3: two ballots) over the
-    // active lanes, which need not be contiguous
-    const uint32_t mine = __popc(take);
-    const unsigned b0 = __ballot_sync(active, mine & 1u), b1 = __ballot_sync(active, (mine >> 1) & 1u);
-    const unsigned lt = (1u << lane) - 1u;
-    const uint32_t total = __popc(b0) + 2u * __popc(b1);
-    const int leader = __ffs(active) - 1;
-    uint32_t base = 0;
-    if (lane == leader && total) base = atomicAdd(tr.count, total);
-    base = __shfl_sync(active, base, leader);
-    uint32_t idx = base + __popc(b0 & lt) + 2u * __popc(b1 & lt);
+}
+// The accepted records of a lane as samples idx, idx + 1, ... (those below
+// the cap); returns the sum of their weights.
+RGR_DEV float guide_write(const GuideRenderD& gd, uint32_t slot, const GuideOffer& o, uint32_t idx) {
+    const GuideTrainD& tr = gd.train;
     float wsum = 0.0f;
     for (uint32_t r = 0; r < (uint32_t)kGuideRecords; ++r) {
-        if (!((take >> r) & 1u)) continue;
+        if (!((o.take >> r) & 1u)) continue;
         if (idx < tr.cap) {
             const float4* rec = gd.records + ((size_t)slot * kGuideRecords + r) * 5;
             float4* dst = reinterpret_cast<float4*>(tr.samples + 16 * (size_t)idx);
             dst[0] = rec[0];  // x, n.x
             dst[1] = rec[1];  // n.yz, wo.xy
             dst[2] = rec[2];  // wo.z, wi
-            dst[3] = make_float4(w[r], rec[4].w, 0.0f, 0.0f);  // weight, BSDF pdf of wi
-            wsum += w[r];
+            dst[3] = make_float4(o.w[r], rec[4].w, 0.0f, 0.0f);  // weight, BSDF pdf of wi
+            wsum += o.w[r];
         }
         ++idx;
     }
-    // the weight sum, gathered lane by lane (the active lanes are not contiguous)
-    float wtot = 0.0f;
-    for (unsigned m = active; m; m &= m - 1u) wtot += __shfl_sync(active, wsum, __ffs(m) - 1);
-    offered = __reduce_add_sync(active, offered);
-    if (lane == leader) {
-        if (wtot > 0.0f) atomicAdd(tr.wsum, wtot);
-        if (offered) atomicAdd(tr.candidates, (unsigned long long)offered);
-    }
+    return wsum;
 }
 
 // extension_ray_cast (extension_ray_cast_stackless.cl:202-246) of the slots
@@ -915,7 +904,8 @@ __global__ void __launch_bounds__(256, 5) k_trace_paths(PathsView P, QueueView Q
                     if (P.qid[r] != kQueueIdle) {
                         slot = r;
                         scp = &rp.reqs[P.req[r]].sc;
-                        const float4 ro4 = P.ro[r], rd4 = P.rd[r];
+                        float4 ro4, rd4;
+                        ld_sector<0>(P, r, ro4, rd4);
                         trace_begin(*scp, s, xyz(ro4), xyz(rd4), ro4.w);
                     }
                 }
@@ -946,36 +936,39 @@ __global__ void __launch_bounds__(256, 5) k_trace_paths(PathsView P, QueueView Q
 // cast the extension rays of this bounce; otherwise the thread traces first.
 template <bool kGuided, bool kPreTraced>
 RGR_DEV int logic_slot(const PathsView& P, const QueueView& Q, const RenderParams& rp, uint32_t slot,
-                       unsigned active) {
+                       unsigned active, GuideOffer& go) {
     const int req = P.req[slot];
     const RequestD& rq = rp.reqs[req];
     const SceneView& sc = rq.sc;
-    const float4 rd4 = P.rd[slot];
+    float4 ro4, rd4, ng4, rng4, T4, L4;
+    ld_sector<0>(P, slot, ro4, rd4);
+    if (kPreTraced) {  // the trace kernel wrote the hit; else loaded after the traversal
+        ld_sector<1>(P, slot, T4, L4);
+        ld_sector<2>(P, slot, ng4, rng4);
+    }
     f3 rd = xyz(rd4);
     int32_t hv = __float_as_int(rd4.w);
     uint32_t err = 0;
     int32_t hs;
     if (kPreTraced) {
-        hs = __float_as_int(P.ng[slot].w);
+        hs = __float_as_int(ng4.w);
     } else {
         // extension_ray_cast (extension_ray_cast_stackless.cl:202-246)
-        const float4 ro4 = P.ro[slot];
         f3 ro = xyz(ro4);
         float tmin = ro4.w;
         hs = trace_closest<false>(sc, ro, rd, tmin, nullptr, err);
+        ld_sector<1>(P, slot, T4, L4);
+        ld_sector<2>(P, slot, ng4, rng4);
         if (hs >= 0) {
-            f3 ng = hit_normal(sc, hs, ro, rd, tmin);
-            P.ng[slot] = f4(ng, __int_as_float(hs));
-            P.ro[slot] = f4(ro, tmin);
+            ng4 = f4(hit_normal(sc, hs, ro, rd, tmin), __int_as_float(hs));
             hv = -1;
-            P.rd[slot] = f4(rd, __int_as_float(-1));
+            st_sector<0>(P, slot, f4(ro, tmin), f4(rd, __int_as_float(-1)));
         }
     }
     // logic (logic.cl:27-190)
-    float4 T4 = P.T[slot], L4 = P.L[slot];
     f3 T = xyz(T4), L = xyz(L4);
     uint32_t logic_i = __float_as_uint(L4.w);
-    Rng rng = rng_load(P.rng, slot);
+    Rng rng = rng_of_bits(rng4);
     bool evalEnv = false, newPath = false;
     if (hs < 0 && hv < 0) {
         newPath = true;
@@ -1020,11 +1013,10 @@ RGR_DEV int logic_slot(const PathsView& P, const QueueView& Q, const RenderParam
         !(rp.sample_limit != 0ull && *Q.next_pixel >= rp.sample_limit)) {
         const float cl = rq.radiance_clamp;
         const bool kept = is_finite(L.x) && is_finite(L.y) && is_finite(L.z) && L.x < cl && L.y < cl && L.z < cl;
-        guide_emit_samples(rp.gd, slot, L, newPath && kept, active);
+        guide_offer(rp.gd, slot, L, newPath && kept, go);
     }
-    P.T[slot] = f4(T, T4.w);
-    P.L[slot] = f4(L, __uint_as_float(logic_i + 1));
-    rng_store(P.rng, slot, rng);
+    st_sector<1>(P, slot, f4(T, T4.w), f4(L, __uint_as_float(logic_i + 1)));
+    st_sector<2>(P, slot, ng4, rng_bits(rng));
     int q;
     if (newPath) {
         q = 0;
@@ -1065,33 +1057,59 @@ RGR_DEV int logic_slot(const PathsView& P, const QueueView& Q, const RenderParam
 constexpr int kLogicThreads = 256;
 template <bool kGuided, bool kPreTraced>
 __global__ void __launch_bounds__(kLogicThreads) k_trace_logic(PathsView P, QueueView Q, RenderParams rp) {
+    const unsigned full = 0xffffffffu;
     __shared__ uint32_t s_q[kNumQueues];  // items per queue, then the block's base in it
+    __shared__ uint32_t s_samples, s_offered;  // guided recording: accepted samples (then their base), offered
     if (threadIdx.x < kNumQueues) s_q[threadIdx.x] = 0;
+    if (kGuided && threadIdx.x == 32) s_samples = s_offered = 0u;
     const int lane = threadIdx.x & 31;
+    const unsigned lt = (1u << lane) - 1u;
     const uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x;
     const bool live = slot < P.n && P.qid[slot] != kQueueIdle;
-    const unsigned active = __ballot_sync(0xffffffffu, live);
+    const unsigned active = __ballot_sync(full, live);
     int q = 0;
-    if (live) q = logic_slot<kGuided, kPreTraced>(P, Q, rp, slot, active);
+    GuideOffer go;
+    if (live) q = logic_slot<kGuided, kPreTraced>(P, Q, rp, slot, active, go);
     const bool mat = live && q != 0;
-    const unsigned matmask = __ballot_sync(0xffffffffu, mat);
-    __syncthreads();  // s_q cleared
+    const unsigned matmask = __ballot_sync(full, mat);
+    __syncthreads();  // s_q, s_samples, s_offered cleared
     uint32_t off = 0;
     if (mat) {
         const unsigned peers = __match_any_sync(matmask, q);
         const int leader = __ffs(peers) - 1;
         uint32_t base = 0;
         if (lane == leader) base = atomicAdd(&s_q[q], (uint32_t)__popc(peers));
-        off = __shfl_sync(peers, base, leader) + __popc(peers & ((1u << lane) - 1u));
+        off = __shfl_sync(peers, base, leader) + __popc(peers & lt);
+    }
+    uint32_t sidx = 0;  // this lane's first sample within the block's
+    if (kGuided) {
+        // exclusive prefix of the accepted counts (0..3: two ballots)
+        const uint32_t mine = __popc(go.take);
+        const unsigned b0 = __ballot_sync(full, mine & 1u), b1 = __ballot_sync(full, (mine >> 1) & 1u);
+        const uint32_t wtot = __popc(b0) + 2u * __popc(b1);
+        const uint32_t offered = __reduce_add_sync(full, go.offered);
+        uint32_t wbase = 0;
+        if (lane == 0 && wtot) wbase = atomicAdd(&s_samples, wtot);
+        if (lane == 0 && offered) atomicAdd(&s_offered, offered);
+        sidx = __shfl_sync(full, wbase, 0) + __popc(b0 & lt) + 2u * __popc(b1 & lt);
     }
     const int nlive = __syncthreads_count(live);
     if (threadIdx.x < kNumQueues) {
         const uint32_t n = s_q[threadIdx.x];
         if (n) s_q[threadIdx.x] = atomicAdd(Q.counts + threadIdx.x, n);
     }
+    if (kGuided && threadIdx.x == 32) {
+        if (s_samples) s_samples = atomicAdd(rp.gd.train.count, s_samples);
+        if (s_offered) atomicAdd(rp.gd.train.candidates, (unsigned long long)s_offered);
+    }
     if (threadIdx.x == 0 && nlive) atomicAdd(rp.rays, (unsigned long long)nlive);
     __syncthreads();
     if (mat) queue_items(Q, q)[s_q[q] + off] = slot;
+    if (kGuided && __any_sync(full, go.take != 0u)) {
+        float ws = go.take ? guide_write(rp.gd, slot, go, s_samples + sidx) : 0.0f;
+        for (int o = 16; o > 0; o >>= 1) ws += __shfl_xor_sync(full, ws, o);
+        if (lane == 0 && ws > 0.0f) atomicAdd(rp.gd.train.wsum, ws);
+    }
 }
 
 // The completion time of each request whose paths have all finished, stamped

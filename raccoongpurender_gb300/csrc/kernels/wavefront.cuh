@@ -56,6 +56,32 @@ struct PathsView {
     }
 };
 
+// The two vectors of a slot's 32-byte sector kSector (fields 2 kSector and
+// 2 kSector + 1) in one 32-byte access (sm_100 and later): a warp over
+// consecutive slots then makes one request per sector instead of two, and a
+// store writes the whole sector.
+template <int kSector>
+__device__ __forceinline__ void ld_sector(const PathsView& P, uint32_t slot, float4& a, float4& b) {
+    const float4* p = P.ro.base + (size_t)slot * kSlotVecs + 2 * kSector;
+    asm("ld.global.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+        : "=f"(a.x), "=f"(a.y), "=f"(a.z), "=f"(a.w), "=f"(b.x), "=f"(b.y), "=f"(b.z), "=f"(b.w)
+        : "l"(p)
+        : "memory");
+}
+template <int kSector>
+__device__ __forceinline__ void st_sector(const PathsView& P, uint32_t slot, const float4& a, const float4& b) {
+    float4* p = P.ro.base + (size_t)slot * kSlotVecs + 2 * kSector;
+    asm volatile("st.global.v8.f32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8};" ::"l"(p), "f"(a.x), "f"(a.y), "f"(a.z),
+                 "f"(a.w), "f"(b.x), "f"(b.y), "f"(b.z), "f"(b.w)
+                 : "memory");
+}
+__device__ __forceinline__ float4 rng_bits(const Rng& r) {
+    return make_float4(__uint_as_float(r.s0), __uint_as_float(r.s1), __uint_as_float(r.s2), __uint_as_float(r.s3));
+}
+__device__ __forceinline__ Rng rng_of_bits(const float4& v) {
+    return Rng{__float_as_uint(v.x), __float_as_uint(v.y), __float_as_uint(v.z), __float_as_uint(v.w)};
+}
+
 struct QueueView {
     uint32_t* items[kNumQueues];
     uint32_t* counts;               // [kNumQueues]

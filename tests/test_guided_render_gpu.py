@@ -53,7 +53,12 @@ def test_guided_is_unbiased(rg, which):
     hist = g.loss_history()
     assert np.isfinite(hist).all()
     plain = guiding.render_mean(rg, sm, cam, spp=512, seed_offset=1, path_count=1 << 18)
-    guided = guiding.render_mean(rg, sm, cam, spp=512, seed_offset=1, path_count=1 << 18, guide=g)
+    # the guided image over four seeds: on the mixed scene a guided render's error is
+    # heavy-tailed (a sun caustic found by BSDF sampling weighs up to 1 / (1 - share)
+    # times its plain weight), and one such sample can move a block by several percent
+    g.set_config(train=0)
+    guided = np.mean([guiding.render_mean(rg, sm, cam, spp=512, seed_offset=1 + k * (1 << 18), path_count=1 << 18,
+                                          guide=g) for k in range(4)], axis=0)
     m = ref.mean()
     print(f"{which}: mean ref {m:.5f} plain {plain.mean():.5f} guided {guided.mean():.5f}; relMSE plain "
           f"{guiding.relmse(plain, ref):.5f} guided {guiding.relmse(guided, ref):.5f}")
