@@ -10,9 +10,12 @@
 //      order, new_path / strategy_selection / envmap sample / BSDF sample or
 //      pdf / envmap pdf / material stage / homogeneous_volume_through, keeping
 //      IncidentSample and ShadingResult in registers;
-//   3. trace_logic  — closest-hit traversal fused with logic.cl: throughput
-//      update, envmap on miss, Russian roulette, FP64 per-pixel accumulation,
-//      and warp-aggregated enqueue into next step's material queues.
+//   3. trace_logic  — logic.cl after the bounce's closest hits (cast by the
+//      persistent trace kernel, or fused for small scenes): throughput update,
+//      envmap on miss, Russian roulette, FP64 per-pixel accumulation, and the
+//      appends to the next step's material queues, aggregated per warp
+//      (match_any) and per block (shared-memory counts, one global atomic per
+//      queue per block).
 // Every slot's arithmetic is the reference kernels' arithmetic (see the
 // file:line notes); the translation unit is built with --fmad=false.
 #include <cuda_fp16.h>
@@ -776,18 +779,6 @@ __global__ void __launch_bounds__(256) k_guide_select(PathsView P, QueueView Q, 
             if (take) gd.sel[row] = slot;
         }
     }
-}
-
-// warp-aggregated append of `slot` to queue q (one atomic per distinct queue per warp)
-RGR_DEV void enqueue(const QueueView& Q, int q, uint32_t slot, unsigned active) {
-    unsigned peers = __match_any_sync(active, q);
-    int leader = __ffs(peers) - 1;
-    int lane = threadIdx.x & 31;
-    uint32_t base = 0;
-    if (lane == leader) base = atomicAdd(Q.counts + q, (uint32_t)__popc(peers));
-    base = __shfl_sync(peers, base, leader);
-    uint32_t rank = __popc(peers & ((1u << lane) - 1u));
-    queue_items(Q, q)[base + rank] = slot;
 }
 
 RGR_DEV uint32_t mix32(uint32_t h) {  // murmur3 finaliser
