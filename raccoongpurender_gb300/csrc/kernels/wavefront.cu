@@ -738,13 +738,17 @@ __device__ __forceinline__ void shade_items(const PathsView& P, const QueueView&
 }
 
 // The plain and guided shading kernels: one queue item per thread, all
-// queues in one launch.  Their launch bounds differ: the plain kernel's
-// registers are left to the compiler, the guided one is held to
-// RGR_SHADE_GUIDED_MIN_BLOCKS resident blocks per SM.
-#ifndef RGR_SHADE_GUIDED_MIN_BLOCKS
-#define RGR_SHADE_GUIDED_MIN_BLOCKS 3
+// queues in one launch, held to 4 resident 256-thread blocks per SM (64
+// registers, a few spilled: the mixed 1080p render 1370 against 1347 Mpaths/s
+// with the compiler's 78 registers and 3 blocks; the guided render 1.6 %
+// faster than at 3 blocks and 80 registers).
+#ifndef RGR_SHADE_MIN_BLOCKS
+#define RGR_SHADE_MIN_BLOCKS 4
 #endif
-__global__ void __launch_bounds__(256) k_shade(PathsView P, QueueView Q, RenderParams rp) {
+#ifndef RGR_SHADE_GUIDED_MIN_BLOCKS
+#define RGR_SHADE_GUIDED_MIN_BLOCKS 4
+#endif
+__global__ void __launch_bounds__(256, RGR_SHADE_MIN_BLOCKS) k_shade(PathsView P, QueueView Q, RenderParams rp) {
     shade_items<false>(P, Q, rp);
 }
 __global__ void __launch_bounds__(256, RGR_SHADE_GUIDED_MIN_BLOCKS) k_shade_guided(PathsView P, QueueView Q,
@@ -1047,7 +1051,10 @@ RGR_DEV int logic_slot(const PathsView& P, const QueueView& Q, const RenderParam
 // the same few counters.
 constexpr int kLogicThreads = 256;
 template <bool kGuided, bool kPreTraced>
-__global__ void __launch_bounds__(kLogicThreads) k_trace_logic(PathsView P, QueueView Q, RenderParams rp) {
+// latency-bound: 6 resident blocks per SM for the logic alone (40 registers; the
+// render 0.6 % faster than at 5), 5 while it records guide samples, 4 with the
+// traversal fused in
+__global__ void __launch_bounds__(kLogicThreads, kPreTraced ? (kGuided ? 5 : 6) : 4) k_trace_logic(PathsView P, QueueView Q, RenderParams rp) {
     const unsigned full = 0xffffffffu;
     __shared__ uint32_t s_q[kNumQueues];  // items per queue, then the block's base in it
     __shared__ uint32_t s_samples, s_offered;  // guided recording: accepted samples (then their base), offered
