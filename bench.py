@@ -747,15 +747,28 @@ def main() -> None:
     sptr = stream.cuda_stream
     assert sptr != 0
 
-    def step():
-        for soa, prim, t, n in sets:
-            lane.trace_closest_device([a.data_ptr() for a in soa], n, prim.data_ptr(), t.data_ptr(), 0, sptr)
-
-    # launch shape and BVH staging depth from the autotuner (results do not depend on them)
+    # launch shape and BVH staging depth from the autotuner, for each ray set (coherent
+    # rays prefer fewer refills than incoherent ones); results do not depend on them
     from raccoongpurender_gb300 import autotune
-    trace_tuned, trace_trials = autotune.tune_trace(
-        lane, [([a.data_ptr() for a in soa], n, prim.data_ptr(), t.data_ptr()) for soa, prim, t, n in sets], sptr,
-        device=local, log=lambda *_: None)
+    set_names = ("coherent", "incoherent")
+    trace_tuned, trace_trials = {}, []
+    for name, (soa, prim, t, n) in zip(set_names, sets):
+        tuned_k, trials_k = autotune.tune_trace(lane, [([a.data_ptr() for a in soa], n, prim.data_ptr(),
+                                                        t.data_ptr())], sptr, device=local, log=lambda *_: None)
+        trace_tuned[name] = tuned_k
+        trace_trials += [dict(t_["params"], set=name, ms=round(t_["seconds"] * 1e3, 3)) for t_ in trials_k]
+
+    def shape(k):
+        """The launch shape tuned for ray set k (host-side settings, no device work)."""
+        p = trace_tuned[set_names[k]]
+        lane.set_trace_staging(p["trace_stage"])
+        lane.set_trace_tuning(p["trace_refill"], 0)
+        lane.set_trace_search(p["trace_search"], 0)
+
+    def step():
+        for k, (soa, prim, t, n) in enumerate(sets):
+            shape(k)
+            lane.trace_closest_device([a.data_ptr() for a in soa], n, prim.data_ptr(), t.data_ptr(), 0, sptr)
 
     # algorithmic traffic: exact node visits and primitive tests per ray
     counts = []
@@ -786,9 +799,11 @@ def main() -> None:
         for k in range(args.steps):
             ev[k][0].record(stream)
             soa, prim, t, n = sets[0]
+            shape(0)
             lane.trace_closest_device([a.data_ptr() for a in soa], n, prim.data_ptr(), t.data_ptr(), 0, sptr)
             ev[k][1].record(stream)
             soa, prim, t, n = sets[1]
+            shape(1)
             lane.trace_closest_device([a.data_ptr() for a in soa], n, prim.data_ptr(), t.data_ptr(), 0, sptr)
             ev[k][2].record(stream)
         t_end.record(stream)
@@ -830,7 +845,12 @@ def main() -> None:
         return (time.perf_counter() - t0) / args.e2e_steps
 
     # the default: the traversal kernel reads the pinned rays and writes the hits
-    # across the CPU-GPU link itself; for comparison, staged copies through device buffers
+    # across the CPU-GPU link itself (its warps refill only when all lanes are idle,
+    # so the shapes tuned for rays in device memory do not apply: the library's
+    # default leaf batching); for comparison, staged copies through device buffers
+    lane.set_trace_staging(0)
+    lane.set_trace_tuning(24, 0)
+    lane.set_trace_search(8, 0)
     lane.set_trace_host_mode(rg.TRACE_HOST_COPY)
     e2e_staged = rays_per_step / e2e_time() / 1e6
     lane.set_trace_host_mode(rg.TRACE_HOST_AUTO)
@@ -903,8 +923,7 @@ def main() -> None:
                                    "depth": int(info.depth), "build_s": round(build_s, 2)},
                            "l2": "inputs larger than L2 (224 MB of rays per step)",
                            "autotuned": trace_tuned,
-                           "autotune_trials": [dict(t["params"], ms=round(t["seconds"] * 1e3, 3))
-                                               for t in trace_trials],
+                           "autotune_trials": trace_trials,
                            "parallelism": f"replicas{world}"},
                 "e2e": {"value": round(e2e_value, 1), "unit": "Mrays/s", "h2d_bytes_per_step": rays_per_step * 28,
                         "d2h_bytes_per_step": rays_per_step * 8,
