@@ -198,8 +198,8 @@ def render_bench(dev_index: int, which: str, repeats: int = 2, pools=(1 << 22,))
             "config": f"{camd['w']}x{camd['h']}, {spp} spp, max depth {depth}, {mesh.ntris} triangles"}
 
 
-# Algorithmic bytes per extension segment of the wavefront render in this
-# library's structure-of-arrays layout (16-byte vectors per slot), traversal
+# Algorithmic bytes per extension segment of the wavefront render (the state
+# each stage uses, in 16-byte vectors of the slot records), traversal
 # excluded.  Per shaded queue item: the item (4), request id (2), material
 # reference (8), ro, rd, T, L, ng and RNG in (6 x 16) and out (6 x 16), the
 # volume list in (32); the persistent trace: the item (4), ro and rd in (32),
@@ -211,7 +211,7 @@ RENDER_STATE_BYTES = (4 + 2 + 8 + 96 + 96 + 32) + (4 + 32 + 24) + (1 + 2 + 80 + 
 
 def render_roofline(dev_index: int, mrays_s: float, mpaths_s: float, l2_gbs: float, hbm_gbs: float) -> dict:
     """Roofline of the mixed 1080p render: bytes per extension segment = the
-    path-state traffic of the SoA layout (RENDER_STATE_BYTES) + 64 per BVH
+    path-state traffic the stages use (RENDER_STATE_BYTES) + 64 per BVH
     node visited + 48 per primitive tested, the counts measured by the
     instrumented closest-hit kernel on the extension rays of the render's
     third bounce (2^22 resident paths).  The state streams from HBM, the tree
