@@ -761,6 +761,7 @@ def main() -> None:
     def shape(k):
         """The launch shape tuned for ray set k (host-side settings, no device work)."""
         p = trace_tuned[set_names[k]]
+        lane.set_trace_reorder(p.get("trace_reorder", 0))
         lane.set_trace_staging(p["trace_stage"])
         lane.set_trace_tuning(p["trace_refill"], 0)
         lane.set_trace_search(p["trace_search"], 0)
@@ -848,6 +849,7 @@ def main() -> None:
     # across the CPU-GPU link itself (its warps refill only when all lanes are idle,
     # so the shapes tuned for rays in device memory do not apply: the library's
     # default leaf batching); for comparison, staged copies through device buffers
+    lane.set_trace_reorder(0)
     lane.set_trace_staging(0)
     lane.set_trace_tuning(24, 0)
     lane.set_trace_search(8, 0)

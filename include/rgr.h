@@ -352,6 +352,15 @@ int rgr_set_trace_search(rgr_context* c, int32_t closest, int32_t render);
    0 = off.  Chosen by the autotuner. */
 int rgr_set_trace_staging(rgr_context* c, uint32_t staged_nodes);
 
+/* Ray reordering of rgr_trace_closest_device (no counterpart in the
+   reference): reorder = 1 sorts the rays by a 16-bit key of their origin and
+   direction before the traversal (a counting sort on the device, 32 bytes of
+   scratch per ray), so that a warp's rays walk similar paths through the
+   tree; it pays for incoherent rays and costs more than it saves on coherent
+   ones (camera rays).  0 = off (default).  Results are identical either way;
+   the order only changes the schedule.  Chosen by the autotuner. */
+int rgr_set_trace_reorder(rgr_context* c, int32_t reorder);
+
 /* ---- learned path guiding (no counterpart in the reference) --------------
    A small MLP maps a shading vertex (frequency-encoded position, normal and
    outgoing direction: 36 inputs) through 4 hidden layers of 64 (ReLU) to an

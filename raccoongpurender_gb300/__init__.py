@@ -170,6 +170,7 @@ _SIGS = {
     "rgr_set_trace_host_mode": (C.c_int, [C.c_void_p, C.c_int32]),
     "rgr_set_render_trace": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32]),
     "rgr_set_trace_search": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32]),
+    "rgr_set_trace_reorder": (C.c_int, [C.c_void_p, C.c_int32]),
     "rgr_set_render_tuning": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32]),
     "rgr_batch_create": (C.c_int, [C.c_void_p, C.c_int32, C.c_uint32]),
     "rgr_batch_destroy": (None, [C.c_void_p]),
@@ -616,6 +617,12 @@ class WavefrontLane:
     def set_trace_staging(self, staged_nodes: int) -> None:
         """Top BVH nodes each traversal CTA keeps in shared memory (0 = off)."""
         _check(self._lib.rgr_set_trace_staging(self._h, staged_nodes), "rgr_set_trace_staging")
+
+    def set_trace_reorder(self, reorder: int) -> None:
+        """trace_closest_device sorts the rays by origin and direction before the
+        traversal (1) or takes them in the given order (0, default).  Results are
+        identical; sorting pays for incoherent rays."""
+        _check(self._lib.rgr_set_trace_reorder(self._h, reorder), "rgr_set_trace_reorder")
 
     def trace_closest_counts_device(self, soa_ptrs, n: int, prim_ptr: int, t_ptr: int, nodes_ptr: int,
                                     prims_ptr: int, stream: int = 0) -> None:

@@ -31,8 +31,10 @@ from pathlib import Path
 DEFAULTS = dict(path_count=1 << 22, graph_steps=8, shade_blocks=8, render_refill=12, render_search=8)
 CANDIDATES = dict(path_count=[1 << 20, 1 << 21, 1 << 22, 1 << 23, 1 << 24], graph_steps=[4, 8, 16], shade_blocks=[4, 8, 16],
                   render_refill=[8, 16, 24], render_search=[4, 12, 16])
-TRACE_DEFAULTS = dict(trace_refill=24, trace_search=8, trace_stage=0)
-TRACE_CANDIDATES = dict(trace_refill=[8, 16, 32], trace_search=[4, 12, 16], trace_stage=[0, 64, 256, 1024])
+TRACE_DEFAULTS = dict(trace_reorder=0, trace_refill=24, trace_search=8, trace_stage=0)
+# ray reordering first: the launch shape is then tuned for the rays in the order they are traced
+TRACE_CANDIDATES = dict(trace_reorder=[1], trace_refill=[8, 16, 32], trace_search=[4, 12, 16],
+                        trace_stage=[0, 64, 256, 1024])
 
 
 def _gpu_name(device: int) -> str:
@@ -124,8 +126,9 @@ def tune_batch(scenes_and_requests, device: int = 0, spp_cap: int = 4, use_cache
 
 def tune_trace(lane, ray_sets, stream: int, device: int = 0, reps: int = 3, use_cache: bool = False,
                log=print) -> tuple[dict, list]:
-    """Tune the closest-hit kernel (refill threshold, BVH staging depth) on
-    `ray_sets`, a list of (7 device pointers, n, prim pointer, t pointer), by
+    """Tune the closest-hit kernel (ray reordering, refill threshold, leaf
+    batching, BVH staging depth) on `ray_sets`, a list of (7 device pointers,
+    n, prim pointer, t pointer), by
     timing `reps` passes over all sets with CUDA events on `stream`.  Applies
     the best to `lane`; returns (params, trials)."""
     import torch
@@ -134,6 +137,7 @@ def tune_trace(lane, ray_sets, stream: int, device: int = 0, reps: int = 3, use_
     st = torch.cuda.ExternalStream(stream)
 
     def run(p):
+        lane.set_trace_reorder(p["trace_reorder"])
         lane.set_trace_staging(p["trace_stage"])
         lane.set_trace_tuning(p["trace_refill"], 0)
         lane.set_trace_search(p["trace_search"], 0)
@@ -150,6 +154,7 @@ def tune_trace(lane, ray_sets, stream: int, device: int = 0, reps: int = 3, use_
 
     tuner = Autotuner(device, log=log)
     best = tuner.tune(sig, run, use_cache=use_cache, defaults=TRACE_DEFAULTS, candidates=TRACE_CANDIDATES)
+    lane.set_trace_reorder(best.get("trace_reorder", 0))
     lane.set_trace_staging(best["trace_stage"])
     lane.set_trace_tuning(best["trace_refill"], 0)
     lane.set_trace_search(best["trace_search"], 0)

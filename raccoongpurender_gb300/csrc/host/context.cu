@@ -203,6 +203,9 @@ struct rgr_context {
     TraceShape render_trace{true, 12, 8, 0, nullptr};
     int render_trace_mode = -1;  // 1 persistent, 0 fused, -1 by scene size at render begin
     uint32_t trace_stage = 0;  // top BVH nodes staged in shared memory per CTA
+    int trace_reorder = 0;     // rgr_trace_closest_device sorts the rays first
+    int packed_grid = 0;       // its traversal grid (no staged nodes)
+    DevBuf tbins, tpacked;     // its bucket counts and the reordered 32-byte records
     // learned path guiding: the attached network and this render's per-slot buffers
     rgr_guide* guide = nullptr;
     bool guided = false;      // the current render uses `guide`
@@ -467,6 +470,7 @@ int rgr_context_create(rgr_context** out, int32_t device, uint32_t path_count) {
     }
     cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device);
     c->trace_grid = c->num_sms * std::max(1, trace_rays_max_blocks_per_sm());
+    c->packed_grid = c->trace_grid;
     c->render_trace.grid = c->num_sms * std::max(1, trace_paths_max_blocks_per_sm());
     c->npaths = path_count;
     c->ntiles = (path_count + kTile - 1) / kTile;
@@ -763,6 +767,31 @@ int rgr_trace_closest_device(rgr_context* c, const rgr_ray_soa* rays, uint64_t n
     int r = c->err.alloc(16);
     if (r != RGR_OK) return r;
     if ((r = c->tcounter.alloc(8)) != RGR_OK) return r;
+    if (c->trace_reorder && n < (1ull << 32)) {
+        if ((r = c->tbins.alloc(2 * sizeof(uint32_t) * kRayBins)) != RGR_OK) return r;
+        if ((r = c->tpacked.alloc(32 * (size_t)n)) != RGR_OK) return r;
+        // the key's boxes: the scene's, and for the point half its diagonal along
+        // the ray the same box widened by that reach
+        RayKeyBox kb;
+        const float* b = c->scene_bounds;
+        float d2 = 0.0f;
+        for (int k = 0; k < 3; ++k) d2 += (b[3 + k] - b[k]) * (b[3 + k] - b[k]);
+        kb.reach = 0.5f * std::sqrt(d2);
+        for (int k = 0; k < 3; ++k) {
+            const float e = b[3 + k] - b[k];
+            kb.lo[k] = b[k];
+            kb.scale[k] = e > 0.0f ? 8.0f / e : 0.0f;
+            kb.lo_far[k] = b[k] - kb.reach;
+            kb.scale_far[k] = e + 2.0f * kb.reach > 0.0f ? 8.0f / (e + 2.0f * kb.reach) : 0.0f;
+        }
+        launch_ray_reorder(rays->ox, rays->oy, rays->oz, rays->dx, rays->dy, rays->dz, rays->tmax, n, kb,
+                           c->tbins.as<uint32_t>(), c->tpacked.as<float4>(), c->num_sms * 64, st);
+        launch_trace_packed(c->scene.sv, c->tpacked.as<float4>(), n, prim, t, ng_xyz, c->err.as<uint32_t>(),
+                            c->tcounter.as<unsigned long long>(), c->trace_refill, c->trace_search, c->packed_grid,
+                            st);
+        RGR_CUDA(cudaGetLastError());
+        return RGR_OK;
+    }
     launch_trace_rays(c->scene.sv, rays->ox, rays->oy, rays->oz, rays->dx, rays->dy, rays->dz, rays->tmax, n, prim, t, ng_xyz,
                       c->err.as<uint32_t>(), c->tcounter.as<unsigned long long>(), c->trace_refill, c->trace_search,
                       c->trace_grid, c->trace_stage, st);
@@ -797,6 +826,8 @@ int rgr_set_trace_tuning(rgr_context* c, int32_t refill, int32_t blocks_per_sm) 
     c->trace_refill = refill;
     c->trace_blocks = blocks_per_sm;
     c->trace_grid = c->num_sms * (blocks_per_sm ? blocks_per_sm : maxb);
+    const int maxb0 = std::max(1, trace_rays_max_blocks_per_sm(0));
+    c->packed_grid = c->num_sms * (blocks_per_sm ? std::min(blocks_per_sm, maxb0) : maxb0);
     return RGR_OK;
 }
 
@@ -823,6 +854,12 @@ int rgr_set_trace_search(rgr_context* c, int32_t closest, int32_t render) {
 int rgr_set_trace_host_mode(rgr_context* c, int32_t mode) {
     if (!c || (mode != RGR_TRACE_HOST_AUTO && mode != RGR_TRACE_HOST_COPY)) return RGR_E_INVALID;
     c->trace_host_mode = mode;
+    return RGR_OK;
+}
+
+int rgr_set_trace_reorder(rgr_context* c, int32_t reorder) {
+    if (!c || reorder < 0 || reorder > 1) return RGR_E_INVALID;
+    c->trace_reorder = reorder;
     return RGR_OK;
 }
 

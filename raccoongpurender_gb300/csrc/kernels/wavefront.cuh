@@ -265,6 +265,24 @@ void launch_trace_rays_counts(const SceneView& sc, const float* ox, const float*
                               int grid, cudaStream_t st);
 // resident 256-thread blocks per SM of the closest-hit kernel with `stage` staged nodes
 int trace_rays_max_blocks_per_sm(uint32_t stage = 0);
+// Ray reordering: a 16-bit key per ray from its origin and the point `reach`
+// along it, each quantised to 3 bits per axis: (x - lo) * scale in [0, 8)
+constexpr int kRayKeyBits = 16;
+constexpr uint32_t kRayBins = 1u << kRayKeyBits;
+struct RayKeyBox {
+    float lo[3], scale[3];          // the origin's box
+    float lo_far[3], scale_far[3];  // the far point's box
+    float reach;
+};
+// counting sort of n < 2^32 rays into `packed` (32 bytes per ray); bins: 2 x kRayBins
+// words (counts, cursors); grid: the most blocks of the key passes
+void launch_ray_reorder(const float* ox, const float* oy, const float* oz, const float* dx, const float* dy,
+                        const float* dz, const float* tmax, uint64_t n, const RayKeyBox& kb, uint32_t* bins,
+                        float4* packed, int grid, cudaStream_t st);
+// closest hit of reordered records; hits written at each record's ray index
+void launch_trace_packed(const SceneView& sc, const float4* packed, uint64_t n, int32_t* prim, float* t, float* ng,
+                         uint32_t* err, unsigned long long* counter, int refill, int search, int grid,
+                         cudaStream_t st);
 
 }  // namespace dev
 }  // namespace rgr

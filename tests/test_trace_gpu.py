@@ -106,6 +106,57 @@ def test_leaf_batching(rg, po, search, refill):
         assert (bits(t.cpu().numpy()) == bits(ot)).all()
 
 
+def _device_hits(lane, rays):
+    import torch
+    dev = torch.device("cuda", 0)
+    soa = [torch.from_numpy(np.ascontiguousarray(a)).to(dev) for a in rays.soa()]
+    prim = torch.full((len(rays),), -7, dtype=torch.int32, device=dev)
+    t = torch.zeros(len(rays), dtype=torch.float32, device=dev)
+    torch.cuda.synchronize()  # the context stream does not wait for torch's stream
+    lane.trace_closest_device([a.data_ptr() for a in soa], len(rays), prim.data_ptr(), t.data_ptr(), 0, 0)
+    lane.synchronize()
+    return prim.cpu().numpy(), t.cpu().numpy()
+
+
+@pytest.mark.parametrize("n", [1, 31, 33, 4097, 65537])
+def test_ray_reorder(rg, po, n):
+    """Rays sorted by origin and direction before the traversal: every ray's
+    hit is the oracle's, written at its own index, for ragged counts, rays
+    starting outside the scene's box (their key coordinates clamp), camera
+    rays (many share a key) and zero or non-finite directions."""
+    mesh = scenes.displaced_icosphere(6, seed=7)
+    sm, osc = build(mesh)
+    lane = rg.WavefrontLane(0, 1024)
+    lane.setup(sm)
+    lane.set_trace_reorder(1)
+    prim_rays, _ = scenes.closest_hit_rays(mesh, res=128, n_random=16, seed=6)
+    far = scenes.random_rays(n, (-4.0, -4.0, -4.0), (4.0, 4.0, 4.0), seed=n)
+    o = np.concatenate([far.o, prim_rays.o[: 2 * n]])
+    d = np.concatenate([far.d, prim_rays.d[: 2 * n]])
+    d[::97] = 0.0
+    d[5::101, 1] = np.inf
+    tmax = np.concatenate([far.tmax, prim_rays.tmax[: 2 * n]])
+    tmax[::7] = 0.75
+    rays = scenes.Rays(o.astype(np.float32), d.astype(np.float32), tmax.astype(np.float32))
+    prim, t = _device_hits(lane, rays)
+    oprim, ot, _ = osc.trace(rays.packed8(), threads=16)
+    assert (prim == oprim).all(), f"{(prim != oprim).sum()} prim mismatches"
+    # an infinite direction can give a hit at t = NaN, whose bits are the
+    # platform's default NaN on the host: any NaN matches any NaN
+    same = (bits(t) == bits(ot)) | (np.isnan(t) & np.isnan(ot))
+    assert same.all(), f"{(~same).sum()} t mismatches"
+    lane.set_trace_reorder(0)
+    p0, t0 = _device_hits(lane, rays)
+    assert (p0 == prim).all() and (bits(t0) == bits(t)).all()
+
+
+def test_ray_reorder_range(rg):
+    lane = rg.WavefrontLane(0, 1024)
+    for bad in (-1, 2):
+        with pytest.raises(RuntimeError):
+            lane.set_trace_reorder(bad)
+
+
 def test_trace_search_range(rg):
     lane = rg.WavefrontLane(0, 1024)
     for bad in ((-1, 8), (33, 8), (8, 33), (8, -1)):
@@ -191,7 +242,8 @@ def test_headline_scale_level8(rg, po):
     displaced icosphere with its SAH tree (leaves of at most 4), and every
     16th ray of the 2048x2048 coherent and the 4M incoherent ray sets
     (262,144 of each), traced through the host entry point and through the
-    device entry point with the autotuned refill threshold."""
+    device entry point with the autotuned refill threshold, the rays in their
+    own order and sorted by origin and direction."""
     import torch
     mesh = scenes.displaced_icosphere(8, seed=7)
     assert mesh.ntris == 1310720
@@ -208,8 +260,12 @@ def test_headline_scale_level8(rg, po):
         dprim = torch.empty(len(rays), dtype=torch.int32, device="cuda")
         dt = torch.empty(len(rays), dtype=torch.float32, device="cuda")
         lane.set_trace_tuning(refill=24)
-        lane.trace_closest_device([a.data_ptr() for a in soa], len(rays), dprim.data_ptr(), dt.data_ptr())
-        lane.synchronize()
-        assert (dprim.cpu().numpy() == p).all()
         oprim, ot, _ = osc.trace(rays.packed8(), threads=16, normals=False)
-        assert (bits(dt.cpu().numpy()) == bits(ot)).all()
+        for reorder in (0, 1):
+            lane.set_trace_reorder(reorder)
+            dprim.fill_(-7)
+            lane.trace_closest_device([a.data_ptr() for a in soa], len(rays), dprim.data_ptr(), dt.data_ptr())
+            lane.synchronize()
+            assert (dprim.cpu().numpy() == p).all()
+            assert (bits(dt.cpu().numpy()) == bits(ot)).all()
+        lane.set_trace_reorder(0)
