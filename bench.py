@@ -123,16 +123,19 @@ def build_workload(level: int = 8, res: int = 2048):
     return mesh, sm, coherent, incoherent, build_s
 
 
-def closest_hit_once(dev_index: int = 0) -> None:
+def closest_hit_once(dev_index: int = 0, reorder: int = 0) -> None:
     """One launch of the closest-hit kernel per ray set of the workload above
     (coherent, then incoherent) with the library's default launch shape, rays
-    in device memory: the command the kernel's ncu captures run."""
+    in device memory: the command the kernel's ncu captures run.  reorder = 1
+    sorts each set by origin and direction first (three more launches per
+    set: the key histogram, its scan and the scatter)."""
     import torch
 
     import raccoongpurender_gb300 as rg
     mesh, sm, coherent, incoherent, _ = build_workload()
     lane = rg.WavefrontLane(dev_index, 1024)
     lane.setup(sm)
+    lane.set_trace_reorder(reorder)
     dev = torch.device("cuda", dev_index)
     stream = torch.cuda.Stream(dev)
     for rays in (coherent, incoherent):
