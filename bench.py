@@ -822,6 +822,8 @@ def main() -> None:
         total_ms = float(x.item())
     ms_per_step = total_ms / args.steps
     rays_per_step = 2 * n_each
+    # the traversal kernel per set, and for a sorted set the key histogram, its scan and the scatter
+    launches_per_step = sum(1 + 3 * int(trace_tuned[name].get("trace_reorder", 0)) for name in set_names)
     value = rays_per_step * world / (ms_per_step * 1e-3) / 1e6
 
     # end to end through the C ABI with pinned host buffers
@@ -935,7 +937,7 @@ def main() -> None:
                         "path": "rgr_trace_closest on page-locked host arrays: the traversal kernel reads the rays "
                                 "and writes the hits across NVLink-C2C (zero copy)",
                         "staged_copies_value": round(e2e_staged, 1)},
-                "gpu_launches": 2 * args.steps, "roofline": roof, "cpu_baseline": cpu,
+                "gpu_launches": launches_per_step * args.steps, "roofline": roof, "cpu_baseline": cpu,
                 "parity": cpu["parity"] if cpu else None, "clocks": clocks,
                 "render": render, "bvh_build": bvh, "guiding": guide}
         print(json.dumps(line), flush=True)
