@@ -287,7 +287,11 @@ int rgr_trace_closest(rgr_context* c, const rgr_ray_soa* rays, uint64_t n, int32
 #define RGR_TRACE_HOST_AUTO 0
 #define RGR_TRACE_HOST_COPY 1
 int rgr_set_trace_host_mode(rgr_context* c, int32_t mode);
-/* device arrays in and out, enqueued on `stream` (cudaStream_t, NULL = context stream) */
+/* device arrays in and out, enqueued on `stream` (cudaStream_t, NULL = context stream).
+   The calls of one context share its work counter (and, with ray reordering, its sort
+   buffers): calls on different streams must not overlap.  A call that needs a larger
+   sort buffer than the context holds allocates it (cudaMalloc), so the first call of a
+   size with reordering on cannot be made under stream capture. */
 int rgr_trace_closest_device(rgr_context* c, const rgr_ray_soa* rays, uint64_t n, int32_t* prim, float* t,
                              float* ng_xyz, void* stream);
 
