@@ -137,6 +137,8 @@ def tune_trace(lane, ray_sets, stream: int, device: int = 0, reps: int = 3, use_
     st = torch.cuda.ExternalStream(stream)
 
     def run(p):
+        if p["trace_reorder"] and p["trace_stage"]:
+            return float("inf")  # the sorted rays' traversal stages no nodes
         lane.set_trace_reorder(p["trace_reorder"])
         lane.set_trace_staging(p["trace_stage"])
         lane.set_trace_tuning(p["trace_refill"], 0)
