@@ -68,8 +68,9 @@ class Autotuner:
         os.replace(tmp, self.cache_path)
 
     def tune(self, signature: str, run_trial, use_cache: bool = True, defaults: dict | None = None,
-             candidates: dict | None = None) -> dict:
-        """run_trial(params) -> seconds.  Returns the best params."""
+             candidates: dict | None = None, valid=None) -> dict:
+        """run_trial(params) -> seconds.  Returns the best params; `valid(params)`
+        False skips a combination without running it."""
         defaults = DEFAULTS if defaults is None else defaults
         candidates = CANDIDATES if candidates is None else candidates
         key = hashlib.sha1((_gpu_name(self.device) + "|" + signature).encode()).hexdigest()[:16]
@@ -85,6 +86,8 @@ class Autotuner:
                     continue
                 p = dict(best)
                 p[knob] = v
+                if valid is not None and not valid(p):
+                    continue
                 t = self._time(run_trial, p)
                 if t < best_t:
                     best, best_t = p, t
@@ -137,8 +140,6 @@ def tune_trace(lane, ray_sets, stream: int, device: int = 0, reps: int = 3, use_
     st = torch.cuda.ExternalStream(stream)
 
     def run(p):
-        if p["trace_reorder"] and p["trace_stage"]:
-            return float("inf")  # the sorted rays' traversal stages no nodes
         lane.set_trace_reorder(p["trace_reorder"])
         lane.set_trace_staging(p["trace_stage"])
         lane.set_trace_tuning(p["trace_refill"], 0)
@@ -155,7 +156,9 @@ def tune_trace(lane, ray_sets, stream: int, device: int = 0, reps: int = 3, use_
         return e0.elapsed_time(e1) * 1e-3 / reps
 
     tuner = Autotuner(device, log=log)
-    best = tuner.tune(sig, run, use_cache=use_cache, defaults=TRACE_DEFAULTS, candidates=TRACE_CANDIDATES)
+    # the sorted rays' traversal stages no nodes: no staging trials with sorting on
+    best = tuner.tune(sig, run, use_cache=use_cache, defaults=TRACE_DEFAULTS, candidates=TRACE_CANDIDATES,
+                      valid=lambda p: not (p["trace_reorder"] and p["trace_stage"]))
     lane.set_trace_reorder(best.get("trace_reorder", 0))
     lane.set_trace_staging(best["trace_stage"])
     lane.set_trace_tuning(best["trace_refill"], 0)
