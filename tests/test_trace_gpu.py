@@ -150,6 +150,30 @@ def test_ray_reorder(rg, po, n):
     assert (p0 == prim).all() and (bits(t0) == bits(t)).all()
 
 
+def test_ray_reorder_one_bucket(rg, po):
+    """70,000 rays with one key (the same origin, directions within a few
+    degrees) and a ragged tail of others: one bucket holds almost all rays,
+    warps count whole runs of equal keys at once."""
+    mesh = scenes.displaced_icosphere(6, seed=7)
+    sm, osc = build(mesh)
+    lane = rg.WavefrontLane(0, 1024)
+    lane.setup(sm)
+    lane.set_trace_reorder(1)
+    rng = np.random.default_rng(3)
+    n = 70000
+    o = np.tile(np.array([[0.0, 0.2, 3.0]], np.float32), (n, 1))
+    d = np.array([0.0, -0.05, -1.0]) + 0.02 * rng.standard_normal((n, 3))
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    tail = scenes.random_rays(77, (-1.0, -1.0, -1.0), (1.0, 1.0, 1.0), seed=4)
+    rays = scenes.Rays(np.concatenate([o, tail.o]).astype(np.float32), np.concatenate([d, tail.d]).astype(np.float32),
+                       np.concatenate([np.full(n, 3.4028235e38, np.float32), tail.tmax]))
+    prim, t = _device_hits(lane, rays)
+    oprim, ot, _ = osc.trace(rays.packed8(), threads=16)
+    assert (prim == oprim).all(), f"{(prim != oprim).sum()} prim mismatches"
+    assert (bits(t) == bits(ot)).all(), f"{(bits(t) != bits(ot)).sum()} t mismatches"
+    assert (prim[:n] >= 0).mean() > 0.5
+
+
 def test_ray_reorder_range(rg):
     lane = rg.WavefrontLane(0, 1024)
     for bad in (-1, 2):
