@@ -205,7 +205,7 @@ struct rgr_context {
     uint32_t trace_stage = 0;  // top BVH nodes staged in shared memory per CTA
     int trace_reorder = 0;     // rgr_trace_closest_device sorts the rays first
     int packed_grid = 0;       // its traversal grid (no staged nodes)
-    DevBuf tbins, tpacked;     // its bucket counts and the reordered 32-byte records
+    DevBuf tbins, trank, tpacked;  // its bucket counts, the rays' ranks, the reordered 32-byte records
     // learned path guiding: the attached network and this render's per-slot buffers
     rgr_guide* guide = nullptr;
     bool guided = false;      // the current render uses `guide`
@@ -770,6 +770,7 @@ int rgr_trace_closest_device(rgr_context* c, const rgr_ray_soa* rays, uint64_t n
     if (c->trace_reorder && n < (1ull << 32)) {
         if ((r = c->tbins.alloc(2 * sizeof(uint32_t) * kRayBins)) != RGR_OK) return r;
         if ((r = c->tpacked.alloc(32 * (size_t)n)) != RGR_OK) return r;
+        if ((r = c->trank.alloc(4 * (size_t)n)) != RGR_OK) return r;
         // the key's boxes: the scene's, and for the point half its diagonal along
         // the ray the same box widened by that reach
         RayKeyBox kb;
@@ -785,7 +786,8 @@ int rgr_trace_closest_device(rgr_context* c, const rgr_ray_soa* rays, uint64_t n
             kb.scale_far[k] = e + 2.0f * kb.reach > 0.0f ? 8.0f / (e + 2.0f * kb.reach) : 0.0f;
         }
         launch_ray_reorder(rays->ox, rays->oy, rays->oz, rays->dx, rays->dy, rays->dz, rays->tmax, n, kb,
-                           c->tbins.as<uint32_t>(), c->tpacked.as<float4>(), c->num_sms * 64, st);
+                           c->tbins.as<uint32_t>(), c->trank.as<uint32_t>(), c->tpacked.as<float4>(),
+                           c->num_sms * 64, st);
         launch_trace_packed(c->scene.sv, c->tpacked.as<float4>(), n, prim, t, ng_xyz, c->err.as<uint32_t>(),
                             c->tcounter.as<unsigned long long>(), c->trace_refill, c->trace_search, c->packed_grid,
                             st);

@@ -202,22 +202,38 @@ RGR_DEV void load_rays(const float* const* a, uint64_t i0, uint64_t n, int lane,
     }
 }
 
-__global__ void __launch_bounds__(256) k_ray_bins(RaySoA r, uint64_t n, RayKeyBox kb, uint32_t* __restrict__ bins) {
+// The counts of the keys, and each ray's rank among the rays of its key: the
+// run's atomic returns the rays of that key counted before it
+__global__ void __launch_bounds__(256) k_ray_bins(RaySoA r, uint64_t n, RayKeyBox kb, uint32_t* __restrict__ bins,
+                                                 uint32_t* __restrict__ rank) {
+    const unsigned full = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     const float* const a[6] = {r.ox, r.oy, r.oz, r.dx, r.dy, r.dz};
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x * kKeyRays;
     for (uint64_t i0 = ((uint64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31u)) * kKeyRays; i0 < n; i0 += stride) {
         float v[6][kKeyRays];
         load_rays<6, false>(a, i0, n, lane, v);
+        uint32_t base[kKeyRays];
+        int off[kKeyRays], head[kKeyRays];
 #pragma unroll
         for (int j = 0; j < kKeyRays; ++j) {
             const uint64_t left = n - (i0 + 32 * j);
             const int nvalid = i0 + 32 * j >= n ? 0 : (left >= 32 ? 32 : (int)left);
-            if (nvalid == 0) break;
+            base[j] = 0u;
+            head[j] = 0;
+            off[j] = -1;
+            if (nvalid == 0) continue;
             const uint32_t key = ray_key(kb, mk(v[0][j], v[1][j], v[2][j]), mk(v[3][j], v[4][j], v[5][j]));
-            int head, len;
-            key_run(key, lane, nvalid, head, len);
-            if (lane == head && lane < nvalid) atomicAdd(bins + key, (uint32_t)len);
+            int len;
+            key_run(key, lane, nvalid, head[j], len);
+            if (lane == head[j] && lane < nvalid) base[j] = atomicAdd(bins + key, (uint32_t)len);
+            if (lane < nvalid) off[j] = lane - head[j];
+        }
+        // the ranks, once the atomics of all kKeyRays rows are in flight
+#pragma unroll
+        for (int j = 0; j < kKeyRays; ++j) {
+            const uint32_t b = __shfl_sync(full, base[j], head[j]);
+            if (off[j] >= 0) rank[i0 + lane + 32 * j] = b + (uint32_t)off[j];
         }
     }
 }
@@ -267,41 +283,29 @@ __global__ void __launch_bounds__(1024) k_ray_bins_scan(const uint32_t* __restri
     reinterpret_cast<uint2*>(cursor)[1024 * blockIdx.x + threadIdx.x] = make_uint2(e, e + v.x);
 }
 
-// each ray's 32-byte record to the next place of its bucket (cursors: the
-// scanned counts)
+// each ray's 32-byte record to its place: the start of its key's bucket (the
+// scanned counts) plus its rank there
 __global__ void __launch_bounds__(256) k_ray_scatter(RaySoA r, uint64_t n, RayKeyBox kb,
-                                                    uint32_t* __restrict__ cursor, float4* __restrict__ packed) {
-    const unsigned full = 0xffffffffu;
+                                                    const uint32_t* __restrict__ start,
+                                                    const uint32_t* __restrict__ rank, float4* __restrict__ packed) {
     const int lane = threadIdx.x & 31;
     const float* const a[7] = {r.ox, r.oy, r.oz, r.dx, r.dy, r.dz, r.tmax};
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x * kKeyRays;
     for (uint64_t i0 = ((uint64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31u)) * kKeyRays; i0 < n; i0 += stride) {
         float v[7][kKeyRays];
         load_rays<7, true>(a, i0, n, lane, v);
-        uint32_t pos[kKeyRays];
 #pragma unroll
         for (int j = 0; j < kKeyRays; ++j) {
-            const uint64_t left = n - (i0 + 32 * j);
-            const int nvalid = i0 + 32 * j >= n ? 0 : (left >= 32 ? 32 : (int)left);
-            pos[j] = ~0u;
-            if (nvalid == 0) continue;
+            const uint64_t i = i0 + lane + 32 * j;
+            if (i >= n) continue;
             const uint32_t key = ray_key(kb, mk(v[0][j], v[1][j], v[2][j]), mk(v[3][j], v[4][j], v[5][j]));
-            int head, len;
-            key_run(key, lane, nvalid, head, len);
-            uint32_t base = 0;
-            if (lane == head && lane < nvalid) base = atomicAdd(cursor + key, (uint32_t)len);
-            base = __shfl_sync(full, base, head);
-            if (lane < nvalid) pos[j] = base + (uint32_t)(lane - head);
-        }
-#pragma unroll
-        for (int j = 0; j < kKeyRays; ++j) {
-            // pos < n always (both passes compute the same key); a lane past n has ~0
-            if (pos[j] >= n) continue;
-            float4* q = packed + 2 * (size_t)pos[j];
-            const uint32_t i = (uint32_t)(i0 + lane + 32 * j);
+            const uint32_t pos = __ldg(start + key) + __ldcs(rank + i);
+            // pos < n always (both passes compute the same key)
+            if (pos >= n) continue;
+            float4* q = packed + 2 * (size_t)pos;
             asm volatile("st.global.v8.f32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8};" ::"l"(q), "f"(v[0][j]),
                          "f"(v[1][j]), "f"(v[2][j]), "f"(v[6][j]), "f"(v[3][j]), "f"(v[4][j]), "f"(v[5][j]),
-                         "f"(__uint_as_float(i))
+                         "f"(__uint_as_float((uint32_t)i))
                          : "memory");
         }
     }
@@ -335,18 +339,18 @@ void launch_trace_rays_counts(const SceneView& sc, const float* ox, const float*
 
 void launch_ray_reorder(const float* ox, const float* oy, const float* oz, const float* dx, const float* dy,
                         const float* dz, const float* tmax, uint64_t n, const RayKeyBox& kb, uint32_t* bins,
-                        float4* packed, int grid, cudaStream_t st) {
+                        uint32_t* rank, float4* packed, int grid, cudaStream_t st) {
     if (n == 0) return;
     RaySoA r{ox, oy, oz, dx, dy, dz, tmax};
     // one pass of 256 x kKeyRays rays per block where the grid allows (the
     // block scheduler then overlaps one block's loads with another's work)
     const uint64_t tiles = (n + 256 * kKeyRays - 1) / (256 * kKeyRays);
     const int g = (int)std::min<uint64_t>(tiles, (uint64_t)grid);
-    uint32_t* cursor = bins + kRayBins;
+    uint32_t* start = bins + kRayBins;
     cudaMemsetAsync(bins, 0, sizeof(uint32_t) * kRayBins, st);
-    k_ray_bins<<<g, 256, 0, st>>>(r, n, kb, bins);
-    k_ray_bins_scan<<<kScanBlocks, 1024, 0, st>>>(bins, cursor);
-    k_ray_scatter<<<g, 256, 0, st>>>(r, n, kb, cursor, packed);
+    k_ray_bins<<<g, 256, 0, st>>>(r, n, kb, bins, rank);
+    k_ray_bins_scan<<<kScanBlocks, 1024, 0, st>>>(bins, start);
+    k_ray_scatter<<<g, 256, 0, st>>>(r, n, kb, start, rank, packed);
 }
 
 void launch_trace_packed(const SceneView& sc, const float4* packed, uint64_t n, int32_t* prim, float* t, float* ng,

@@ -275,10 +275,10 @@ struct RayKeyBox {
     float reach;
 };
 // counting sort of n < 2^32 rays into `packed` (32 bytes per ray); bins: 2 x kRayBins
-// words (counts, cursors); grid: the most blocks of the key passes
+// words (counts, bucket starts); rank: n words; grid: the most blocks of the key passes
 void launch_ray_reorder(const float* ox, const float* oy, const float* oz, const float* dx, const float* dy,
                         const float* dz, const float* tmax, uint64_t n, const RayKeyBox& kb, uint32_t* bins,
-                        float4* packed, int grid, cudaStream_t st);
+                        uint32_t* rank, float4* packed, int grid, cudaStream_t st);
 // closest hit of reordered records; hits written at each record's ray index
 void launch_trace_packed(const SceneView& sc, const float4* packed, uint64_t n, int32_t* prim, float* t, float* ng,
                          uint32_t* err, unsigned long long* counter, int refill, int search, int grid,
