@@ -358,11 +358,12 @@ int rgr_set_trace_staging(rgr_context* c, uint32_t staged_nodes);
 
 /* Ray reordering of rgr_trace_closest_device (no counterpart in the
    reference): reorder = 1 sorts the rays by a 16-bit key of their origin and
-   direction before the traversal (a counting sort on the device, 32 bytes of
-   scratch per ray), so that a warp's rays walk similar paths through the
-   tree; it pays for incoherent rays and costs more than it saves on coherent
-   ones (camera rays).  0 = off (default).  Results are identical either way;
-   the order only changes the schedule.  Chosen by the autotuner. */
+   direction before the traversal (a counting sort on the device, 36 bytes of
+   scratch per ray; calls of 2^32 rays or more are traced unsorted), so that a
+   warp's rays walk similar paths through the tree; it pays for incoherent rays
+   and costs more than it saves on coherent ones (camera rays).  0 = off
+   (default).  Results are identical either way; the order only changes the
+   schedule.  Chosen by the autotuner. */
 int rgr_set_trace_reorder(rgr_context* c, int32_t reorder);
 
 /* ---- learned path guiding (no counterpart in the reference) --------------
