@@ -43,6 +43,27 @@ def test_sphere_trace(rg, po):
         assert (prim >= 36).any()  # some sphere hits
 
 
+def test_sphere_trace_sorted(rg, po):
+    """Rays in device memory sorted by origin and direction before the
+    traversal: the same hits, sphere leaves included."""
+    import torch
+    sm, osc = _scene(rg, po)
+    lane = rg.WavefrontLane(0, 1024)
+    lane.setup(sm)
+    lane.set_trace_reorder(1)
+    rnd = scenes.random_rays(20000, (-1.0, 0.0, -1.0), (1.0, 2.0, 1.0), seed=8)
+    soa = [torch.from_numpy(a).cuda() for a in rnd.soa()]
+    prim = torch.empty(len(rnd), dtype=torch.int32, device="cuda")
+    t = torch.empty(len(rnd), dtype=torch.float32, device="cuda")
+    torch.cuda.synchronize()  # the context stream does not wait for torch's stream
+    lane.trace_closest_device([a.data_ptr() for a in soa], len(rnd), prim.data_ptr(), t.data_ptr())
+    lane.synchronize()
+    oprim, ot, _ = osc.trace(rnd.packed8())
+    p = prim.cpu().numpy()
+    assert (p == oprim).all() and (bits(t.cpu().numpy()) == bits(ot)).all()
+    assert (p >= 36).any()
+
+
 def test_sphere_render(rg, po):
     sm, osc = _scene(rg, po)
     cam = camera(scenes.cornell_camera(), 64, 64)

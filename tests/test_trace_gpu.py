@@ -204,8 +204,9 @@ def test_staged_top_levels(rg, po, stage):
 
 def test_lbvh_built_on_gpu(rg, po):
     """A linear BVH built on the GPU: hits bit-exact against the oracle on the
-    same tree; the same closest t as the SAH tree for every ray (the primitive
-    may differ only where two primitives tie at that t)."""
+    same tree (rays in their order and sorted first); the same closest t as the
+    SAH tree for every ray (the primitive may differ only where two primitives
+    tie at that t)."""
     mesh = scenes.displaced_icosphere(6, seed=7)
     sm = rg.SceneManager()
     sm.addMesh(mesh)
@@ -216,6 +217,11 @@ def test_lbvh_built_on_gpu(rg, po):
     prim_rays, rnd = scenes.closest_hit_rays(mesh, res=128, n_random=32768, seed=4)
     p1 = _check(lane, osc, prim_rays)
     p2 = _check(lane, osc, rnd)
+    lane.set_trace_reorder(1)  # the same hits with the rays sorted first
+    ps, ts = _device_hits(lane, rnd)
+    lane.set_trace_reorder(0)
+    _, ot, _ = osc.trace(rnd.packed8(), threads=16, normals=False)
+    assert (ps == p2).all() and (bits(ts) == bits(ot)).all()
     info = sm.info()
     assert info.depth <= 63 and info.num_leaves > 0
     sah, _ = build(mesh, leaf=4)
