@@ -916,8 +916,9 @@ __global__ void __launch_bounds__(256, 5) k_trace_paths(PathsView P, QueueView Q
             if (s.prim >= 0) {
                 const f3 ng = hit_normal(*scp, s.prim, s.ro, s.rd, s.tmin);
                 P.ng[slot] = f4(ng, __int_as_float(s.prim));
-                P.ro[slot] = f4(s.ro, s.tmin);
-                P.rd[slot] = f4(s.rd, __int_as_float(-1));
+                // the ray's whole sector in one store: two 16-byte stores to a line
+                // that is not in L2 each cost a read of the sector from DRAM
+                st_sector<0>(P, slot, f4(s.ro, s.tmin), f4(s.rd, __int_as_float(-1)));
             }
             slot = ~0u;
         }
