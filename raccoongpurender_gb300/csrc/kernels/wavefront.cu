@@ -914,11 +914,11 @@ __global__ void __launch_bounds__(256, 5) k_trace_paths(PathsView P, QueueView Q
                                                    pol);
         if (slot != ~0u && s.link == kDone) {
             if (s.prim >= 0) {
-                const f3 ng = hit_normal(*scp, s.prim, s.ro, s.rd, s.tmin);
-                P.ng[slot] = f4(ng, __int_as_float(s.prim));
-                // the ray's whole sector in one store: two 16-byte stores to a line
-                // that is not in L2 each cost a read of the sector from DRAM
-                st_sector<0>(P, slot, f4(s.ro, s.tmin), f4(s.rd, __int_as_float(-1)));
+                // the ray's whole sector in one store (a partial store to a line that is
+                // not in L2 costs a read of the sector from DRAM); the hit primitive
+                // rides where the volume-hit id goes (-1 after a surface hit): the logic
+                // kernel computes the normal and restores -1
+                st_sector<0>(P, slot, f4(s.ro, s.tmin), f4(s.rd, __int_as_float(-2 - s.prim)));
             }
             slot = ~0u;
         }
@@ -948,6 +948,12 @@ RGR_DEV int logic_slot(const PathsView& P, const QueueView& Q, const RenderParam
     int32_t hs;
     if (kPreTraced) {
         hs = __float_as_int(ng4.w);
+        if (hv <= -2) {  // k_trace_paths found primitive -2 - hv
+            hs = -2 - hv;
+            hv = -1;
+            ng4 = f4(hit_normal(sc, hs, xyz(ro4), rd, ro4.w), __int_as_float(hs));
+            st_sector<0>(P, slot, ro4, f4(rd, __int_as_float(-1)));
+        }
     } else {
         // extension_ray_cast (extension_ray_cast_stackless.cl:202-246)
         f3 ro = xyz(ro4);
