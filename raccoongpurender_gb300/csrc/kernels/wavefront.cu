@@ -239,10 +239,16 @@ RGR_DEV void shade_slot(const RequestD& rq, const PathsView& P, int k, uint32_t 
     // the ray's sector and the (ng, rng) sector, each in one access; (T, L) likewise
     ld_sector<0>(P, slot, ro4, rd4);
     ld_sector<2>(P, slot, ng4, rng4);
+    int vcount = 0;
     if (!fresh) {
         ld_sector<1>(P, slot, T4, L4);
-        vb = P.vb[slot];
-        if (k == kMatVolume || vb.w > 0) va = P.va[slot];
+        vcount = vcount_of(__float_as_uint(L4.w));
+        if (k == kMatVolume || vcount > 0) {
+            float4 a, b;
+            ld_sector<3>(P, slot, a, b);
+            va = make_int4(__float_as_int(a.x), __float_as_int(a.y), __float_as_int(a.z), __float_as_int(a.w));
+            vb = make_int4(__float_as_int(b.x), __float_as_int(b.y), __float_as_int(b.z), __float_as_int(b.w));
+        }
     } else {
         ro4 = ng4 = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     }
@@ -253,7 +259,6 @@ RGR_DEV void shade_slot(const RequestD& rq, const PathsView& P, int k, uint32_t 
     int32_t hs = __float_as_int(ng4.w);
     uint32_t pixel = __float_as_uint(T4.w);
     uint32_t logic_i = 0;
-    int vcount = vb.w;
 
     if (k == 0) {  // new_path (new_path.cl:17-83)
         const CameraD& cam = rq.cam;
@@ -544,9 +549,11 @@ RGR_DEV void shade_slot(const RequestD& rq, const PathsView& P, int k, uint32_t 
     // guided renders (the training records carry it).
     const bool touch_L = fresh || kGuided || shLe.x != 0.0f || shLe.y != 0.0f || shLe.z != 0.0f ||
                          !is_finite(T.x) || !is_finite(T.y) || !is_finite(T.z);
-    if (touch_L && !fresh) {
+    // the volume stage changes the volume count, which L.w carries
+    const bool store_L = touch_L || k == kMatVolume;
+    if (store_L && !fresh) {
         L = xyz(L4);
-        logic_i = __float_as_uint(L4.w);
+        logic_i = depth_of(__float_as_uint(L4.w));
     }
     L = L + T * shLe;
     T = T * shT;
@@ -585,16 +592,15 @@ RGR_DEV void shade_slot(const RequestD& rq, const PathsView& P, int k, uint32_t 
         tmin = -1.0f / vol.w * log_(u);
     }
     st_sector<0>(P, slot, f4(ro, tmin), f4(rd, __int_as_float(hv)));
-    if (touch_L)
-        st_sector<1>(P, slot, f4(T, __uint_as_float(pixel)), f4(L, __uint_as_float(logic_i)));
-    else
+    if (store_L)  // a new path's count is 0; its list keeps the stale ids
+        st_sector<1>(P, slot, f4(T, __uint_as_float(pixel)), f4(L, __uint_as_float(depth_word(logic_i, vcount))));
+    else  // the sector was read above: this half store finds it in L2
         P.T[slot] = f4(T, __uint_as_float(pixel));
     if (k == kMatVolume) {
         vb.w = vcount;
-        P.va[slot] = va;
-        P.vb[slot] = vb;
-    } else if (fresh) {
-        reinterpret_cast<int*>(&P.vb[slot])[3] = 0;  // an empty list; the stale entries stay
+        st_sector<3>(P, slot,
+                     make_float4(__int_as_float(va.x), __int_as_float(va.y), __int_as_float(va.z), __int_as_float(va.w)),
+                     make_float4(__int_as_float(vb.x), __int_as_float(vb.y), __int_as_float(vb.z), __int_as_float(vb.w)));
     }
     st_sector<2>(P, slot, f4(Ng, __int_as_float(hs)), rng_bits(rng));
 }
@@ -771,7 +777,7 @@ __global__ void __launch_bounds__(256) k_guide_select(PathsView P, QueueView Q, 
         bool take = false;
         if (gi < n) {
             slot = guided_item_slot(Q, gi);
-            take = __float_as_uint(P.L[slot].w) <= gd.max_depth;
+            take = depth_of(__float_as_uint(P.L[slot].w)) <= gd.max_depth;
         }
         const unsigned m = __ballot_sync(0xffffffffu, take);
         uint32_t first = 0;
@@ -969,7 +975,8 @@ RGR_DEV int logic_slot(const PathsView& P, const QueueView& Q, const RenderParam
     }
     // logic (logic.cl:27-190)
     f3 T = xyz(T4), L = xyz(L4);
-    uint32_t logic_i = __float_as_uint(L4.w);
+    const uint32_t lw = __float_as_uint(L4.w);  // segment count and volume count
+    uint32_t logic_i = depth_of(lw);
     Rng rng = rng_of_bits(rng4);
     bool evalEnv = false, newPath = false;
     if (hs < 0 && hv < 0) {
@@ -1017,7 +1024,7 @@ RGR_DEV int logic_slot(const PathsView& P, const QueueView& Q, const RenderParam
         const bool kept = is_finite(L.x) && is_finite(L.y) && is_finite(L.z) && L.x < cl && L.y < cl && L.z < cl;
         guide_offer(rp.gd, slot, L, newPath && kept, go);
     }
-    st_sector<1>(P, slot, f4(T, T4.w), f4(L, __uint_as_float(logic_i + 1)));
+    st_sector<1>(P, slot, f4(T, T4.w), f4(L, __uint_as_float(depth_word(logic_i + 1, vcount_of(lw)))));
     st_sector<2>(P, slot, ng4, rng_bits(rng));
     int q;
     if (newPath) {
@@ -1211,7 +1218,7 @@ __global__ void k_debug_slots(PathsView P, uint32_t* out) {
     int4 va = P.va[i], vb = P.vb[i];
     const float f[12] = {T.x, T.y, T.z, L.x, L.y, L.z, ro.x, ro.y, ro.z, rd.x, rd.y, rd.z};
     for (int k = 0; k < 12; ++k) o[k] = __float_as_uint(f[k]);
-    o[12] = __float_as_uint(L.w);
+    o[12] = depth_of(__float_as_uint(L.w));
     o[13] = __float_as_uint(T.w);
     o[14] = r.x;
     o[15] = r.y;
@@ -1225,7 +1232,7 @@ __global__ void k_debug_slots(PathsView P, uint32_t* out) {
     o[23] = __float_as_uint(ng.z);
     uint8_t q = P.qid[i];
     o[24] = q == kQueueIdle ? 0xffffffffu : (uint32_t)q;
-    o[25] = (uint32_t)vb.w;
+    o[25] = (uint32_t)vcount_of(__float_as_uint(L.w));
     const int v[7] = {va.x, va.y, va.z, va.w, vb.x, vb.y, vb.z};
     for (int k = 0; k < 7; ++k) o[26 + k] = (uint32_t)v[k];
     o[33] = 0;

@@ -75,6 +75,16 @@ __device__ __forceinline__ void st_sector(const PathsView& P, uint32_t slot, con
                  "f"(a.w), "f"(b.x), "f"(b.y), "f"(b.z), "f"(b.w)
                  : "memory");
 }
+// L.w of a slot record: the path's segment count (logic_i, low 24 bits) and the
+// number of volumes it is inside (high 8 bits; their ids are the record's last
+// sector), so that a stage that reads (T, L) knows without reading the list
+// whether it needs it
+constexpr uint32_t kDepthMask = 0x00ffffffu;
+__device__ __forceinline__ uint32_t depth_of(uint32_t w) { return w & kDepthMask; }
+__device__ __forceinline__ int vcount_of(uint32_t w) { return (int)(w >> 24); }
+__device__ __forceinline__ uint32_t depth_word(uint32_t depth, int vcount) {
+    return (depth & kDepthMask) | ((uint32_t)vcount << 24);
+}
 __device__ __forceinline__ float4 rng_bits(const Rng& r) {
     return make_float4(__uint_as_float(r.s0), __uint_as_float(r.s1), __uint_as_float(r.s2), __uint_as_float(r.s3));
 }
