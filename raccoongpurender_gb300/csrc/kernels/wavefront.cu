@@ -922,8 +922,9 @@ __global__ void __launch_bounds__(256, 5) k_trace_paths(PathsView P, QueueView Q
             if (s.prim >= 0) {
                 // the ray's whole sector in one store (a partial store to a line that is
                 // not in L2 costs a read of the sector from DRAM); the hit primitive
-                // rides where the volume-hit id goes (-1 after a surface hit): the logic
-                // kernel computes the normal and restores -1
+                // rides where the volume-hit id goes (none after a surface hit: every
+                // reader takes a negative id as none), and the logic kernel, which
+                // writes the (ng, rng) sector anyway, computes the normal
                 st_sector<0>(P, slot, f4(s.ro, s.tmin), f4(s.rd, __int_as_float(-2 - s.prim)));
             }
             slot = ~0u;
@@ -958,7 +959,6 @@ RGR_DEV int logic_slot(const PathsView& P, const QueueView& Q, const RenderParam
             hs = -2 - hv;
             hv = -1;
             ng4 = f4(hit_normal(sc, hs, xyz(ro4), rd, ro4.w), __int_as_float(hs));
-            st_sector<0>(P, slot, ro4, f4(rd, __int_as_float(-1)));
         }
     } else {
         // extension_ray_cast (extension_ray_cast_stackless.cl:202-246)
@@ -1225,7 +1225,7 @@ __global__ void k_debug_slots(PathsView P, uint32_t* out) {
     o[16] = r.z;
     o[17] = r.w;
     o[18] = __float_as_uint(ng.w);
-    o[19] = __float_as_uint(rd.w);
+    o[19] = __float_as_int(rd.w) < -1 ? 0xffffffffu : __float_as_uint(rd.w);  // no volume hit: -1
     o[20] = __float_as_uint(ro.w);
     o[21] = __float_as_uint(ng.x);
     o[22] = __float_as_uint(ng.y);
