@@ -902,7 +902,9 @@ __global__ void __launch_bounds__(256, 5) k_trace_paths(PathsView P, QueueView Q
 #pragma unroll
                     for (int j = 1; j < kNumQueues; ++j) k += ((uint32_t)i >= off[j]) ? 1 : 0;
                     const uint32_t r = queue_items(Q, k)[(uint32_t)i - pick(off, k)];
-                    if (P.qid[r] != kQueueIdle) {
+                    // only a new-path item can have retired (sample budget reached in
+                    // the shading kernel): material-queue items skip the check
+                    if (k != 0 || P.qid[r] != kQueueIdle) {
                         slot = r;
                         scp = &rp.reqs[P.req[r]].sc;
                         float4 ro4, rd4;
