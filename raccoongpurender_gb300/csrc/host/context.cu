@@ -314,7 +314,7 @@ struct rgr_context {
         const size_t n = (size_t)ntiles * kTile;
         int r;
         if ((r = globes.alloc(16 * kGuideMixVecs * n)) != RGR_OK) return r;
-        if ((r = grecords.alloc(16 * 5 * kGuideRecords * n)) != RGR_OK) return r;
+        if ((r = grecords.alloc(16 * kGuideRecordVecs * kGuideRecords * n)) != RGR_OK) return r;
         if ((r = gnrec.alloc(n)) != RGR_OK) return r;
         if (guide->cfg.max_depth) {
             if ((r = gsel.alloc(4 * n)) != RGR_OK) return r;

@@ -565,12 +565,11 @@ RGR_DEV void shade_slot(const RequestD& rq, const PathsView& P, int k, uint32_t 
         if (r < (uint32_t)kGuideRecords) {
             const float c = (hs >= 0) ? fmax_(dot(is.wi, gn), 0.0f) : 1.0f;
             const float cp = c / incident_pdf<kGuided>(is);
-            float4* rec = gd.records + ((size_t)slot * kGuideRecords + r) * 5;
-            rec[0] = make_float4(gx.x, gx.y, gx.z, gn.x);
-            rec[1] = make_float4(gn.y, gn.z, wo_in.x, wo_in.y);
-            rec[2] = make_float4(wo_in.z, is.wi.x, is.wi.y, is.wi.z);
-            rec[3] = make_float4(L.x, L.y, L.z, T.x);
-            rec[4] = make_float4(T.y, T.z, cp, is.pdf0);  // pdf0: the BSDF (phase) pdf of wi
+            float4* rec = gd.records + ((size_t)slot * kGuideRecords + r) * kGuideRecordVecs;
+            st_v8(rec, make_float4(L.x, L.y, L.z, T.x),
+                  make_float4(T.y, T.z, cp, is.pdf0));  // pdf0: the BSDF (phase) pdf of wi
+            st_v8(rec + 2, make_float4(gx.x, gx.y, gx.z, gn.x), make_float4(gn.y, gn.z, wo_in.x, wo_in.y));
+            st_v8(rec + 4, make_float4(wo_in.z, is.wi.x, is.wi.y, is.wi.z), make_float4(0.0f, 0.0f, 0.0f, 0.0f));
             gd.nrec[slot] = (uint8_t)(r + 1);
         }
     }
@@ -825,8 +824,9 @@ RGR_DEV void guide_offer(const GuideRenderD& gd, uint32_t slot, f3 L, bool endin
     const uint32_t it = *tr.iter;
     for (uint32_t r = 0; r < (uint32_t)kGuideRecords; ++r) {
         if (r >= nr) continue;
-        const float4* rec = gd.records + ((size_t)slot * kGuideRecords + r) * 5;
-        const float4 d = rec[3], e = rec[4];
+        const float4* rec = gd.records + ((size_t)slot * kGuideRecords + r) * kGuideRecordVecs;
+        float4 d, e;
+        ld_v8(rec, d, e);
         const float lx = d.w > 0.0f ? (L.x - d.x) / d.w : 0.0f;
         const float ly = e.x > 0.0f ? (L.y - d.y) / e.x : 0.0f;
         const float lz = e.y > 0.0f ? (L.z - d.z) / e.y : 0.0f;
@@ -847,12 +847,13 @@ RGR_DEV float guide_write(const GuideRenderD& gd, uint32_t slot, const GuideOffe
     for (uint32_t r = 0; r < (uint32_t)kGuideRecords; ++r) {
         if (!((o.take >> r) & 1u)) continue;
         if (idx < tr.cap) {
-            const float4* rec = gd.records + ((size_t)slot * kGuideRecords + r) * 5;
-            float4* dst = reinterpret_cast<float4*>(tr.samples + 16 * (size_t)idx);
-            dst[0] = rec[0];  // x, n.x
-            dst[1] = rec[1];  // n.yz, wo.xy
-            dst[2] = rec[2];  // wo.z, wi
-            dst[3] = make_float4(o.w[r], rec[4].w, 0.0f, 0.0f);  // weight, BSDF pdf of wi
+            const float4* rec = gd.records + ((size_t)slot * kGuideRecords + r) * kGuideRecordVecs;
+            float4* dst = reinterpret_cast<float4*>(tr.samples + 16 * (size_t)idx);  // 64 bytes
+            float4 x, n, wi, d;
+            ld_v8(rec + 2, x, n);
+            ld_v8(rec + 4, wi, d);
+            st_v8(dst, x, n);                                                // x, n.x | n.yz, wo.xy
+            st_v8(dst + 2, wi, make_float4(o.w[r], rec[1].w, 0.0f, 0.0f));  // wo.z, wi | weight, BSDF pdf of wi
             wsum += o.w[r];
         }
         ++idx;
@@ -865,9 +866,10 @@ RGR_DEV float guide_write(const GuideRenderD& gd, uint32_t slot, const GuideOffe
 // shading kernel reads them, less the new-path slots it retired — by
 // persistent warps that hand finished lanes the next items (one atomic per
 // refill per warp), as the closest-hit service kernel does with rays.  Runs
-// between the shading kernel and the queue resets.  A hit writes Ng and the
-// primitive into P.ng, t into P.ro.w and clears the volume hit in P.rd.w; a
-// miss leaves P.ng.w at the -1 the shading stage wrote.  Each slot may belong
+// between the shading kernel and the queue resets.  A hit writes the ray's
+// sector once: t into P.ro.w and the primitive, as -2 - prim, into the volume-hit
+// field P.rd.w (its readers take a negative id as none); the logic kernel computes
+// Ng into P.ng.  A miss leaves P.ng.w at the -1 the shading stage wrote.  Each slot may belong
 // to another request (scene).
 __global__ void __launch_bounds__(256, 5) k_trace_paths(PathsView P, QueueView Q, RenderParams rp,
                                                          unsigned long long* next, int refill, int search) {

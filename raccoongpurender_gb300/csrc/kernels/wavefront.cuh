@@ -68,6 +68,18 @@ __device__ __forceinline__ void ld_sector(const PathsView& P, uint32_t slot, flo
         : "l"(p)
         : "memory");
 }
+// two float4 at a 32-byte aligned address in one 32-byte access
+__device__ __forceinline__ void ld_v8(const float4* p, float4& a, float4& b) {
+    asm("ld.global.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+        : "=f"(a.x), "=f"(a.y), "=f"(a.z), "=f"(a.w), "=f"(b.x), "=f"(b.y), "=f"(b.z), "=f"(b.w)
+        : "l"(p)
+        : "memory");
+}
+__device__ __forceinline__ void st_v8(float4* p, const float4& a, const float4& b) {
+    asm volatile("st.global.v8.f32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8};" ::"l"(p), "f"(a.x), "f"(a.y), "f"(a.z),
+                 "f"(a.w), "f"(b.x), "f"(b.y), "f"(b.z), "f"(b.w)
+                 : "memory");
+}
 template <int kSector>
 __device__ __forceinline__ void st_sector(const PathsView& P, uint32_t slot, const float4& a, const float4& b) {
     float4* p = P.ro.base + (size_t)slot * kSlotVecs + 2 * kSector;
@@ -176,6 +188,11 @@ struct GuideTrainD {
 };
 constexpr uint32_t kLossHist = 4096;
 constexpr int kGuideRecords = 3;   // training records kept per path (its first guided vertices)
+// A training record: three whole 32-byte sectors (a partial store to a line that
+// is not in L2 costs a read of the sector from DRAM): (L, T.x) (T.yz, cos/pdf,
+// BSDF pdf) | (x, n.x) (n.yz, wo.xy) | (wo.z, wi) (unused).  The first sector is
+// what the logic kernel reads of every record of an ending path.
+constexpr int kGuideRecordVecs = 6;
 constexpr int kGuideMixVecs = 5;    // 16-byte words per inferred mixture: 8 x FP16 (mean xyz, kappa) + 8 FP16 weights
 
 // training still wanted (iteration budget not used up)
@@ -186,7 +203,7 @@ __device__ __forceinline__ bool guide_training_open(const GuideTrainD& t) {
 // per-render guiding state the wavefront kernels read
 struct GuideRenderD {
     uint4* lobes;         // kGuideMixVecs per guided queue item of this bounce
-    float4* records;      // per slot kGuideRecords x 5 float4
+    float4* records;      // per slot kGuideRecords x kGuideRecordVecs float4
     uint8_t* nrec;        // records written on the slot's current path
     GuideTrainD train;
     float guide_frac;     // share of the non-envmap selection probability given to the guide (learn_frac = 0)
