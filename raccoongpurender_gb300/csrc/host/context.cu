@@ -26,7 +26,7 @@ namespace {
 // (SceneManager::createBuffer / createMaterialBuffer / createEnvmapBuffer,
 // scene_manager.hpp:579-650).
 struct DeviceScene {
-    DevBuf nodes, prims, points, indices, spheres, materials, lambertians, wards, volumes;
+    DevBuf nodes, prims, points, indices, spheres, materials, lambertians, wards, volumes, tri_normals;
     DevBuf env_rgba, env_pdf, env_alias, env_frag;
     SceneView sv{};
     bool valid = false;
@@ -104,6 +104,13 @@ struct DeviceScene {
         for (int k = 0; k < 6; ++k) small = small && std::fabs(b.bounds[k]) <= 1.0e30f;
         v.small_coords = small ? 1 : 0;
         v.num_nodes = (uint32_t)b.nodes.size();
+        // the hit normals, computed once here by the kernels' own function
+        v.tri_normals = nullptr;
+        if ((r = tri_normals.alloc(16 * std::max<size_t>(ntri, 1))) != RGR_OK) return r;
+        launch_tri_normals(v, (uint32_t)ntri, tri_normals.as<float4>(), st);
+        RGR_CUDA(cudaGetLastError());
+        RGR_CUDA(cudaStreamSynchronize(st));  // calls on other streams read the table
+        v.tri_normals = ntri ? tri_normals.as<float4>() : nullptr;
         valid = true;
         return RGR_OK;
     }

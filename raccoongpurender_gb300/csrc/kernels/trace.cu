@@ -337,6 +337,19 @@ void launch_trace_rays_counts(const SceneView& sc, const float* ox, const float*
     k_trace_rays<true, false><<<grid, kStackThreads, 0, st>>>(sc, b);
 }
 
+// the per-triangle normal table of a scene (its tri_normals still null)
+__global__ void k_tri_normals(SceneView sc, uint32_t ntri, float4* __restrict__ out) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= ntri) return;
+    const f3 n = triangle_normal(sc, (int32_t)i);
+    out[i] = make_float4(n.x, n.y, n.z, 0.0f);
+}
+
+void launch_tri_normals(const SceneView& sc, uint32_t ntri, float4* out, cudaStream_t st) {
+    if (ntri == 0) return;
+    k_tri_normals<<<(ntri + 255) / 256, 256, 0, st>>>(sc, ntri, out);
+}
+
 void launch_ray_reorder(const float* ox, const float* oy, const float* oz, const float* dx, const float* dy,
                         const float* dz, const float* tmax, uint64_t n, const RayKeyBox& kb, uint32_t* bins,
                         uint32_t* rank, float4* packed, int grid, cudaStream_t st) {

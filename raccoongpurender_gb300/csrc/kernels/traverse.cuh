@@ -341,13 +341,16 @@ RGR_DEV int32_t trace_closest(const SceneView& sc, f3 ro, f3 rd, float& tmin, Tr
 
 // geometric normal of a hit (extension_ray_cast_stackless.cl:224-239), from
 // the original vertices so the subtractions match the reference exactly
+RGR_DEV f3 triangle_normal(const SceneView& sc, int32_t prim) {
+    const uint32_t i0 = __ldg(sc.indices + 3 * (size_t)prim), i1 = __ldg(sc.indices + 3 * (size_t)prim + 1),
+                   i2 = __ldg(sc.indices + 3 * (size_t)prim + 2);
+    f3 v0 = xyz(__ldg(sc.points + i0)), v1 = xyz(__ldg(sc.points + i1)), v2 = xyz(__ldg(sc.points + i2));
+    return normalize(cross(v2 - v1, v1 - v0));
+}
+// a triangle's normal comes from the per-triangle table the upload fills with
+// triangle_normal (one gather instead of the indices, then the points)
 RGR_DEV f3 hit_normal(const SceneView& sc, int32_t prim, f3 ro, f3 rd, float t) {
-    if (prim < sc.sphere_begin) {
-        const uint32_t i0 = __ldg(sc.indices + 3 * (size_t)prim), i1 = __ldg(sc.indices + 3 * (size_t)prim + 1),
-                       i2 = __ldg(sc.indices + 3 * (size_t)prim + 2);
-        f3 v0 = xyz(__ldg(sc.points + i0)), v1 = xyz(__ldg(sc.points + i1)), v2 = xyz(__ldg(sc.points + i2));
-        return normalize(cross(v2 - v1, v1 - v0));
-    }
+    if (prim < sc.sphere_begin) return sc.tri_normals ? xyz(__ldg(sc.tri_normals + prim)) : triangle_normal(sc, prim);
     float4 s = __ldg(sc.spheres + (prim - sc.sphere_begin));
     return normalize((ro + rd * t) - xyz(s));
 }

@@ -292,6 +292,8 @@ void launch_trace_rays_counts(const SceneView& sc, const float* ox, const float*
                               int grid, cudaStream_t st);
 // resident 256-thread blocks per SM of the closest-hit kernel with `stage` staged nodes
 int trace_rays_max_blocks_per_sm(uint32_t stage = 0);
+// the per-triangle normal table (ntri float4) of a scene whose tri_normals is null
+void launch_tri_normals(const SceneView& sc, uint32_t ntri, float4* out, cudaStream_t st);
 // Ray reordering: a 16-bit key per ray from its origin and the point `reach`
 // along it, each quantised to 3 bits per axis: (x - lo) * scale in [0, 8)
 constexpr int kRayKeyBits = 16;
