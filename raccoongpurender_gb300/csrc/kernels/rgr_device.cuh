@@ -78,7 +78,8 @@ struct SceneView {
     uint32_t num_prims;       // 0 = empty scene
     const float4* points;     // original vertices (Ng of the hit)
     const uint32_t* indices;  // 3 per triangle
-    const float4* tri_normals;  // per triangle, as hit_normal computes it from the points (or null)
+    const float4* tri_normals;  // per triangle: the normal as hit_normal computes it from the points,
+                                // and in w its material type (or null)
     const float4* spheres;    // center, radius
     int32_t sphere_begin;
     // materials

@@ -337,12 +337,13 @@ void launch_trace_rays_counts(const SceneView& sc, const float* ox, const float*
     k_trace_rays<true, false><<<grid, kStackThreads, 0, st>>>(sc, b);
 }
 
-// the per-triangle normal table of a scene (its tri_normals still null)
+// the per-triangle table of a scene (its tri_normals still null): the normal,
+// and in w the triangle's material type (the queue of its next stage)
 __global__ void k_tri_normals(SceneView sc, uint32_t ntri, float4* __restrict__ out) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= ntri) return;
     const f3 n = triangle_normal(sc, (int32_t)i);
-    out[i] = make_float4(n.x, n.y, n.z, 0.0f);
+    out[i] = make_float4(n.x, n.y, n.z, __int_as_float(__ldg(sc.materials + i).x));
 }
 
 void launch_tri_normals(const SceneView& sc, uint32_t ntri, float4* out, cudaStream_t st) {

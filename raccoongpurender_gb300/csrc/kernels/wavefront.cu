@@ -957,12 +957,19 @@ RGR_DEV int logic_slot(const PathsView& P, const QueueView& Q, const RenderParam
     int32_t hv = __float_as_int(rd4.w);
     uint32_t err = 0;
     int32_t hs;
+    int mtype = -1;  // the hit triangle's material type, where the triangle table gave it
     if (kPreTraced) {
         hs = __float_as_int(ng4.w);
         if (hv <= -2) {  // k_trace_paths found primitive -2 - hv
             hs = -2 - hv;
             hv = -1;
-            ng4 = f4(hit_normal(sc, hs, xyz(ro4), rd, ro4.w), __int_as_float(hs));
+            if (sc.tri_normals && hs < sc.sphere_begin) {
+                const float4 tn = __ldg(sc.tri_normals + hs);
+                ng4 = f4(xyz(tn), __int_as_float(hs));
+                mtype = __float_as_int(tn.w);
+            } else {
+                ng4 = f4(hit_normal(sc, hs, xyz(ro4), rd, ro4.w), __int_as_float(hs));
+            }
         }
     } else {
         // extension_ray_cast (extension_ray_cast_stackless.cl:202-246)
@@ -1034,7 +1041,7 @@ RGR_DEV int logic_slot(const PathsView& P, const QueueView& Q, const RenderParam
     if (newPath) {
         q = 0;
     } else if (0 <= hs) {
-        q = __ldg(sc.materials + hs).x;
+        q = mtype >= 0 ? mtype : __ldg(sc.materials + hs).x;
     } else {
         q = kMatVolumeInside;
     }
