@@ -8,6 +8,8 @@ Knobs (all results are bit-identical across knob values; only speed changes):
                      when this many lanes are idle;
   * render_search  — that kernel's warps take node steps while this many
                      lanes still search for their next leaf;
+  * trace_reorder  — the closest-hit call sorts its rays by origin and
+                     direction first (pays for incoherent rays);
   * trace_refill   — refill a closest-hit warp with new rays when this many
                      lanes are idle;
   * trace_search   — the same leaf batching for the closest-hit kernel;
