@@ -1079,7 +1079,10 @@ template <bool kGuided, bool kPreTraced>
 // latency-bound: 6 resident blocks per SM for the logic alone (40 registers; the
 // render 0.6 % faster than at 5), 5 while it records guide samples, 4 with the
 // traversal fused in
-__global__ void __launch_bounds__(kLogicThreads, kPreTraced ? (kGuided ? 5 : 6) : 4) k_trace_logic(PathsView P, QueueView Q, RenderParams rp) {
+#ifndef RGR_LOGIC_MIN_BLOCKS  // the plain pre-traced logic: 5 / 6 / 7 give 1464 / 1472 / 1436 Mpaths/s
+#define RGR_LOGIC_MIN_BLOCKS 6
+#endif
+__global__ void __launch_bounds__(kLogicThreads, kPreTraced ? (kGuided ? 5 : RGR_LOGIC_MIN_BLOCKS) : 4) k_trace_logic(PathsView P, QueueView Q, RenderParams rp) {
     const unsigned full = 0xffffffffu;
     __shared__ uint32_t s_q[kNumQueues];  // items per queue, then the block's base in it
     __shared__ uint32_t s_samples, s_offered;  // guided recording: accepted samples (then their base), offered
