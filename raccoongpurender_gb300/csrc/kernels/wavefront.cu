@@ -871,7 +871,10 @@ RGR_DEV float guide_write(const GuideRenderD& gd, uint32_t slot, const GuideOffe
 // field P.rd.w (its readers take a negative id as none); the logic kernel computes
 // Ng into P.ng.  A miss leaves P.ng.w at the -1 the shading stage wrote.  Each slot may belong
 // to another request (scene).
-__global__ void __launch_bounds__(256, 5) k_trace_paths(PathsView P, QueueView Q, RenderParams rp,
+#ifndef RGR_TRACE_PATHS_MIN_BLOCKS  // 4 / 5 / 6 (64 / 48 / 40 registers, 6 spilling): 1428 / 1473 / 1442 Mpaths/s
+#define RGR_TRACE_PATHS_MIN_BLOCKS 5
+#endif
+__global__ void __launch_bounds__(256, RGR_TRACE_PATHS_MIN_BLOCKS) k_trace_paths(PathsView P, QueueView Q, RenderParams rp,
                                                          unsigned long long* next, int refill, int search) {
     const unsigned full = 0xffffffffu;
     const int lane = threadIdx.x & 31;
